@@ -1,0 +1,104 @@
+/* CPU oracle for the partial-assembly H1 path: a plain-C restatement of the
+ * reference's algorithms, used ONLY as the checker by tests/, by smoke() and by
+ * bench.py's CPU-baseline leg. It is never linked into or called by the GPU
+ * library. Every function cites the reference file:line it restates.
+ *
+ * Layouts are the reference's column-major ones:
+ *   B, G        (Q, D)            B[q + Q*d]
+ *   W           (Q, Q, Q)
+ *   J           (Q, Q, Q, 3, 3, NE)  J[q + Q3*(row + 3*(col + 3*e))]
+ *   qdata diff  (Q, Q, Q, S, NE)  S = 6 (symmetric) or 9
+ *   qdata mass  (Q, Q, Q, NE)
+ *   E-vector    (D, D, D, NE)
+ */
+#ifndef GBPA_ORACLE_H
+#define GBPA_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* fem/restriction.cpp:26-114 (vdim = 1) */
+void or_restriction_build(int ne, int dof, int ndofs, const int *elem_dofs,
+                          const int *dof_map, int *offsets, int *indices,
+                          int *gather_map);
+/* fem/restriction.cpp:116-136 */
+void or_restriction_mult(int ne, int nd, const int *gather_map,
+                         const double *x, double *y);
+/* fem/restriction.cpp:159-201; add != 0 accumulates into y */
+void or_restriction_mult_transpose(int nd, int ndofs, const int *offsets,
+                                   const int *indices, const double *x,
+                                   double *y, int add);
+/* fem/restriction.cpp:203-228 */
+void or_restriction_abs_mult_transpose(int nd, int ndofs, const int *offsets,
+                                       const int *indices, const double *x,
+                                       double *y);
+
+/* fem/intrules.cpp:620-690 (Gauss-Legendre on [0,1]) */
+void or_gauss_legendre(int n, double *x, double *w);
+/* fem/intrules.cpp:708-800 (Gauss-Lobatto points on [0,1]) */
+void or_gauss_lobatto(int n, double *x);
+/* fem/fe/fe_base.cpp:2697-2741: B[q + Q*d] = phi_d(xq), G = phi_d'(xq) for
+ * the Lagrange basis on the np = D nodes `nodes` at the Q points `xq`. */
+void or_basis_tables(int D, const double *nodes, int Q, const double *xq,
+                     double *B, double *G);
+
+/* fem/qinterp/grad.hpp:233-376 (byNODES, reference-space derivatives):
+ * J(q, c, d, e) = d x_c / d xi_d from the lexicographic nodes E-vector
+ * X (Dg, Dg, Dg, 3, NE). */
+void or_geom_jacobians3d(int ne, int dg, int q1d, const double *Bg,
+                         const double *Gg, const double *X, double *J);
+/* determinant of each J (fem/qinterp/det.hpp:253-330) */
+void or_geom_det3d(int ne, const double *J, int q3, double *detJ);
+
+/* fem/integ/bilininteg_diffusion_kernels.cpp:262-386. c_size = coeff_dim
+ * (constant) or coeff_dim*Q^3*NE. */
+void or_diffusion_setup3d(int ne, int q1d, int coeff_dim, const double *W,
+                          const double *J, const double *C, long c_size,
+                          double *D);
+/* fem/integ/bilininteg_diffusion_kernels.hpp:796-986 (accumulates y) */
+void or_diffusion_apply3d(int ne, int symm, int d1d, int q1d, const double *B,
+                          const double *G, const double *D, const double *x,
+                          double *y);
+/* fem/integ/bilininteg_diffusion_kernels.hpp:268-366 (accumulates y) */
+void or_diffusion_diagonal3d(int ne, int symm, int d1d, int q1d,
+                             const double *B, const double *G, const double *D,
+                             double *y);
+/* fem/integ/bilininteg_mass_pa.cpp:73-89: v = W * c * detJ (by_val) or W*c/detJ */
+void or_mass_setup3d(int ne, int nq, const double *W, const double *detJ,
+                     const double *C, long c_size, int by_val, double *D);
+/* fem/integ/bilininteg_mass_kernels.hpp:664-813 (accumulates y) */
+void or_mass_apply3d(int ne, int d1d, int q1d, const double *B,
+                     const double *D, const double *x, double *y);
+/* fem/integ/bilininteg_mass_kernels.hpp:262-329 (accumulates y) */
+void or_mass_diagonal3d(int ne, int d1d, int q1d, const double *B,
+                        const double *D, double *y);
+
+/* PABilinearFormExtension::MultInternal, fem/bilinearform_ext.cpp:487-564:
+ * y = R^T A_e R x for one integrator; kind 0 = diffusion, 1 = mass.
+ * work: 2*ne*D^3 doubles. */
+void or_pa_mult(int kind, int ne, int ndofs, int symm, int d1d, int q1d,
+                const int *gather_map, const int *offsets, const int *indices,
+                const double *B, const double *G, const double *D,
+                const double *x, double *y, double *work);
+
+/* CGSolver::Mult (linalg/solvers.cpp:869-1050) with OperatorJacobiSmoother
+ * (linalg/solvers.cpp:401-452) on ConstrainedOperator (linalg/operator.cpp:
+ * 601-661, DIAG_ONE) around the PA diffusion operator. dinv is the smoother's
+ * inverse diagonal (ess entries already set to 1). Returns iterations;
+ * *final_norm = sqrt(betanom); *converged set. x is the initial guess when
+ * iterative_mode != 0 and is overwritten with the solution. */
+int or_pcg_diffusion(int ne, int ndofs, int symm, int d1d, int q1d,
+                     const int *gather_map, const int *offsets,
+                     const int *indices, const double *B, const double *G,
+                     const double *D, const int *ess, int n_ess,
+                     const double *dinv, const double *b, double *x,
+                     double rel_tol, double abs_tol, int max_it,
+                     int iterative_mode, double *final_norm, int *converged);
+
+/* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
+int or_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,408 @@
+// Golden-vector generator. Runs the UNMODIFIED reference MFEM (serial CPU
+// build made by oracle/ref/Makefile) through its public partial-assembly API
+// and writes every intermediate of the PA H1 path as .npy files:
+//   ElementRestriction maps      fem/restriction.cpp:26-114
+//   DofToQuad B/G tables         fem/fe/fe_base.cpp:2697-2741
+//   Jacobians / determinants     mesh/mesh.cpp:15445-15500
+//   PADiffusionSetup3D qdata     fem/integ/bilininteg_diffusion_kernels.cpp:262-386
+//   AddMultPA / AssembleDiagonal fem/integ/bilininteg_{diffusion,mass}_pa.cpp
+//   BilinearForm::Mult (PA)      fem/bilinearform_ext.cpp:487-564
+//   PCG + OperatorJacobiSmoother linalg/solvers.cpp:331-452,869-1050
+// Usage: golden_driver <outdir>   (one subdirectory per case)
+#include "mfem.hpp"
+#include "fem/integ/bilininteg_diffusion_kernels.hpp"
+#include <cstdio>
+#include <cstdint>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <sys/stat.h>
+
+using namespace mfem;
+
+// ---------------------------------------------------------------- npy writer
+static void write_npy(const std::string &path, const char *descr,
+                      const std::vector<long> &shape, const void *data,
+                      size_t elem_size)
+{
+   std::string hdr = "{'descr': '";
+   hdr += descr;
+   hdr += "', 'fortran_order': False, 'shape': (";
+   size_t n = 1;
+   for (size_t i = 0; i < shape.size(); i++)
+   {
+      hdr += std::to_string(shape[i]);
+      hdr += (shape.size() == 1 || i + 1 < shape.size()) ? ", " : "";
+      n *= shape[i];
+   }
+   hdr += "), }";
+   size_t total = 10 + hdr.size() + 1;
+   size_t pad = (64 - total % 64) % 64;
+   hdr += std::string(pad, ' ');
+   hdr += "\n";
+   FILE *f = fopen(path.c_str(), "wb");
+   if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); exit(1); }
+   const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+   fwrite(magic, 1, 8, f);
+   uint16_t hl = (uint16_t)hdr.size();
+   fwrite(&hl, 2, 1, f);
+   fwrite(hdr.data(), 1, hdr.size(), f);
+   if (n) { fwrite(data, elem_size, n, f); }
+   fclose(f);
+}
+static void save(const std::string &dir, const char *name, const Vector &v)
+{
+   write_npy(dir + "/" + name + ".npy", "<f8", {(long)v.Size()},
+             v.HostRead(), 8);
+}
+static void save(const std::string &dir, const char *name,
+                 const Array<real_t> &v)
+{
+   write_npy(dir + "/" + name + ".npy", "<f8", {(long)v.Size()},
+             v.HostRead(), 8);
+}
+static void save(const std::string &dir, const char *name, const Array<int> &v)
+{
+   write_npy(dir + "/" + name + ".npy", "<i4", {(long)v.Size()},
+             v.HostRead(), 4);
+}
+static void save_ints(const std::string &dir, const char *name,
+                      const std::vector<int> &v)
+{
+   write_npy(dir + "/" + name + ".npy", "<i4", {(long)v.size()}, v.data(), 4);
+}
+static void save_dbls(const std::string &dir, const char *name,
+                      const std::vector<double> &v)
+{
+   write_npy(dir + "/" + name + ".npy", "<f8", {(long)v.size()}, v.data(), 8);
+}
+
+// ------------------------------------------- synthetic inputs (shared recipe)
+// splitmix64 stream: the same generator is used by the GPU library's mesh
+// builder, so jittered vertices and coefficient modes are identical.
+static uint64_t splitmix64(uint64_t &s)
+{
+   uint64_t z = (s += 0x9e3779b97f4a7c15ULL);
+   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+   z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+   return z ^ (z >> 31);
+}
+static double u01(uint64_t &s) { return (splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+struct Modes { int k[16][3]; double phi[16]; };
+static Modes make_modes(uint64_t seed)
+{
+   Modes m; uint64_t s = seed;
+   for (int i = 0; i < 16; i++)
+   {
+      for (int d = 0; d < 3; d++) { m.k[i][d] = (int)(u01(s) * 9.0) - 4; }
+      m.phi[i] = 2.0 * M_PI * u01(s);
+   }
+   return m;
+}
+static Modes g_modes;
+static double kappa_fn(const Vector &x)
+{
+   double g = 0.0;
+   for (int i = 0; i < 16; i++)
+   {
+      const double a = 2.0 * M_PI * (g_modes.k[i][0] * x(0) + g_modes.k[i][1] * x(1) +
+                                     g_modes.k[i][2] * x(2)) + g_modes.phi[i];
+      g += 0.5 * cos(a);
+   }
+   return exp(g);
+}
+static void vec_kappa_fn(const Vector &x, Vector &v)
+{
+   v.SetSize(3);
+   const double k = kappa_fn(x);
+   v(0) = k; v(1) = 1.0 + 0.5 * x(0); v(2) = 2.0 - x(1) * x(2);
+}
+static void sym_mat_fn(const Vector &x, DenseMatrix &M)
+{
+   M.SetSize(3);
+   const double k = kappa_fn(x);
+   M(0,0) = 2.0 + k;  M(0,1) = 0.3 * x(2); M(0,2) = 0.1;
+   M(1,0) = M(0,1);   M(1,1) = 3.0 - x(0); M(1,2) = -0.2 * x(1);
+   M(2,0) = M(0,2);   M(2,1) = M(1,2);     M(2,2) = 2.5 + x(1);
+}
+static void sym_mat_fn_s(const Vector &x, DenseSymmetricMatrix &M)
+{
+   DenseMatrix F; sym_mat_fn(x, F);
+   M.SetSize(3);
+   for (int i = 0; i < 3; i++) for (int j = i; j < 3; j++) { M(i, j) = F(i, j); }
+}
+static void nonsym_mat_fn(const Vector &x, DenseMatrix &M)
+{
+   sym_mat_fn(x, M);
+   M(0,1) += 0.25; M(2,0) -= 0.15 * x(0); M(1,2) += 0.05;
+}
+static void curve_map(const Vector &x, Vector &y)
+{
+   y = x;
+   const double s = 0.05 * sin(2 * M_PI * x(0)) * sin(2 * M_PI * x(1)) *
+                    sin(2 * M_PI * x(2));
+   for (int d = 0; d < 3; d++) { y(d) = x(d) + s; }
+}
+
+static void jitter_vertices(Mesh &mesh, int n, double amp, uint64_t seed)
+{
+   // Interior vertices move by U(-amp*h, amp*h) in each coordinate; three
+   // draws are consumed per vertex (in vertex order) whether it moves or not.
+   const double h = 1.0 / n;
+   uint64_t s = seed;
+   for (int v = 0; v < mesh.GetNV(); v++)
+   {
+      real_t *c = mesh.GetVertex(v);
+      bool interior = true;
+      for (int d = 0; d < 3; d++)
+      {
+         if (!(c[d] > 1e-12 && c[d] < 1.0 - 1e-12)) { interior = false; }
+      }
+      for (int d = 0; d < 3; d++)
+      {
+         const double r = u01(s);
+         if (interior) { c[d] += (2.0 * r - 1.0) * amp * h; }
+      }
+   }
+}
+
+enum CoeffKind { C_ONE = 0, C_FN = 1, C_VEC = 2, C_SYM = 3, C_NONSYM = 4, C_CONST = 5 };
+
+struct Case
+{
+   const char *name;
+   int n, p, q;       // elements per side, order, quadrature points per dim
+   double jitter;     // vertex jitter amplitude in units of h
+   int coeff;         // CoeffKind
+   bool curved;       // order-3 curved geometry (x + 0.05 sin sin sin)
+   bool solve;        // cfg1-style Dirichlet Poisson + Jacobi-PCG
+};
+
+static void run_case(const Case &c, const std::string &root)
+{
+   const std::string dir = root + "/" + c.name;
+   mkdir(dir.c_str(), 0755);
+   Mesh mesh = Mesh::MakeCartesian3D(c.n, c.n, c.n, Element::HEXAHEDRON,
+                                     1.0, 1.0, 1.0, true);
+   if (c.jitter > 0) { jitter_vertices(mesh, c.n, c.jitter, 1); }
+   {
+      std::vector<double> vtx(3 * mesh.GetNV());
+      for (int v = 0; v < mesh.GetNV(); v++)
+      {
+         for (int d = 0; d < 3; d++) { vtx[3*v+d] = mesh.GetVertex(v)[d]; }
+      }
+      save_dbls(dir, "vertices", vtx);
+      std::vector<int> ev(8 * mesh.GetNE());
+      for (int e = 0; e < mesh.GetNE(); e++)
+      {
+         Array<int> vv; mesh.GetElementVertices(e, vv);
+         for (int k = 0; k < 8; k++) { ev[8*e+k] = vv[k]; }
+      }
+      save_ints(dir, "elem_vertices", ev);
+   }
+   if (c.curved)
+   {
+      mesh.SetCurvature(3, false, 3, Ordering::byVDIM);
+      mesh.Transform(curve_map);
+   }
+   mesh.EnsureNodes();
+
+   H1_FECollection fec(c.p, 3);
+   FiniteElementSpace fes(&mesh, &fec);
+   const int ndofs = fes.GetNDofs();
+   const int ne = mesh.GetNE();
+   const int p = c.p, q = c.q;
+   const IntegrationRule &ir = IntRules.Get(Geometry::CUBE, 2 * q - 1);
+   MFEM_VERIFY(ir.GetNPoints() == q * q * q, "rule size");
+
+   // --- restriction maps (a1)
+   const ElementRestriction *R = dynamic_cast<const ElementRestriction*>(
+      fes.GetElementRestriction(ElementDofOrdering::LEXICOGRAPHIC));
+   MFEM_VERIFY(R, "expected ElementRestriction");
+   save(dir, "gather_map", R->GatherMap());
+   save(dir, "offsets", R->Offsets());
+   save(dir, "indices", R->Indices());
+   {
+      const Table &e2d = fes.GetElementToDofTable();
+      std::vector<int> j(e2d.GetJ(), e2d.GetJ() + e2d.Size_of_connections());
+      save_ints(dir, "elem_dofs", j);
+      auto el_t = dynamic_cast<const TensorBasisElement*>(fes.GetTypicalFE());
+      save(dir, "dof_map", el_t->GetDofMap());
+   }
+
+   // --- basis tables and geometry (a5-a7)
+   const FiniteElement &el = *fes.GetTypicalFE();
+   const DofToQuad &maps = el.GetDofToQuad(ir, DofToQuad::TENSOR);
+   save(dir, "B", maps.B); save(dir, "G", maps.G);
+   save(dir, "Bt", maps.Bt); save(dir, "Gt", maps.Gt);
+   save(dir, "W", ir.GetWeights());
+   {
+      // nodal (geometry) space: E-vector of nodes and its tables
+      const FiniteElementSpace *nfes = mesh.GetNodalFESpace();
+      const GridFunction *nodes = mesh.GetNodes();
+      const Operator *nR = nfes->GetElementRestriction(ElementDofOrdering::LEXICOGRAPHIC);
+      Vector nodesE(nR->Height());
+      nR->Mult(*nodes, nodesE);
+      save(dir, "nodesE", nodesE);
+      const DofToQuad &nmaps = nfes->GetTypicalFE()->GetDofToQuad(ir, DofToQuad::TENSOR);
+      save(dir, "Bg", nmaps.B); save(dir, "Gg", nmaps.G);
+   }
+   const GeometricFactors *geom = mesh.GetGeometricFactors(
+      ir, GeometricFactors::JACOBIANS | GeometricFactors::DETERMINANTS);
+   if (!c.solve) { save(dir, "J", geom->J); }
+   save(dir, "detJ", geom->detJ);
+
+   // --- coefficients
+   g_modes = make_modes(3);
+   ConstantCoefficient one(1.0), twelve(12.34);
+   FunctionCoefficient kfn(kappa_fn);
+   VectorFunctionCoefficient kvec(3, vec_kappa_fn);
+   SymmetricMatrixFunctionCoefficient ksym(3, sym_mat_fn_s);
+   MatrixFunctionCoefficient knon(3, nonsym_mat_fn);
+   QuadratureSpace qs(mesh, ir);
+   CoefficientVector cv(qs, CoefficientStorage::COMPRESSED);
+   DiffusionIntegrator *dint = nullptr;
+   Coefficient *mass_coeff = nullptr;
+   switch (c.coeff)
+   {
+      case C_ONE: cv.SetConstant(1.0); dint = new DiffusionIntegrator(&ir); mass_coeff = &one; break;
+      case C_CONST: cv.SetConstant(12.34); dint = new DiffusionIntegrator(twelve, &ir); mass_coeff = &twelve; break;
+      case C_FN: cv.Project(kfn); dint = new DiffusionIntegrator(kfn, &ir); mass_coeff = &kfn; break;
+      case C_VEC: cv.Project(kvec); dint = new DiffusionIntegrator(kvec, &ir); mass_coeff = &kfn; break;
+      case C_SYM: cv.ProjectTranspose(ksym); dint = new DiffusionIntegrator(ksym, &ir); mass_coeff = &kfn; break;
+      case C_NONSYM: cv.ProjectTranspose(knon); dint = new DiffusionIntegrator(knon, &ir); mass_coeff = &kfn; break;
+   }
+   save(dir, "coeff", cv);
+   std::vector<int> meta = {ne, ndofs, p + 1, q, cv.GetVDim(), c.coeff, c.n};
+   save_ints(dir, "meta", meta);
+
+   // --- qdata through the reference's own setup kernel (a8)
+   const int coeff_dim = cv.GetVDim();
+   const bool symm = coeff_dim != 9;
+   Vector qd((symm ? 6 : 9) * q * q * q * ne);
+   if (!c.solve)
+   {
+      internal::PADiffusionSetup(3, 3, p + 1, q, coeff_dim, ne, ir.GetWeights(),
+                                 geom->J, cv, qd);
+      save(dir, "qdata_diff", qd);
+   }
+   {
+      // mass qdata: v(q,e) = W(q) * coeff * detJ (fem/integ/bilininteg_mass_pa.cpp:73-89)
+      CoefficientVector mc(*mass_coeff, qs, CoefficientStorage::COMPRESSED);
+      save(dir, "coeff_mass", mc);
+      const int NQ = q * q * q;
+      Vector mq(NQ * ne);
+      const bool cc = mc.Size() == 1;
+      for (int e = 0; e < ne; e++)
+         for (int k = 0; k < NQ; k++)
+            mq(k + NQ * e) = ir.GetWeights()[k] * (cc ? mc(0) : mc(k + NQ * e)) *
+                             geom->detJ(k + NQ * e);
+      if (!c.solve) { save(dir, "qdata_mass", mq); }
+   }
+
+   // --- operator applications through BilinearForm (PA)
+   Vector x(ndofs);
+   {
+      uint64_t s = 2;
+      for (int i = 0; i < ndofs; i++) { x(i) = 2.0 * u01(s) - 1.0; }
+   }
+   save(dir, "x", x);
+   Vector dof_xyz(3 * ndofs);
+   for (int d = 0; d < 3; d++)
+   {
+      GridFunction gx(&fes);
+      FunctionCoefficient fc([d](const Vector &pt) { return pt(d); });
+      gx.ProjectCoefficient(fc);
+      for (int i = 0; i < ndofs; i++) { dof_xyz(3 * i + d) = gx(i); }
+   }
+   save(dir, "dof_xyz", dof_xyz);
+
+   BilinearForm a(&fes);
+   a.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+   a.AddDomainIntegrator(dint);
+   a.Assemble();
+   Vector y(ndofs); a.Mult(x, y); save(dir, "y_diff", y);
+   Vector diag(ndofs); a.AssembleDiagonal(diag); save(dir, "diag_diff", diag);
+   {
+      Vector xE(R->Height()), yE(R->Height());
+      R->Mult(x, xE); yE = 0.0;
+      dint->AddMultPA(xE, yE);
+      if (!c.solve) { save(dir, "xE", xE); save(dir, "yE_diff", yE); }
+      Vector dE(R->Height()); dE = 0.0; dint->AssembleDiagonalPA(dE);
+      if (!c.solve) { save(dir, "diagE_diff", dE); }
+   }
+
+   BilinearForm m(&fes);
+   m.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+   MassIntegrator *mint = new MassIntegrator(*mass_coeff, &ir);
+   m.AddDomainIntegrator(mint);
+   m.Assemble();
+   Vector ym(ndofs); m.Mult(x, ym); save(dir, "y_mass", ym);
+   Vector dm(ndofs); m.AssembleDiagonal(dm); save(dir, "diag_mass", dm);
+   if (!c.solve)
+   {
+      Vector xE(R->Height()), yE(R->Height());
+      R->Mult(x, xE); yE = 0.0;
+      mint->AddMultPA(xE, yE); save(dir, "yE_mass", yE);
+   }
+
+   if (c.solve)
+   {
+      // cfg1: f = 1, homogeneous Dirichlet on the whole boundary, PCG + Jacobi
+      Array<int> ess_tdof_list, ess_bdr(mesh.bdr_attributes.Max());
+      ess_bdr = 1;
+      fes.GetEssentialTrueDofs(ess_bdr, ess_tdof_list);
+      save(dir, "ess_tdofs", ess_tdof_list);
+      LinearForm b(&fes);
+      b.AddDomainIntegrator(new DomainLFIntegrator(one));
+      b.Assemble();
+      save(dir, "b", b);
+      GridFunction xs(&fes); xs = 0.0;
+      OperatorPtr A; Vector X, Bv;
+      a.FormLinearSystem(ess_tdof_list, xs, b, A, X, Bv);
+      save(dir, "B_rhs", Bv);
+      Vector Ax(ndofs); A->Mult(x, Ax); save(dir, "Ax_constrained", Ax);
+      OperatorJacobiSmoother M(a, ess_tdof_list);
+      Vector Mx(ndofs); M.Mult(x, Mx); save(dir, "Mx_jacobi", Mx);
+      CGSolver cg;
+      cg.SetRelTol(1e-12); cg.SetAbsTol(0.0); cg.SetMaxIter(500);
+      cg.SetPrintLevel(0);
+      cg.SetOperator(*A); cg.SetPreconditioner(M);
+      cg.Mult(Bv, X);
+      a.RecoverFEMSolution(X, b, xs);
+      save(dir, "X", X);
+      std::vector<double> info = {(double)cg.GetNumIterations(), cg.GetFinalNorm(),
+                                  (double)cg.GetConverged()};
+      save_dbls(dir, "cg_info", info);
+      printf("%s: PCG iterations %d final norm %.6e\n", c.name,
+             cg.GetNumIterations(), cg.GetFinalNorm());
+   }
+   printf("%s: ne=%d ndofs=%d D=%d Q=%d coeff_dim=%d\n", c.name, ne, ndofs,
+          p + 1, q, coeff_dim);
+}
+
+int main(int argc, char **argv)
+{
+   if (argc < 2) { fprintf(stderr, "usage: %s outdir\n", argv[0]); return 1; }
+   Device device("cpu");
+   const std::string root = argv[1];
+   mkdir(root.c_str(), 0755);
+   const Case cases[] =
+   {
+      // name            n  p  q  jitter coeff    curved solve
+      {"cart2_p2_one",    2, 2, 4, 0.0, C_ONE,    false, false},
+      {"cart2_p1_const",  2, 1, 3, 0.0, C_CONST,  false, false},
+      {"jit3_p3_fn",      3, 3, 5, 0.1, C_FN,     false, false},
+      {"jit2_p4_vec",     2, 4, 6, 0.1, C_VEC,    false, false},
+      {"jit2_p4_sym",     2, 4, 6, 0.1, C_SYM,    false, false},
+      {"jit2_p2_nonsym",  2, 2, 4, 0.1, C_NONSYM, false, false},
+      {"jit2_p6_fn",      2, 6, 8, 0.1, C_FN,     false, false},
+      {"cart1_p8_one",    1, 8, 10, 0.0, C_ONE,   false, false},
+      {"jit1_p7_fn",      1, 7, 9, 0.1, C_FN,     false, false},
+      {"curv2_p3_fn",     2, 3, 5, 0.0, C_FN,     true,  false},
+      {"cfg1_solve",      8, 3, 4, 0.0, C_ONE,    false, true},
+   };
+   for (const Case &c : cases) { run_case(c, root); }
+   return 0;
+}

@@ -1,0 +1,138 @@
+"""The CPU oracle is pinned against golden vectors produced by the reference
+itself (tests/golden/*.npz, made by tests/golden/make_golden.py from MFEM's own
+partial-assembly path). Tolerances follow the reference's unit tests
+(MFEM_Approx 1e-12) except where noted; integer maps are bit-exact."""
+import numpy as np
+import pytest
+
+from tests.conftest import golden_cases, load_golden
+
+CASES = golden_cases()
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def meta(g):
+    ne, ndofs, D, Q, cdim, ckind, n = (int(v) for v in g["meta"])
+    return ne, ndofs, D, Q, cdim
+
+
+def tensor_weights(w):
+    Q = len(w)
+    return np.einsum("k,j,i->kji", w, w, w).reshape(Q ** 3)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_restriction_maps_bit_exact(oracle, case):
+    g = load_golden(case)
+    ne, ndofs, D, Q, _ = meta(g)
+    off, ind, gm = oracle.restriction_build(ne, D ** 3, ndofs, g["elem_dofs"], g["dof_map"])
+    assert np.array_equal(gm, g["gather_map"])
+    assert np.array_equal(off, g["offsets"])
+    assert np.array_equal(ind, g["indices"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_quadrature_and_basis(oracle, case):
+    g = load_golden(case)
+    ne, ndofs, D, Q, _ = meta(g)
+    xq, wq = oracle.gauss_legendre(Q)
+    assert np.allclose(tensor_weights(wq), g["W"], rtol=1e-14, atol=1e-15)
+    nodes = oracle.gauss_lobatto(D)
+    B, G = oracle.basis_tables(nodes, xq)
+    assert np.abs(B - g["B"]).max() < 1e-13
+    assert np.abs(G - g["G"]).max() < 1e-12 * max(1.0, np.abs(g["G"]).max())
+    # Bt/Gt are the transposes (D, Q)
+    assert np.array_equal(g["Bt"].reshape(Q, D, order="C"), g["B"].reshape(D, Q).T)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_geometric_factors(oracle, case):
+    g = load_golden(case)
+    ne, ndofs, D, Q, _ = meta(g)
+    dg = int(round((g["nodesE"].size / (3 * ne)) ** (1 / 3)))
+    J = oracle.geom_jacobians3d(ne, dg, Q, g["Bg"], g["Gg"], g["nodesE"])
+    if "J" in g:
+        assert relerr(J, g["J"]) < 1e-14
+    det = oracle.geom_det3d(ne, J, Q ** 3)
+    assert relerr(det, g["detJ"]) < 1e-14
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c != "cfg1_solve"])
+def test_diffusion_setup_apply_diag(oracle, case):
+    g = load_golden(case)
+    ne, ndofs, D, Q, cdim = meta(g)
+    symm = cdim != 9
+    qd = oracle.diffusion_setup3d(ne, Q, cdim, g["W"], g["J"], g["coeff"])
+    assert relerr(qd, g["qdata_diff"]) < 1e-14
+    yE = oracle.diffusion_apply3d(ne, symm, D, Q, g["B"], g["G"], g["qdata_diff"], g["xE"])
+    assert relerr(yE, g["yE_diff"]) < 1e-12
+    y = oracle.pa_mult(0, ne, ndofs, symm, D, Q, g["gather_map"], g["offsets"], g["indices"],
+                       g["B"], g["G"], g["qdata_diff"], g["x"])
+    assert relerr(y, g["y_diff"]) < 1e-12
+    dE = oracle.diffusion_diagonal3d(ne, symm, D, Q, g["B"], g["G"], g["qdata_diff"])
+    assert relerr(dE, g["diagE_diff"]) < 1e-12
+    d = oracle.restriction_abs_mult_transpose(D ** 3, ndofs, g["offsets"], g["indices"], dE)
+    assert relerr(d, g["diag_diff"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c != "cfg1_solve"])
+def test_mass_setup_apply_diag(oracle, case):
+    g = load_golden(case)
+    ne, ndofs, D, Q, _ = meta(g)
+    qm = oracle.mass_setup3d(ne, Q ** 3, g["W"], g["detJ"], g["coeff_mass"])
+    assert relerr(qm, g["qdata_mass"]) < 1e-14
+    yE = oracle.mass_apply3d(ne, D, Q, g["B"], qm, g["xE"])
+    assert relerr(yE, g["yE_mass"]) < 1e-12
+    y = oracle.pa_mult(1, ne, ndofs, True, D, Q, g["gather_map"], g["offsets"], g["indices"],
+                       g["B"], g["G"], qm, g["x"])
+    assert relerr(y, g["y_mass"]) < 1e-12
+    dE = oracle.mass_diagonal3d(ne, D, Q, g["B"], qm)
+    d = oracle.restriction_abs_mult_transpose(D ** 3, ndofs, g["offsets"], g["indices"], dE)
+    assert relerr(d, g["diag_mass"]) < 1e-12
+
+
+def cfg1_operator(oracle, g):
+    ne, ndofs, D, Q, cdim = meta(g)
+    dg = int(round((g["nodesE"].size / (3 * ne)) ** (1 / 3)))
+    J = oracle.geom_jacobians3d(ne, dg, Q, g["Bg"], g["Gg"], g["nodesE"])
+    qd = oracle.diffusion_setup3d(ne, Q, cdim, g["W"], J, g["coeff"])
+    return ne, ndofs, D, Q, qd
+
+
+def test_cfg1_operator_and_jacobi(oracle):
+    g = load_golden("cfg1_solve")
+    ne, ndofs, D, Q, qd = cfg1_operator(oracle, g)
+    y = oracle.pa_mult(0, ne, ndofs, True, D, Q, g["gather_map"], g["offsets"], g["indices"],
+                       g["B"], g["G"], qd, g["x"])
+    assert relerr(y, g["y_diff"]) < 1e-12
+    dE = oracle.diffusion_diagonal3d(ne, True, D, Q, g["B"], g["G"], qd)
+    diag = oracle.restriction_abs_mult_transpose(D ** 3, ndofs, g["offsets"], g["indices"], dE)
+    assert relerr(diag, g["diag_diff"]) < 1e-12
+    ess = g["ess_tdofs"]
+    # ConstrainedOperator (DIAG_ONE) applied to x
+    z = g["x"].copy(); z[ess] = 0.0
+    Ax = oracle.pa_mult(0, ne, ndofs, True, D, Q, g["gather_map"], g["offsets"], g["indices"],
+                        g["B"], g["G"], qd, z)
+    Ax[ess] = g["x"][ess]
+    assert relerr(Ax, g["Ax_constrained"]) < 1e-12
+    dinv = 1.0 / diag; dinv[ess] = 1.0
+    assert relerr(dinv * g["x"], g["Mx_jacobi"]) < 1e-12
+
+
+def test_cfg1_pcg_solution(oracle):
+    g = load_golden("cfg1_solve")
+    ne, ndofs, D, Q, qd = cfg1_operator(oracle, g)
+    dE = oracle.diffusion_diagonal3d(ne, True, D, Q, g["B"], g["G"], qd)
+    diag = oracle.restriction_abs_mult_transpose(D ** 3, ndofs, g["offsets"], g["indices"], dE)
+    ess = g["ess_tdofs"]
+    dinv = 1.0 / diag; dinv[ess] = 1.0
+    X, it, fn, conv = oracle.pcg_diffusion(ne, ndofs, True, D, Q, g["gather_map"], g["offsets"],
+                                           g["indices"], g["B"], g["G"], qd, ess, dinv, g["B_rhs"],
+                                           rel_tol=1e-12, max_it=500)
+    ref_it, ref_norm, ref_conv = g["cg_info"]
+    assert conv and bool(ref_conv)
+    assert abs(it - int(ref_it)) <= 1
+    assert relerr(X, g["X"]) < 1e-10
