@@ -1,0 +1,348 @@
+"""Benchmark of the PA H1 path on one GB300 (or N replicas).
+
+Workload (default): FP64 PA diffusion operator apply, L-vector to L-vector
+(restriction gather fused into the sum-factorised apply, deterministic CSR
+scatter), on the jittered Cartesian hex mesh of the unit cube with n = 77
+elements per side (interior vertices jittered by U(-0.1h, 0.1h), seed 1),
+H1 order p = 4, Gauss-Legendre rule with p + 2 = 6 points per dimension,
+29,503,629 DOFs, x ~ U[-1, 1] (seed 2). One step = one operator apply.
+Inputs (qdata 4.7 GB) are larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbpa|reference]
+
+Prints one JSON line. --impl reference times the CPU oracle (the plain-C
+restatement of the reference's PA path) on the host cores instead.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "GDOF/s PA diffusion apply; PCG time-to-1e-10 mixed vs FP64, one GB300"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbpa", choices=["gbpa", "reference"])
+    ap.add_argument("--n", type=int, default=77)
+    ap.add_argument("--p", type=int, default=4)
+    ap.add_argument("--kind", default="diffusion", choices=["diffusion", "mass"])
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=38)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def algorithmic_bytes(ne, ndofs, D, Q, w, kind, element_only):
+    """Algorithmic HBM bytes of one apply: qdata once, index map once, x read
+    once; L->L also writes y once; the element kernel alone writes the
+    E-vector instead of y."""
+    S = 6 if kind == "diffusion" else 1
+    qd = ne * S * Q ** 3 * w
+    maps = ne * D ** 3 * 4
+    if element_only:
+        return qd + maps + ndofs * w + ne * D ** 3 * w
+    return qd + maps + 2 * ndofs * w
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- problem set-up
+def build_problem(n, p, kind, seed_jitter=1):
+    """Mesh, maps and qdata on the device through the library."""
+    import torch
+    from mfem_gb300 import fem
+    from mfem_gb300.pa import (DiffusionIntegrator, FiniteElementSpace, MassIntegrator, PAOperator)
+    mesh = fem.CartesianMesh(n, jitter=0.1, seed=seed_jitter)
+    fes = FiniteElementSpace(mesh, p)
+    integ = DiffusionIntegrator() if kind == "diffusion" else MassIntegrator()
+    integ.AssemblePA(fes)
+    kind_id = 0 if kind == "diffusion" else 1
+    return fes, integ, kind_id
+
+
+def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1):
+    """The oracle's L->L apply (gather, element kernel, CSR scatter) on the
+    host cores, set up by the oracle itself from the same synthetic mesh."""
+    from mfem_gb300 import fem
+    from tests import oracle_lib
+    o = oracle_lib.load()
+    mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
+    sp = fem.H1Space(mesh, p)
+    D, Q = p + 1, p + 2
+    t = fem.Tables(p, Q)
+    off, ind, gm = o.restriction_build(mesh.ne, D ** 3, sp.ndofs, sp.element_dofs(), None)
+    gt = fem.Tables(1, Q)
+    J = o.geom_jacobians3d(mesh.ne, 2, Q, gt.B, gt.G, mesh.nodes_evector(1))
+    if kind == "diffusion":
+        qd = o.diffusion_setup3d(mesh.ne, Q, 1, t.W, J, np.array([1.0]))
+    else:
+        det = o.geom_det3d(mesh.ne, J, Q ** 3)
+        qd = o.mass_setup3d(mesh.ne, Q ** 3, t.W, det, np.array([1.0]))
+    del J
+    x = 2 * fem.u01_array(2, sp.ndofs) - 1
+    kid = 0 if kind == "diffusion" else 1
+    for _ in range(warmup):
+        o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+    dt = time.perf_counter() - t0
+    return sp.ndofs * steps / dt / 1e9, sp.ndofs, o.num_threads(), dt
+
+
+# ------------------------------------------------------------------- reference arm
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    steps, warm = args.steps, args.warmup
+    rate, ndofs, threads, dt = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, steps,
+                                                     warmup=min(warm, 2))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "GDOF/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"PA {args.kind} apply L->L, jittered hex mesh, p={args.p}, "
+                               f"q={args.p + 2}; each step one apply on the n={args.cpu_sample_n} "
+                               f"sample mesh ({ndofs} DOFs)", "p": args.p, "n": args.cpu_sample_n},
+        "cpu_baseline": {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} applies of the n={args.cpu_sample_n} p={args.p} mesh "
+                                   f"({ndofs} DOFs), OpenMP over elements/dofs"},
+        "e2e": {"value": rate, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# -------------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from mfem_gb300 import _lib
+    from mfem_gb300.pa import Device, PAOperator
+    dev = Device("cuda", local)
+    lib = dev.lib
+    stream = torch.cuda.current_stream()
+    fes, integ, kid = build_problem(args.n, args.p, args.kind)
+    ne, ndofs, D, Q = fes.ne, fes.ndofs, integ.D, integ.Q
+    op = PAOperator(kid, fes, D, Q, integ.B, integ.G, integ.qdata)
+    from mfem_gb300 import fem
+    x = torch.from_numpy(2 * fem.u01_array(2, ndofs) - 1).cuda()
+    y = torch.empty_like(x)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    # ---- device-resident timing of the L->L apply (value)
+    for _ in range(max(args.warmup, 3)):
+        op.Mult(x, y)
+    barrier()
+    launches0 = dev.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            op.Mult(x, y)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = dev.launches() - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ndofs * args.steps / (ms * 1e-3) / 1e9
+
+    # ---- dominant kernel alone: gather-fused element apply (E-vector out)
+    yE = torch.empty(ne * D ** 3, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        _lib.check(lib.gbpa_operator_apply_element(op.handle, P(x), P(yE)), "apply_element")
+    torch.cuda.synchronize()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nk = max(10, args.steps // 2)
+    k0.record(stream)
+    for _ in range(nk):
+        _lib.check(lib.gbpa_operator_apply_element(op.handle, P(x), P(yE)), "apply_element")
+    k1.record(stream)
+    torch.cuda.synchronize()
+    k_ms = k0.elapsed_time(k1) / nk
+    kbytes = algorithmic_bytes(ne, ndofs, D, Q, 8, args.kind, element_only=True)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = kbytes / (k_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    hx = torch.empty(ndofs, dtype=torch.float64).pin_memory()
+    hx.copy_(x.cpu())
+    hy = torch.empty(ndofs, dtype=torch.float64).pin_memory()
+    dx = torch.empty_like(x)
+    for _ in range(2):
+        dx.copy_(hx, non_blocking=True); op.Mult(dx, y); hy.copy_(y, non_blocking=True)
+    barrier()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        dx.copy_(hx, non_blocking=True)
+        op.Mult(dx, y)
+        hy.copy_(y, non_blocking=True)
+    t1.record(stream)
+    barrier()
+    e2e_ms = t0.elapsed_time(t1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = world * ndofs * args.steps / (e2e_ms * 1e-3) / 1e9
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        extras = run_extras(args, fes, integ, op, x, y)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"FP64 PA {args.kind} operator apply L->L (gather fused, CSR scatter), "
+                               f"jittered hex mesh n={args.n}^3, p={args.p}, q={args.p + 2}, "
+                               f"{ndofs} DOFs per GPU, x~U[-1,1]",
+                   "ne": ne, "ndofs": ndofs, "p": args.p, "q1d": Q, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (qdata %.2f GB); no flush" % (integ.qdata.numel() * 8 / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": f"{args.kind}_apply (gather fused)",
+                     "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind},
+        "e2e": {"value": e2e, "unit": "GDOF/s", "h2d_bytes_per_step": ndofs * 8,
+                "d2h_bytes_per_step": ndofs * 8},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        try:
+            rate, sn, threads, dt = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, 3)
+            line["cpu_baseline"] = {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
+                                    "sample": f"3 applies of the n={args.cpu_sample_n} p={args.p} mesh "
+                                              f"({sn} DOFs), {dt:.1f} s"}
+        except Exception as e:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_extras(args, fes, integ, op, x, y):
+    """FP32 twin of the operator and the same apply in FP32 (the inner operator
+    of the mixed-precision form)."""
+    import torch
+    from mfem_gb300.pa import PAOperator
+    out = {}
+    op32 = PAOperator(0 if args.kind == "diffusion" else 1, fes, integ.D, integ.Q, integ.B, integ.G,
+                      integ.qdata, precision=1)
+    x32, y32 = x.float(), y.float()
+    for _ in range(3):
+        op32.Mult(x32, y32)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(args.steps):
+        op32.Mult(x32, y32)
+    b.record(s)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    out["fp32_apply"] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
+                         "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, 4, args.kind,
+                                                           False) / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0]}
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

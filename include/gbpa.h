@@ -1,0 +1,303 @@
+/* gbpa.h -- GB300-native partial-assembly H1 operator library (C ABI).
+ *
+ * Drop-in device kernels for MFEM's partial-assembly (PA) H1 path:
+ * ElementRestriction gather/scatter, geometric factors, diffusion/mass
+ * quadrature-data setup, the sum-factorised 3D diffusion/mass applies and
+ * their Jacobi diagonals, and the PCG vector kernels. The reference call site
+ * each entry point replaces is cited beside it (paths inside the MFEM tree).
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless the comment says
+ *    "host". Ownership stays with the caller; the library allocates only its
+ *    own scratch, which lives in the context.
+ *  - Layouts are MFEM's column-major ones:
+ *      B, G   (Q, D)                B[q + Q*d];  Bt, Gt (D, Q)
+ *      W      (Q, Q, Q)
+ *      J      (Q, Q, Q, 3, 3, NE)   J(qx,qy,qz,row,col,e) = d x_row / d xi_col
+ *      detJ   (Q^3, NE)
+ *      qdata  diffusion (Q, Q, Q, S, NE), S = 6 (symmetric, entries
+ *             11,12,13,22,23,33) or 9 (nonsymmetric, row-major 3x3);
+ *             mass (Q, Q, Q, NE)
+ *      E-vector (D, D, D, NE); L-vector (ndofs) -- vdim = 1 unless stated.
+ *  - The return value is GBPA_SUCCESS (0) or a negative GBPA_ERR_* code.
+ *    Nothing aborts inside the library; kernels that detect a data error
+ *    (non-finite scalar in PCG, zero diagonal) set a sticky flag that
+ *    gbpa_get_error_flags() reads and clears.
+ *  - Work is enqueued on the context's stream; calls return without waiting
+ *    unless they produce a host-visible result (dots, solver statistics).
+ */
+#ifndef GBPA_H
+#define GBPA_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBPA_VERSION 10000
+
+enum gbpa_status
+{
+   GBPA_SUCCESS = 0,
+   GBPA_ERR_INVALID_ARGUMENT = -1,
+   GBPA_ERR_UNSUPPORTED = -2,  /* (D, Q) outside 1..16, vdim > 3, ... */
+   GBPA_ERR_CUDA = -3,         /* a CUDA runtime call failed */
+   GBPA_ERR_NOT_FINITE = -4,   /* PCG produced a non-finite scalar */
+   GBPA_ERR_ZERO_DIAGONAL = -5,
+   GBPA_ERR_NOT_CONVERGED = -6,
+   GBPA_ERR_TIMEOUT = -7,
+   GBPA_ERR_OUT_OF_MEMORY = -8,
+   GBPA_ERR_INDEX = -9         /* an index map entry out of range */
+};
+
+/* Sticky device-side error flags (bit mask). */
+enum gbpa_error_flag
+{
+   GBPA_FLAG_NOT_FINITE = 1,
+   GBPA_FLAG_ZERO_DIAGONAL = 2,
+   GBPA_FLAG_INDEX = 4,
+   GBPA_FLAG_INDEFINITE = 8
+};
+
+typedef struct gbpa_ctx *gbpa_ctx_t;
+
+/* ------------------------------------------------------------ context */
+/* Replaces Device("cuda") configuration: general/device.cpp:191,443-453. */
+int gbpa_version(void);
+const char *gbpa_error_string(int status);
+int gbpa_create(gbpa_ctx_t *ctx, int device);
+int gbpa_destroy(gbpa_ctx_t ctx);
+/* Use `stream` (a cudaStream_t) for all later work; NULL restores the
+ * context's own non-blocking stream. */
+int gbpa_set_stream(gbpa_ctx_t ctx, void *stream);
+void *gbpa_get_stream(gbpa_ctx_t ctx);
+int gbpa_synchronize(gbpa_ctx_t ctx);
+/* host out: flags; clears the device flags. */
+int gbpa_get_error_flags(gbpa_ctx_t ctx, int *flags);
+/* Number of kernels this context has launched (for launch accounting). */
+int64_t gbpa_launch_count(gbpa_ctx_t ctx);
+
+/* -------------------------------------------------- element restriction */
+/* ElementRestriction constructor, fem/restriction.cpp:26-114 (host arrays).
+ * elem_dofs: element-to-dof table J array (ne x dof, signed, native order);
+ * dof_map: lexicographic-to-native map of the element (may be NULL for
+ * native ordering). Outputs (host): offsets[ndofs+1], indices[ne*dof],
+ * gather_map[ne*dof]. Bit-identical to the reference's maps. */
+int gbpa_restriction_build(int ne, int dof, int ndofs, const int *elem_dofs,
+                           const int *dof_map, int *offsets, int *indices,
+                           int *gather_map);
+/* Same construction on the device (all pointers device); gbpa-owned scratch. */
+int gbpa_restriction_build_device(gbpa_ctx_t ctx, int ne, int dof, int ndofs,
+                                  const int *elem_dofs, const int *dof_map,
+                                  int *offsets, int *indices, int *gather_map);
+/* ElementRestriction::Mult, fem/restriction.cpp:116-136:
+ * y(i%nd, c, i/nd) = +-x(gather_map[i], c). byvdim: L-vector ordering. */
+int gbpa_restriction_mult(gbpa_ctx_t ctx, int ne, int nd, int vdim, int byvdim,
+                          int ndofs, const int *gather_map, const double *x,
+                          double *y);
+/* ElementRestriction::AbsMult, fem/restriction.cpp:138-157. */
+int gbpa_restriction_abs_mult(gbpa_ctx_t ctx, int ne, int nd, int vdim,
+                              int byvdim, int ndofs, const int *gather_map,
+                              const double *x, double *y);
+/* ElementRestriction::MultTranspose / AddMultTranspose,
+ * fem/restriction.cpp:159-201 (add != 0 accumulates into y). Deterministic:
+ * each L-dof sums its E-entries in CSR order, as the reference does. */
+int gbpa_restriction_mult_transpose(gbpa_ctx_t ctx, int ne, int nd, int vdim,
+                                    int byvdim, int ndofs, const int *offsets,
+                                    const int *indices, const double *x,
+                                    double *y, int add);
+/* ElementRestriction::AbsMultTranspose, fem/restriction.cpp:203-228. */
+int gbpa_restriction_abs_mult_transpose(gbpa_ctx_t ctx, int ne, int nd,
+                                        int vdim, int byvdim, int ndofs,
+                                        const int *offsets, const int *indices,
+                                        const double *x, double *y);
+
+/* ---------------------------------------------------- geometric factors */
+/* GeometricFactors::Compute (JACOBIANS), mesh/mesh.cpp:15445-15500 with
+ * QuadratureInterpolator derivatives, fem/qinterp/grad.hpp:233-376:
+ * J (Q,Q,Q,3,3,NE) from the lexicographic nodes E-vector X (Dg,Dg,Dg,3,NE)
+ * and the nodal basis tables Bg, Gg (Q, Dg). */
+int gbpa_geom_jacobians3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
+                          const double *Bg, const double *Gg, const double *X,
+                          double *J);
+/* DETERMINANTS, fem/qinterp/det.hpp:253-330: detJ (Q^3, NE). */
+int gbpa_geom_determinants3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
+                             const double *Bg, const double *Gg,
+                             const double *X, double *detJ);
+/* COORDINATES, fem/qinterp/eval.hpp: physical coordinates of the quadrature
+ * points, layout (Q^3, 3, NE). */
+int gbpa_geom_coordinates3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
+                            const double *Bg, const double *X, double *XQ);
+
+/* ------------------------------------------------------------ diffusion */
+/* PADiffusionSetup3D, fem/integ/bilininteg_diffusion_kernels.cpp:262-386.
+ * coeff_dim: 1 (scalar), 3 (vector/diagonal), 6 (symmetric matrix),
+ * 9 (nonsymmetric matrix, transposed as CoefficientVector::ProjectTranspose
+ * stores it). c_size == coeff_dim means a constant coefficient, else
+ * c_size == coeff_dim*Q^3*NE. Output D has S = (coeff_dim == 9 ? 9 : 6). */
+int gbpa_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int coeff_dim,
+                           const double *W, const double *J, const double *C,
+                           int64_t c_size, double *D);
+/* Fused geometric factors + setup: J is evaluated from the nodes at each
+ * quadrature point and consumed in registers (never stored). */
+int gbpa_diffusion_setup3d_nodes(gbpa_ctx_t ctx, int ne, int dg, int q1d,
+                                 int coeff_dim, const double *W,
+                                 const double *Bg, const double *Gg,
+                                 const double *X, const double *C,
+                                 int64_t c_size, double *D);
+/* DiffusionIntegrator::AddMultPA, fem/integ/bilininteg_diffusion_pa.cpp:41-93
+ * (kernels fem/integ/bilininteg_diffusion_kernels.hpp:796-1215):
+ * y_E += A_e x_E. Bt/Gt may be NULL (B/G are used transposed). */
+int gbpa_diffusion_apply3d(gbpa_ctx_t ctx, int ne, int symm, int d1d, int q1d,
+                           const double *B, const double *G, const double *Bt,
+                           const double *Gt, const double *D, const double *x,
+                           double *y);
+int gbpa_diffusion_apply3d_f32(gbpa_ctx_t ctx, int ne, int symm, int d1d,
+                               int q1d, const float *B, const float *G,
+                               const float *D, const float *x, float *y);
+/* DiffusionIntegrator::AssembleDiagonalPA, fem/integ/bilininteg_diffusion_pa.cpp:23-38
+ * (kernels fem/integ/bilininteg_diffusion_kernels.hpp:268-485): y_E += diag. */
+int gbpa_diffusion_diagonal3d(gbpa_ctx_t ctx, int ne, int symm, int d1d,
+                              int q1d, const double *B, const double *G,
+                              const double *D, double *y);
+
+/* ----------------------------------------------------------------- mass */
+/* MassIntegrator::AssemblePA setup, fem/integ/bilininteg_mass_pa.cpp:73-89:
+ * D = W * c * detJ (by_val) or W * c / detJ. c_size 1 = constant. */
+int gbpa_mass_setup3d(gbpa_ctx_t ctx, int ne, int nq, const double *W,
+                      const double *detJ, const double *C, int64_t c_size,
+                      int by_val, double *D);
+/* MassIntegrator::AddMultPA, fem/integ/bilininteg_mass_pa.cpp:151-205. */
+int gbpa_mass_apply3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
+                      const double *B, const double *Bt, const double *D,
+                      const double *x, double *y);
+int gbpa_mass_apply3d_f32(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
+                          const float *B, const float *D, const float *x,
+                          float *y);
+/* MassIntegrator::AssembleDiagonalPA, fem/integ/bilininteg_mass_pa.cpp:138-149. */
+int gbpa_mass_diagonal3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
+                         const double *B, const double *D, double *y);
+
+/* ------------------------------------------- L-vector PA operator (fused) */
+/* PABilinearFormExtension::Mult for one domain integrator,
+ * fem/bilinearform_ext.cpp:487-564 (restriction -> AddMultPA -> transpose),
+ * optionally wrapped in ConstrainedOperator (linalg/operator.cpp:526-661,
+ * DIAG_ONE). The gather of x is fused into the apply kernel; the scatter is
+ * the deterministic CSR sum (or atomic adds, see GBPA_SCATTER_ATOMIC). */
+enum gbpa_kind { GBPA_DIFFUSION = 0, GBPA_MASS = 1 };
+enum gbpa_precision { GBPA_F64 = 0, GBPA_F32 = 1 };
+enum gbpa_scatter { GBPA_SCATTER_CSR = 0, GBPA_SCATTER_ATOMIC = 1 };
+
+typedef struct gbpa_operator_desc
+{
+   int kind;            /* gbpa_kind */
+   int precision;       /* gbpa_precision of qdata/B/G and of x, y in mult */
+   int ne, ndofs, d1d, q1d;
+   int symm;            /* diffusion: 1 if S = 6 */
+   const void *B, *G;   /* (Q, D) in `precision` */
+   const void *qdata;   /* in `precision` */
+   const int *gather_map, *offsets, *indices;
+   const int *ess;      /* essential (constrained) dofs, may be NULL */
+   int n_ess;
+   int scatter;         /* gbpa_scatter */
+} gbpa_operator_desc;
+
+typedef struct gbpa_operator *gbpa_operator_t;
+
+int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
+                         gbpa_operator_t *op);
+int gbpa_operator_destroy(gbpa_operator_t op);
+/* y = A x (L-vectors, the descriptor's precision). With ess dofs:
+ * y = A (x with ess zeroed), then y[ess] = x[ess]. */
+int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y);
+/* Element part of the operator alone: yE = A_e (R x) with the gather of x
+ * fused into the sum-factorised apply (ElementRestriction::Mult followed by
+ * AddMultPA on a zeroed E-vector, fem/bilinearform_ext.cpp:530-546). yE is
+ * an E-vector (D, D, D, NE) in the descriptor's precision. */
+int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, void *yE);
+/* BilinearForm::AssembleDiagonal (PA), fem/bilinearform_ext.cpp:370-454,
+ * with ConstrainedOperator::AssembleDiagonal DIAG_ONE when ess is set.
+ * diag is always FP64. */
+int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag);
+
+/* -------------------------------------------------------- vector kernels */
+/* Vector::operator* (linalg/vector.cpp:1079-1106) with reduce()
+ * (general/reducers.hpp:531-594): host out *result. Warp-shuffle tree,
+ * fixed order (deterministic for a given n). */
+int gbpa_vec_dot(gbpa_ctx_t ctx, int64_t n, const double *x, const double *y,
+                 double *result);
+/* add(x, a, y, z): z = x + a*y (linalg/vector.cpp:414-600). */
+int gbpa_vec_add(gbpa_ctx_t ctx, int64_t n, const double *x, double a,
+                 const double *y, double *z);
+/* OperatorJacobiSmoother::Setup, linalg/solvers.cpp:401-425:
+ * dinv = damping/diag, dinv[ess] = damping. Zero diagonal -> error status. */
+int gbpa_jacobi_setup(gbpa_ctx_t ctx, int64_t n, const double *diag,
+                      const int *ess, int n_ess, double damping, double *dinv);
+
+/* ------------------------------------------------------------------ PCG */
+typedef struct gbpa_solve_info
+{
+   int iterations;       /* CGSolver::GetNumIterations */
+   int converged;        /* CGSolver::GetConverged */
+   double initial_norm;  /* sqrt((B r0, r0)) */
+   double final_norm;    /* sqrt((B r, r)) at exit, CGSolver::GetFinalNorm */
+   double true_rel_residual; /* ||b - A x|| / ||b|| evaluated in FP64 */
+   int outer_iterations; /* mixed-precision form: defect-correction steps */
+   int inner_iterations; /* mixed-precision form: total FP32 PCG iterations */
+   double seconds;       /* device time of the solve */
+} gbpa_solve_info;
+
+/* CGSolver::Mult, linalg/solvers.cpp:869-1050, preconditioned by
+ * OperatorJacobiSmoother::Mult (linalg/solvers.cpp:427-452, non-iterative):
+ * the whole iteration runs on the device (no host round trip per dot); the
+ * host polls the convergence flag every `check_every` iterations from a
+ * captured CUDA graph. iterative_mode != 0 starts from x. Same stopping
+ * rule as the reference: (B r, r) <= max(rel_tol^2 (B r0, r0), abs_tol^2). */
+int gbpa_pcg_solve(gbpa_operator_t A, const double *dinv, const double *b,
+                   double *x, double rel_tol, double abs_tol, int max_it,
+                   int iterative_mode, gbpa_solve_info *info);
+
+/* Mixed-precision form: FP64 defect correction around FP32 Jacobi-PCG inner
+ * solves. A64 is the FP64 operator (true residual r = b - A x in FP64), A32
+ * its FP32 twin (same maps, FP32 qdata/B/G). Outer loop stops when
+ * ||b - A64 x|| <= outer_rel_tol ||b||; each inner solve stops at relative
+ * preconditioned residual inner_rel_tol. dinv32 is FP32. */
+int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
+                         const float *dinv32, const double *b, double *x,
+                         double outer_rel_tol, double inner_rel_tol,
+                         int max_outer, int max_inner, gbpa_solve_info *info);
+
+/* ---------------------------------------------------------- batched PCG */
+/* Batching form: many independent Dirichlet problems of uneven size and
+ * order, solved together. Each problem owns its maps, qdata and vectors
+ * (device pointers inside the descriptor array, which is itself host
+ * memory). All problems advance in the same persistent launches; a per-
+ * problem converged mask stops finished problems. FP64. */
+typedef struct gbpa_problem_desc
+{
+   int ne, ndofs, d1d, q1d;
+   const double *B, *G, *qdata;          /* symmetric diffusion qdata */
+   const int *gather_map, *offsets, *indices;
+   const int *ess; int n_ess;
+   const double *dinv;                   /* Jacobi inverse diagonal */
+   const double *b;
+   double *x;
+} gbpa_problem_desc;
+
+int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob,
+                           const gbpa_problem_desc *probs, double rel_tol,
+                           double abs_tol, int max_it, int *iterations,
+                           int *converged, double *final_norms,
+                           double *seconds);
+
+/* --------------------------------------------------------------- tuning */
+/* Elements per thread block used by the apply kernels for (kind, precision,
+ * d1d, q1d); 0 = library default. The autotuner (python side) sweeps this. */
+int gbpa_set_elements_per_block(int kind, int precision, int d1d, int q1d,
+                                int nbz);
+int gbpa_get_elements_per_block(int kind, int precision, int d1d, int q1d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBPA_H */

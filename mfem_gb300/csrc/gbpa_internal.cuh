@@ -1,0 +1,87 @@
+// Internal declarations shared by the gbpa CUDA translation units.
+#pragma once
+#include "../../include/gbpa.h"
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#define GBPA_MAX_1D 16       // largest D1D / Q1D handled (the generic kernels)
+
+struct gbpa_ctx
+{
+   int device = 0;
+   int num_sms = 0;
+   cudaStream_t own_stream = nullptr;
+   cudaStream_t stream = nullptr;
+   int *d_flags = nullptr;           // sticky device error flags
+   double *h_pinned = nullptr;       // small pinned host staging area (64 doubles)
+   double *d_scalars = nullptr;      // small device scalar area (64 doubles)
+   unsigned int *d_counter = nullptr;// last-block-done counter for reductions
+   double *d_partials = nullptr;     // per-block partial sums (4096 doubles)
+   int64_t launches = 0;
+   // growable scratch slots (device memory owned by the context)
+   struct Slot { void *ptr = nullptr; size_t bytes = 0; };
+   std::vector<Slot> slots;
+};
+
+namespace gbpa
+{
+enum ScratchSlot
+{
+   SLOT_EVEC_A = 0, SLOT_EVEC_B, SLOT_RESTRICT, SLOT_PCG, SLOT_PCG32,
+   SLOT_BATCH, SLOT_TMP, SLOT_COUNT
+};
+
+void *scratch(gbpa_ctx *ctx, int slot, size_t bytes);   // nullptr on OOM
+int check_cuda(cudaError_t e, const char *what);
+inline int last_launch(gbpa_ctx *ctx, const char *what)
+{
+   ctx->launches++;
+   return check_cuda(cudaGetLastError(), what);
+}
+inline unsigned grid_for(int64_t n, int block, int max_blocks = 1 << 20)
+{
+   int64_t g = (n + block - 1) / block;
+   if (g < 1) { g = 1; }
+   if (g > max_blocks) { g = max_blocks; }
+   return (unsigned)g;
+}
+
+// ---------------------------------------------------------------- kernels
+// E-vector apply kernels (2D-slab: one thread per (qx,qy) column, z in
+// registers, nbz elements per block). gather_map != nullptr: x is an
+// L-vector gathered (with sign) through the map; ess_mask zeroes
+// constrained dofs on the fly. accumulate: y += result, else y = result.
+template <typename T>
+int launch_diffusion_apply(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
+                           const T *B, const T *G, const T *qd, const T *x,
+                           const int *gather_map, const unsigned char *ess_mask,
+                           T *y, bool accumulate, const int *skip = nullptr);
+template <typename T>
+int launch_mass_apply(gbpa_ctx *ctx, int ne, int D, int Q, const T *B,
+                      const T *qd, const T *x, const int *gather_map,
+                      const unsigned char *ess_mask, T *y, bool accumulate,
+                      const int *skip = nullptr);
+int launch_diffusion_diagonal(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
+                              const double *B, const double *G,
+                              const double *qd, double *y);
+int launch_mass_diagonal(gbpa_ctx *ctx, int ne, int D, int Q, const double *B,
+                         const double *qd, double *y);
+
+// Deterministic CSR scatter E -> L: y[i] = sum_j +-xE[indices[j]]; with
+// ess_mask, y[i] = xc[i] on constrained dofs (ConstrainedOperator DIAG_ONE).
+template <typename T>
+int launch_csr_scatter(gbpa_ctx *ctx, int ndofs, const int *offsets,
+                       const int *indices, const T *xE, T *y,
+                       const unsigned char *ess_mask, const T *xc, bool add,
+                       bool abs_values);
+
+// nbz chosen for (kind, precision, D, Q): tuned table or default.
+int elements_per_block(int kind, int precision, int D, int Q);
+
+// Deterministic two-level dot product into a device scalar (double).
+template <typename T>
+int launch_dot(gbpa_ctx *ctx, int64_t n, const T *x, const T *y,
+               double *d_result);
+} // namespace gbpa

@@ -1,0 +1,682 @@
+// L-vector PA operator (restriction + integrator + transpose, optionally
+// constrained), its diagonal, and the device-resident PCG solvers.
+//   PABilinearFormExtension::Mult     fem/bilinearform_ext.cpp:487-564
+//   PABilinearFormExtension::AssembleDiagonal  fem/bilinearform_ext.cpp:370-454
+//   ConstrainedOperator (DIAG_ONE)    linalg/operator.cpp:526-661
+//   CGSolver::Mult                    linalg/solvers.cpp:869-1050
+//   OperatorJacobiSmoother::Mult      linalg/solvers.cpp:427-452
+#include "gbpa_dispatch.cuh"
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+struct PcgState
+{
+   double nom, nom0, den, betanom, alpha, beta, r0;
+   double rel_tol2, abs_tol2;
+   int iter, done, converged, status, final_iter, max_it;
+   unsigned int counter_den, counter_beta, counter_init;
+   int pad;
+};
+
+struct gbpa_operator
+{
+   gbpa_ctx *ctx = nullptr;
+   gbpa_operator_desc d{};
+   unsigned char *mask = nullptr;   // ess mask (ndofs) or null
+   void *yE = nullptr;              // E-vector scratch in the operator's precision
+   // PCG workspace (vectors in the operator's precision)
+   void *r = nullptr, *dv = nullptr, *z = nullptr;
+   double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)
+   PcgState *state = nullptr;
+   int64_t ws_n = 0;
+   cudaGraphExec_t graph = nullptr;
+   const void *graph_x = nullptr, *graph_dinv = nullptr;
+   // mixed-precision helpers (FP64 vectors)
+   double *r64 = nullptr, *t64 = nullptr;
+};
+
+namespace gbpa
+{
+constexpr int PCG_BLOCK = 512;
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) { v += __shfl_down_sync(0xffffffffu, v, o); }
+   return v;
+}
+
+// Block sum; result valid in thread 0. Uses a caller-provided 32-entry buffer.
+__device__ double block_sum_d(double v, double *ws)
+{
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   v = warp_sum_d(v);
+   if (lane == 0) { ws[wid] = v; }
+   __syncthreads();
+   const int nw = (blockDim.x + 31) >> 5;
+   v = threadIdx.x < nw ? ws[threadIdx.x] : 0.0;
+   if (wid == 0) { v = warp_sum_d(v); }
+   __syncthreads();
+   return v;
+}
+
+// Publishes this block's partial and returns true in the last block to
+// arrive (which then sees every partial). Deterministic: the last block sums
+// partials in block order.
+__device__ bool finish_partial(double s, double *partials, unsigned int *counter,
+                               double *total, double *ws)
+{
+   __shared__ bool last;
+   if (threadIdx.x == 0)
+   {
+      partials[blockIdx.x] = s;
+      __threadfence();
+      last = atomicInc(counter, gridDim.x - 1) == gridDim.x - 1;
+   }
+   __syncthreads();
+   if (!last) { return false; }
+   __threadfence();
+   double t = 0.0;
+   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+   {
+      t += ((volatile double *)partials)[b];
+   }
+   t = block_sum_d(t, ws);
+   if (threadIdx.x == 0) { *total = t; }
+   return true;
+}
+
+// init: x = 0 (unless iterative), r = b or r = b - Ax (r holds Ax on entry),
+// z = dinv r, d = z, nom = (d, r)
+template <typename T>
+__global__ void pcg_init_kernel(int64_t n, const T *__restrict__ b, T *__restrict__ x,
+                                T *__restrict__ r, T *__restrict__ z, T *__restrict__ d,
+                                const T *__restrict__ dinv, int iterative,
+                                double *partials, PcgState *st)
+{
+   __shared__ double ws[32];
+   double s = 0.0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      T ri;
+      if (iterative) { ri = b[i] - r[i]; }
+      else { ri = b[i]; x[i] = T(0); }
+      r[i] = ri;
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      d[i] = zi;
+      s += (double)zi * (double)ri;
+   }
+   s = block_sum_d(s, ws);
+   double tot;
+   if (finish_partial(s, partials, &st->counter_init, &tot, ws) && threadIdx.x == 0)
+   {
+      st->nom = st->nom0 = tot;
+      st->iter = 1;
+      st->converged = 0;
+      st->status = 0;
+      st->final_iter = 0;
+      st->done = 0;
+      st->betanom = tot;
+      if (!isfinite(tot)) { st->status = GBPA_ERR_NOT_FINITE; st->done = 1; }
+      else if (tot < 0.0) { st->done = 1; }
+      else
+      {
+         st->r0 = fmax(tot * st->rel_tol2, st->abs_tol2);
+         if (tot <= st->r0) { st->converged = 1; st->done = 1; }
+      }
+   }
+}
+
+// z = CSR scatter of yE (with constraint z[ess] = d[ess]); den = (d, z);
+// then alpha = nom / den (and nom = betanom after the first iteration).
+template <typename T>
+__global__ void pcg_scatter_den_kernel(int ndofs, const int *__restrict__ offsets,
+                                       const int *__restrict__ indices,
+                                       const T *__restrict__ yE, T *__restrict__ z,
+                                       const T *__restrict__ d,
+                                       const unsigned char *__restrict__ mask,
+                                       double *partials, PcgState *st, int first)
+{
+   if (st->done) { return; }
+   __shared__ double ws[32];
+   double s = 0.0;
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndofs; i += gridDim.x * blockDim.x)
+   {
+      T v;
+      if (mask && mask[i]) { v = d[i]; }
+      else
+      {
+         v = T(0);
+         for (int j = offsets[i]; j < offsets[i + 1]; ++j)
+         {
+            const int sj = indices[j];
+            const T a = yE[sj >= 0 ? sj : -1 - sj];
+            v += sj >= 0 ? a : -a;
+         }
+      }
+      z[i] = v;
+      s += (double)d[i] * (double)v;
+   }
+   s = block_sum_d(s, ws);
+   double den;
+   if (finish_partial(s, partials, &st->counter_den, &den, ws) && threadIdx.x == 0)
+   {
+      st->den = den;
+      if (!isfinite(den)) { st->status = GBPA_ERR_NOT_FINITE; st->done = 1; st->final_iter = st->iter; }
+      else if (den == 0.0) { st->done = 1; st->final_iter = st->iter; }
+      else
+      {
+         if (!first) { st->nom = st->betanom; }
+         st->alpha = st->nom / den;
+      }
+   }
+}
+
+// x += alpha d; r -= alpha z; z = dinv r; betanom = (r, z); stopping test;
+// beta = betanom / nom.
+template <typename T>
+__global__ void pcg_update_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r,
+                                  T *__restrict__ z, const T *__restrict__ d,
+                                  const T *__restrict__ dinv, double *partials, PcgState *st)
+{
+   if (st->done) { return; }
+   __shared__ double ws[32];
+   const T alpha = (T)st->alpha;
+   double s = 0.0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      x[i] += alpha * d[i];
+      const T ri = r[i] - alpha * z[i];
+      r[i] = ri;
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      s += (double)ri * (double)zi;
+   }
+   s = block_sum_d(s, ws);
+   double bn;
+   if (finish_partial(s, partials, &st->counter_beta, &bn, ws) && threadIdx.x == 0)
+   {
+      st->betanom = bn;
+      if (!isfinite(bn)) { st->status = GBPA_ERR_NOT_FINITE; st->done = 1; st->final_iter = st->iter; }
+      else if (bn < 0.0) { st->done = 1; st->final_iter = st->iter; }
+      else if (bn <= st->r0) { st->converged = 1; st->done = 1; st->final_iter = st->iter; }
+      else if (++st->iter > st->max_it) { st->done = 1; st->final_iter = st->max_it; }
+      else { st->beta = bn / st->nom; }
+   }
+}
+
+// d = z + beta d
+template <typename T>
+__global__ void pcg_direction_kernel(int64_t n, const T *__restrict__ z, T *__restrict__ d,
+                                     const PcgState *st)
+{
+   if (st->done) { return; }
+   const T beta = (T)st->beta;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      d[i] = z[i] + beta * d[i];
+   }
+}
+
+__global__ void fill_mask_kernel(int n, const int *ess, unsigned char *mask, int ndofs, int *flags)
+{
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+   {
+      const int k = ess[i];
+      if (k < 0 || k >= ndofs) { atomicOr(flags, GBPA_FLAG_INDEX); continue; }
+      mask[k] = 1;
+   }
+}
+
+__global__ void set_mask_one_kernel(int ndofs, const unsigned char *mask, double *y)
+{
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndofs; i += gridDim.x * blockDim.x)
+   {
+      if (mask[i]) { y[i] = 1.0; }
+   }
+}
+
+// mixed-precision helpers
+__global__ void scale_to_f32_kernel(int64_t n, const double *r, const double *nrm2, float *r32)
+{
+   const double s = 1.0 / sqrt(*nrm2);
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      r32[i] = (float)(r[i] * s);
+   }
+}
+__global__ void correct_kernel(int64_t n, double *x, const float *c32, const double *nrm2)
+{
+   const double s = sqrt(*nrm2);
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      x[i] += s * (double)c32[i];
+   }
+}
+__global__ void residual_kernel(int64_t n, const double *b, double *r)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      r[i] = b[i] - r[i];
+   }
+}
+
+} // namespace gbpa
+
+using namespace gbpa;
+
+static int64_t evec_size(const gbpa_operator_desc &d)
+{
+   return (int64_t)d.ne * d.d1d * d.d1d * d.d1d;
+}
+static size_t elem_bytes(const gbpa_operator_desc &d) { return d.precision == GBPA_F64 ? 8 : 4; }
+
+extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
+                                    gbpa_operator_t *out)
+{
+   if (!ctx || !desc || !out) { return GBPA_ERR_INVALID_ARGUMENT; }
+   *out = nullptr;
+   const gbpa_operator_desc &d = *desc;
+   if (d.kind != GBPA_DIFFUSION && d.kind != GBPA_MASS) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.precision != GBPA_F64 && d.precision != GBPA_F32) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.d1d < 1 || d.q1d < 1 || d.d1d > GBPA_MAX_1D || d.q1d > GBPA_MAX_1D) { return GBPA_ERR_UNSUPPORTED; }
+   if (d.ne > 0 && (!d.B || !d.qdata || !d.gather_map || !d.offsets || !d.indices)) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.kind == GBPA_DIFFUSION && d.ne > 0 && !d.G) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.n_ess > 0 && !d.ess) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.scatter != GBPA_SCATTER_CSR && d.scatter != GBPA_SCATTER_ATOMIC) { return GBPA_ERR_INVALID_ARGUMENT; }
+   gbpa_operator *op = new (std::nothrow) gbpa_operator;
+   if (!op) { return GBPA_ERR_OUT_OF_MEMORY; }
+   op->ctx = ctx;
+   op->d = d;
+   int rc = GBPA_SUCCESS;
+   const int64_t nE = evec_size(d);
+   if (nE > 0) { rc = check_cuda(cudaMalloc(&op->yE, elem_bytes(d) * nE), "cudaMalloc(yE)"); }
+   if (!rc && d.n_ess > 0)
+   {
+      rc = check_cuda(cudaMalloc(&op->mask, d.ndofs), "cudaMalloc(mask)");
+      if (!rc) { rc = check_cuda(cudaMemsetAsync(op->mask, 0, d.ndofs, ctx->stream), "memset"); }
+      if (!rc)
+      {
+         fill_mask_kernel<<<grid_for(d.n_ess, 256), 256, 0, ctx->stream>>>(d.n_ess, d.ess, op->mask,
+                                                                         d.ndofs, ctx->d_flags);
+         rc = last_launch(ctx, "fill_mask");
+      }
+      int flags = 0;
+      if (!rc) { rc = gbpa_get_error_flags(ctx, &flags); }
+      if (!rc && (flags & GBPA_FLAG_INDEX)) { rc = GBPA_ERR_INDEX; }
+   }
+   if (rc) { gbpa_operator_destroy(op); return rc; }
+   *out = op;
+   return GBPA_SUCCESS;
+}
+
+extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
+{
+   if (!op) { return GBPA_SUCCESS; }
+   cudaStreamSynchronize(op->ctx->stream);
+   if (op->graph) { cudaGraphExecDestroy(op->graph); }
+   cudaFree(op->yE); cudaFree(op->mask);
+   cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
+   cudaFree(op->partials); cudaFree(op->state);
+   cudaFree(op->r64); cudaFree(op->t64);
+   delete op;
+   return GBPA_SUCCESS;
+}
+
+// yE = A_e (R x) with the gather fused (ess dofs read as zero)
+template <typename T>
+static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
+{
+   const gbpa_operator_desc &d = op->d;
+   if (d.kind == GBPA_DIFFUSION)
+   {
+      return launch_diffusion_apply<T>(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
+                                       (const T *)d.B, (const T *)d.G, (const T *)d.qdata, x,
+                                       d.gather_map, op->mask, (T *)op->yE, false, skip);
+   }
+   return launch_mass_apply<T>(op->ctx, d.ne, d.d1d, d.q1d, (const T *)d.B,
+                               (const T *)d.qdata, x, d.gather_map, op->mask, (T *)op->yE,
+                               false, skip);
+}
+
+template <typename T>
+static int op_mult(gbpa_operator *op, const T *x, T *y)
+{
+   int rc = apply_evec<T>(op, x, nullptr);
+   if (rc) { return rc; }
+   return launch_csr_scatter<T>(op->ctx, op->d.ndofs, op->d.offsets, op->d.indices,
+                                (const T *)op->yE, y, op->mask, x, false, false);
+}
+
+extern "C" int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y)
+{
+   if (!op || (op->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (op->d.ndofs == 0) { return GBPA_SUCCESS; }
+   if (op->d.precision == GBPA_F64) { return op_mult<double>(op, (const double *)x, (double *)y); }
+   return op_mult<float>(op, (const float *)x, (float *)y);
+}
+
+extern "C" int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, void *yE)
+{
+   if (!op || (op->d.ne > 0 && (!x || !yE))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (op->d.ne == 0) { return GBPA_SUCCESS; }
+   void *saved = op->yE;
+   op->yE = yE;
+   const int rc = op->d.precision == GBPA_F64 ? apply_evec<double>(op, (const double *)x, nullptr)
+                                              : apply_evec<float>(op, (const float *)x, nullptr);
+   op->yE = saved;
+   return rc;
+}
+
+extern "C" int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag)
+{
+   if (!op || (op->d.ndofs > 0 && !diag)) { return GBPA_ERR_INVALID_ARGUMENT; }
+   const gbpa_operator_desc &d = op->d;
+   if (d.ndofs == 0) { return GBPA_SUCCESS; }
+   if (d.precision != GBPA_F64) { return GBPA_ERR_UNSUPPORTED; }
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t nE = evec_size(d);
+   int rc = check_cuda(cudaMemsetAsync(op->yE, 0, sizeof(double) * nE, ctx->stream), "memset");
+   if (rc) { return rc; }
+   if (d.kind == GBPA_DIFFUSION)
+   {
+      rc = launch_diffusion_diagonal(ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d, (const double *)d.B,
+                                     (const double *)d.G, (const double *)d.qdata, (double *)op->yE);
+   }
+   else
+   {
+      rc = launch_mass_diagonal(ctx, d.ne, d.d1d, d.q1d, (const double *)d.B,
+                                (const double *)d.qdata, (double *)op->yE);
+   }
+   if (rc) { return rc; }
+   rc = launch_csr_scatter<double>(ctx, d.ndofs, d.offsets, d.indices, (const double *)op->yE,
+                                   diag, nullptr, nullptr, false, true);
+   if (rc || !op->mask) { return rc; }
+   set_mask_one_kernel<<<grid_for(d.ndofs, 256), 256, 0, ctx->stream>>>(d.ndofs, op->mask, diag);
+   return last_launch(ctx, "diag_ess_one");
+}
+
+// ------------------------------------------------------------------- PCG
+static int ensure_pcg_workspace(gbpa_operator *op)
+{
+   const int64_t n = op->d.ndofs;
+   if (op->ws_n >= n && op->state) { return GBPA_SUCCESS; }
+   const size_t w = elem_bytes(op->d);
+   cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z); cudaFree(op->partials); cudaFree(op->state);
+   op->r = op->dv = op->z = nullptr; op->partials = nullptr; op->state = nullptr;
+   int rc = check_cuda(cudaMalloc(&op->r, w * n), "cudaMalloc(r)");
+   if (!rc) { rc = check_cuda(cudaMalloc(&op->dv, w * n), "cudaMalloc(d)"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&op->z, w * n), "cudaMalloc(z)"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&op->partials, sizeof(double) * 4096), "cudaMalloc(partials)"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&op->state, sizeof(PcgState)), "cudaMalloc(state)"); }
+   if (!rc) { rc = check_cuda(cudaMemset(op->state, 0, sizeof(PcgState)), "memset(state)"); }
+   if (!rc) { op->ws_n = n; }
+   if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+   return rc;
+}
+
+static int pcg_check_every()
+{
+   const char *s = getenv("GBPA_PCG_CHECK_EVERY");
+   const int k = s ? atoi(s) : 10;
+   return k >= 1 && k <= 1000 ? k : 10;
+}
+
+// One PCG iteration body: update (x, r, z, betanom), direction, A d, den.
+template <typename T>
+static int pcg_iteration(gbpa_operator *op, T *x, const T *dinv, unsigned grid)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = op->d.ndofs;
+   T *r = (T *)op->r, *d = (T *)op->dv, *z = (T *)op->z;
+   pcg_update_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, x, r, z, d, dinv, op->partials,
+                                                           op->state);
+   int rc = last_launch(ctx, "pcg_update");
+   if (rc) { return rc; }
+   pcg_direction_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, z, d, op->state);
+   rc = last_launch(ctx, "pcg_direction");
+   if (rc) { return rc; }
+   rc = apply_evec<T>(op, d, &op->state->done);
+   if (rc) { return rc; }
+   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
+      op->partials + 2048, op->state, 0);
+   return last_launch(ctx, "pcg_scatter_den");
+}
+
+template <typename T>
+static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double rel_tol,
+                   double abs_tol, int max_it, int iterative, gbpa_solve_info *info,
+                   float *elapsed_ms)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = op->d.ndofs;
+   int rc = ensure_pcg_workspace(op);
+   if (rc) { return rc; }
+   T *r = (T *)op->r, *d = (T *)op->dv, *z = (T *)op->z;
+   const unsigned grid = grid_for(n, PCG_BLOCK, 2 * ctx->num_sms);
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   PcgState h{};
+   h.rel_tol2 = rel_tol * rel_tol;
+   h.abs_tol2 = abs_tol * abs_tol;
+   h.max_it = max_it;
+   rc = check_cuda(cudaMemcpyAsync(op->state, &h, sizeof(PcgState), cudaMemcpyHostToDevice,
+                                   ctx->stream), "cudaMemcpyAsync(state)");
+   if (rc) { return rc; }
+   if (iterative)
+   {
+      rc = op_mult<T>(op, x, r);   // r = A x, then r = b - r in the init kernel
+      if (rc) { return rc; }
+   }
+   pcg_init_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, b, x, r, z, d, dinv, iterative,
+                                                         op->partials, op->state);
+   rc = last_launch(ctx, "pcg_init");
+   if (rc) { return rc; }
+   // z = A d, den = (d, z), alpha = nom / den
+   rc = apply_evec<T>(op, d, &op->state->done);
+   if (rc) { return rc; }
+   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
+      op->partials + 2048, op->state, 1);
+   rc = last_launch(ctx, "pcg_scatter_den");
+   if (rc) { return rc; }
+
+   const int K = pcg_check_every();
+   if (!op->graph || op->graph_x != (const void *)x || op->graph_dinv != (const void *)dinv)
+   {
+      if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+      cudaGraph_t g;
+      rc = check_cuda(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
+                      "cudaStreamBeginCapture");
+      if (rc) { return rc; }
+      for (int k = 0; k < K && !rc; ++k) { rc = pcg_iteration<T>(op, x, dinv, grid); }
+      const int rc2 = check_cuda(cudaStreamEndCapture(ctx->stream, &g), "cudaStreamEndCapture");
+      if (rc || rc2) { return rc ? rc : rc2; }
+      rc = check_cuda(cudaGraphInstantiate(&op->graph, g, 0), "cudaGraphInstantiate");
+      cudaGraphDestroy(g);
+      if (rc) { return rc; }
+      op->graph_x = x; op->graph_dinv = dinv;
+   }
+   int *h_done = (int *)ctx->h_pinned;
+   // graph launches are counted as K iterations' worth of kernels
+   const int per_iter = 4;
+   for (int launched = 0; ; launched += K)
+   {
+      rc = check_cuda(cudaMemcpyAsync(h_done, &op->state->done, sizeof(int),
+                                      cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync(done)");
+      if (rc) { return rc; }
+      rc = check_cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+      if (rc) { return rc; }
+      if (*h_done) { break; }
+      if (launched > max_it + K) { break; }   // safety net; the device caps iterations
+      rc = check_cuda(cudaGraphLaunch(op->graph, ctx->stream), "cudaGraphLaunch");
+      if (rc) { return rc; }
+      ctx->launches += (int64_t)K * per_iter;
+   }
+   cudaEventRecord(e1, ctx->stream);
+   cudaEventSynchronize(e1);
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, e0, e1);
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   if (elapsed_ms) { *elapsed_ms = ms; }
+   rc = check_cuda(cudaMemcpy(&h, op->state, sizeof(PcgState), cudaMemcpyDeviceToHost),
+                   "cudaMemcpy(state)");
+   if (rc) { return rc; }
+   if (info)
+   {
+      info->iterations = h.final_iter;
+      info->converged = h.converged;
+      info->initial_norm = h.nom0 >= 0 ? sqrt(h.nom0) : h.nom0;
+      info->final_norm = h.betanom >= 0 ? sqrt(h.betanom) : h.betanom;
+   }
+   if (h.status) { return h.status; }
+   return GBPA_SUCCESS;
+}
+
+// ||b - A x|| / ||b|| in FP64 (op must be FP64); uses op->r64/t64.
+static int true_residual(gbpa_operator *op, const double *b, const double *x, double *rel)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = op->d.ndofs;
+   if (!op->r64)
+   {
+      int rc = check_cuda(cudaMalloc(&op->r64, sizeof(double) * n), "cudaMalloc(r64)");
+      if (!rc) { rc = check_cuda(cudaMalloc(&op->t64, sizeof(double) * 8), "cudaMalloc(t64)"); }
+      if (rc) { return rc; }
+   }
+   int rc = op_mult<double>(op, x, op->r64);
+   if (rc) { return rc; }
+   residual_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, b, op->r64);
+   rc = last_launch(ctx, "residual");
+   if (rc) { return rc; }
+   rc = launch_dot<double>(ctx, n, op->r64, op->r64, op->t64);
+   if (!rc) { rc = launch_dot<double>(ctx, n, b, b, op->t64 + 1); }
+   if (rc) { return rc; }
+   double h[2];
+   rc = check_cuda(cudaMemcpyAsync(h, op->t64, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                   ctx->stream), "cudaMemcpyAsync");
+   if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+   *rel = h[1] > 0 ? sqrt(h[0] / h[1]) : sqrt(h[0]);
+   return rc;
+}
+
+extern "C" int gbpa_pcg_solve(gbpa_operator_t A, const double *dinv, const double *b, double *x,
+                              double rel_tol, double abs_tol, int max_it, int iterative_mode,
+                              gbpa_solve_info *info)
+{
+   if (!A || (A->d.ndofs > 0 && (!dinv || !b || !x)) || max_it < 0 || rel_tol < 0 || abs_tol < 0)
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   if (A->d.precision != GBPA_F64) { return GBPA_ERR_INVALID_ARGUMENT; }
+   gbpa_solve_info tmp{};
+   gbpa_solve_info *inf = info ? info : &tmp;
+   memset(inf, 0, sizeof(*inf));
+   if (A->d.ndofs == 0) { inf->converged = 1; return GBPA_SUCCESS; }
+   float ms = 0.f;
+   int rc = pcg_run<double>(A, dinv, b, x, rel_tol, abs_tol, max_it, iterative_mode, inf, &ms);
+   inf->seconds = ms * 1e-3;
+   if (rc) { return rc; }
+   inf->outer_iterations = 1;
+   inf->inner_iterations = inf->iterations;
+   return true_residual(A, b, x, &inf->true_rel_residual);
+}
+
+extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, const float *dinv32,
+                                    const double *b, double *x, double outer_rel_tol,
+                                    double inner_rel_tol, int max_outer, int max_inner,
+                                    gbpa_solve_info *info)
+{
+   if (!A64 || !A32 || A64->d.precision != GBPA_F64 || A32->d.precision != GBPA_F32 ||
+       A64->d.ndofs != A32->d.ndofs || A64->ctx != A32->ctx || max_outer < 1 || max_inner < 1)
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const int64_t n = A64->d.ndofs;
+   if (n > 0 && (!dinv32 || !b || !x)) { return GBPA_ERR_INVALID_ARGUMENT; }
+   gbpa_solve_info tmp{};
+   gbpa_solve_info *inf = info ? info : &tmp;
+   memset(inf, 0, sizeof(*inf));
+   if (n == 0) { inf->converged = 1; return GBPA_SUCCESS; }
+   gbpa_ctx *ctx = A64->ctx;
+   int rc = ensure_pcg_workspace(A32);
+   if (rc) { return rc; }
+   if (!A64->r64)
+   {
+      rc = check_cuda(cudaMalloc(&A64->r64, sizeof(double) * n), "cudaMalloc(r64)");
+      if (!rc) { rc = check_cuda(cudaMalloc(&A64->t64, sizeof(double) * 8), "cudaMalloc(t64)"); }
+      if (rc) { return rc; }
+   }
+   // inner-solve vectors: rhs and correction in FP32 (separate from A32's PCG workspace)
+   float *r32 = (float *)scratch(ctx, SLOT_PCG32, sizeof(float) * 2 * n);
+   if (!r32) { return GBPA_ERR_OUT_OF_MEMORY; }
+   float *c32 = r32 + n;
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   // x = 0, r = b
+   rc = check_cuda(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream), "memset(x)");
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(A64->r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream), "copy"); }
+   if (!rc) { rc = launch_dot<double>(ctx, n, b, b, A64->t64 + 1); }
+   if (rc) { return rc; }
+   double hb[2];
+   int outer = 0, inner_total = 0, converged = 0;
+   double rel = 1.0;
+   for (outer = 0; outer <= max_outer; ++outer)
+   {
+      rc = launch_dot<double>(ctx, n, A64->r64, A64->r64, A64->t64);
+      if (rc) { return rc; }
+      rc = check_cuda(cudaMemcpyAsync(hb, A64->t64, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                      ctx->stream), "cudaMemcpyAsync");
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+      if (rc) { return rc; }
+      rel = hb[1] > 0 ? sqrt(hb[0] / hb[1]) : sqrt(hb[0]);
+      if (!std::isfinite(rel)) { return GBPA_ERR_NOT_FINITE; }
+      if (rel <= outer_rel_tol) { converged = 1; break; }
+      if (outer == max_outer || hb[0] == 0.0) { break; }
+      // r32 = r / ||r||; solve A32 c = r32 to inner_rel_tol; x += ||r|| c
+      scale_to_f32_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(
+         n, A64->r64, A64->t64, r32);
+      rc = last_launch(ctx, "scale_to_f32");
+      if (rc) { return rc; }
+      gbpa_solve_info ii{};
+      rc = pcg_run<float>(A32, dinv32, r32, c32, inner_rel_tol, 0.0, max_inner, 0, &ii, nullptr);
+      if (rc) { return rc; }
+      inner_total += ii.iterations;
+      correct_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, x, c32,
+                                                                                A64->t64);
+      rc = last_launch(ctx, "correct");
+      if (rc) { return rc; }
+      // true residual in FP64: r = b - A64 x
+      rc = op_mult<double>(A64, x, A64->r64);
+      if (rc) { return rc; }
+      residual_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, b, A64->r64);
+      rc = last_launch(ctx, "residual");
+      if (rc) { return rc; }
+   }
+   cudaEventRecord(e1, ctx->stream);
+   cudaEventSynchronize(e1);
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, e0, e1);
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   inf->seconds = ms * 1e-3;
+   inf->outer_iterations = outer;
+   inf->inner_iterations = inner_total;
+   inf->iterations = inner_total;
+   inf->converged = converged;
+   inf->true_rel_residual = rel;
+   inf->final_norm = sqrt(hb[0]);
+   return converged ? GBPA_SUCCESS : GBPA_ERR_NOT_CONVERGED;
+}

@@ -1,0 +1,425 @@
+"""Host-side mirror of the reference's partial-assembly interface for this
+path (same class and method names as MFEM, same argument meaning and error
+behaviour), driving the CUDA library through its C ABI. Device memory is held
+in torch tensors; torch is plumbing here, every computation on the path is a
+libgbpa kernel.
+
+    dev = Device("cuda")
+    fes = FiniteElementSpace(CartesianMesh(8), p=3)
+    a = BilinearForm(fes)
+    a.AddDomainIntegrator(DiffusionIntegrator(ir_points=4))
+    a.SetAssemblyLevel(AssemblyLevel.PARTIAL)
+    a.Assemble()
+    A, X, B = a.FormLinearSystem(ess_tdof_list, x, b)
+    M = OperatorJacobiSmoother(a, ess_tdof_list)
+    cg = CGSolver(); cg.SetRelTol(1e-12); cg.SetMaxIter(500)
+    cg.SetOperator(A); cg.SetPreconditioner(M); cg.Mult(B, X)
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .fem import H1Space, Tables, kappa_eval
+
+check = _lib.check
+
+
+def _p(t):
+    """Device pointer of a tensor (or None)."""
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class AssemblyLevel:
+    LEGACY, FULL, ELEMENT, PARTIAL, NONE = range(5)
+
+
+class Device:
+    """mfem::Device("cuda"): owns the library context on one GPU."""
+    _current = None
+
+    def __init__(self, spec="cuda", device_id=0):
+        if spec not in ("cuda", "gpu"):
+            raise ValueError("only the CUDA device is provided by this library")
+        if not torch.cuda.is_available():
+            raise RuntimeError("Device('cuda') requires a CUDA GPU")
+        self.lib = _lib.load()
+        torch.cuda.set_device(device_id)
+        self.torch_device = torch.device("cuda", device_id)
+        h = ctypes.c_void_p()
+        check(self.lib.gbpa_create(ctypes.byref(h), device_id), "gbpa_create")
+        self.ctx = h
+        # run on torch's current stream so torch-side copies are ordered with ours
+        check(self.lib.gbpa_set_stream(self.ctx, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+              "gbpa_set_stream")
+        Device._current = self
+
+    @classmethod
+    def get(cls):
+        if cls._current is None:
+            cls._current = Device("cuda")
+        return cls._current
+
+    def launches(self):
+        return self.lib.gbpa_launch_count(self.ctx)
+
+    def synchronize(self):
+        check(self.lib.gbpa_synchronize(self.ctx), "gbpa_synchronize")
+
+    def error_flags(self):
+        f = ctypes.c_int(0)
+        check(self.lib.gbpa_get_error_flags(self.ctx, ctypes.byref(f)), "gbpa_get_error_flags")
+        return f.value
+
+    def __del__(self):
+        try:
+            if self.ctx:
+                self.lib.gbpa_destroy(self.ctx)
+        except Exception:
+            pass
+
+
+def _dev():
+    return Device.get()
+
+
+def to_dev(a, dtype=None):
+    d = _dev().torch_device
+    if isinstance(a, torch.Tensor):
+        return a.to(device=d, dtype=dtype or a.dtype).contiguous()
+    a = np.ascontiguousarray(a)
+    t = torch.from_numpy(a)
+    return t.to(device=d, dtype=dtype or t.dtype).contiguous()
+
+
+class ElementRestriction:
+    """fem/restriction.cpp ElementRestriction (LEXICOGRAPHIC, vdim 1)."""
+
+    def __init__(self, ne, dof, ndofs, elem_dofs, dof_map=None, build_on_device=False):
+        self.ne, self.dof, self.ndofs = ne, dof, ndofs
+        lib = _dev().lib
+        if build_on_device:
+            ed = to_dev(np.asarray(elem_dofs, np.int32))
+            dm = to_dev(np.asarray(dof_map, np.int32)) if dof_map is not None else None
+            d = _dev().torch_device
+            self.offsets = torch.empty(ndofs + 1, dtype=torch.int32, device=d)
+            self.indices = torch.empty(ne * dof, dtype=torch.int32, device=d)
+            self.gather_map = torch.empty(ne * dof, dtype=torch.int32, device=d)
+            check(lib.gbpa_restriction_build_device(_dev().ctx, ne, dof, ndofs, _p(ed), _p(dm),
+                                                    _p(self.offsets), _p(self.indices),
+                                                    _p(self.gather_map)), "restriction_build_device")
+        else:
+            ed = np.ascontiguousarray(elem_dofs, np.int32)
+            dm = None if dof_map is None else np.ascontiguousarray(dof_map, np.int32)
+            off = np.zeros(ndofs + 1, np.int32)
+            ind = np.zeros(ne * dof, np.int32)
+            gm = np.zeros(ne * dof, np.int32)
+            check(lib.gbpa_restriction_build(ne, dof, ndofs, ed.ctypes.data_as(ctypes.c_void_p),
+                                             None if dm is None else dm.ctypes.data_as(ctypes.c_void_p),
+                                             off.ctypes.data_as(ctypes.c_void_p),
+                                             ind.ctypes.data_as(ctypes.c_void_p),
+                                             gm.ctypes.data_as(ctypes.c_void_p)), "restriction_build")
+            self.offsets, self.indices, self.gather_map = to_dev(off), to_dev(ind), to_dev(gm)
+
+    @classmethod
+    def from_maps(cls, ne, dof, ndofs, gather_map, offsets, indices):
+        r = cls.__new__(cls)
+        r.ne, r.dof, r.ndofs = ne, dof, ndofs
+        r.gather_map, r.offsets, r.indices = to_dev(gather_map), to_dev(offsets), to_dev(indices)
+        return r
+
+    def Mult(self, x, y):
+        check(_dev().lib.gbpa_restriction_mult(_dev().ctx, self.ne, self.dof, 1, 0, self.ndofs,
+                                               _p(self.gather_map), _p(x), _p(y)), "restriction_mult")
+
+    def MultTranspose(self, x, y):
+        check(_dev().lib.gbpa_restriction_mult_transpose(_dev().ctx, self.ne, self.dof, 1, 0, self.ndofs,
+                                                         _p(self.offsets), _p(self.indices), _p(x),
+                                                         _p(y), 0), "restriction_mult_transpose")
+
+    def AddMultTranspose(self, x, y):
+        check(_dev().lib.gbpa_restriction_mult_transpose(_dev().ctx, self.ne, self.dof, 1, 0, self.ndofs,
+                                                         _p(self.offsets), _p(self.indices), _p(x),
+                                                         _p(y), 1), "restriction_add_mult_transpose")
+
+    def AbsMultTranspose(self, x, y):
+        check(_dev().lib.gbpa_restriction_abs_mult_transpose(_dev().ctx, self.ne, self.dof, 1, 0,
+                                                             self.ndofs, _p(self.offsets),
+                                                             _p(self.indices), _p(x), _p(y)),
+              "restriction_abs_mult_transpose")
+
+
+class FiniteElementSpace:
+    """H1 order-p space on a CartesianMesh (global lexicographic numbering)."""
+
+    def __init__(self, mesh, p):
+        self.mesh, self.p = mesh, p
+        self.space = H1Space(mesh, p)
+        self.ndofs = self.space.ndofs
+        self.ne = mesh.ne
+        self._restriction = None
+
+    def GetNDofs(self):
+        return self.ndofs
+
+    def GetTrueVSize(self):
+        return self.ndofs
+
+    def GetNE(self):
+        return self.ne
+
+    def GetElementRestriction(self):
+        if self._restriction is None:
+            self._restriction = ElementRestriction(self.ne, (self.p + 1) ** 3, self.ndofs,
+                                                   self.space.element_dofs(), None)
+        return self._restriction
+
+    def GetBoundaryTrueDofs(self):
+        return self.space.boundary_dofs()
+
+
+class _PAIntegrator:
+    kind = None
+
+    def __init__(self, coeff=None, ir_points=None):
+        # coeff: None (1), float (constant), "kappa" (lognormal field at the
+        # quadrature points), or a callable f(xyz torch (..., 3)) -> values
+        self.coeff = coeff
+        self.ir_points = ir_points
+
+    def quad_points(self, p):
+        return self.ir_points if self.ir_points else p + 2
+
+    def _coefficient(self, fes, tables, geom):
+        dev = _dev()
+        c = self.coeff
+        if c is None or isinstance(c, (int, float)):
+            return to_dev(np.array([1.0 if c is None else float(c)])), 1
+        # non-constant: evaluate at the physical quadrature points on the device
+        ne, Q = fes.ne, tables.Q
+        XQ = torch.empty(Q ** 3 * 3 * ne, dtype=torch.float64, device=dev.torch_device)
+        check(dev.lib.gbpa_geom_coordinates3d(dev.ctx, ne, geom["dg"], Q, _p(geom["Bg"]),
+                                              _p(geom["X"]), _p(XQ)), "geom_coordinates3d")
+        xyz = XQ.view(ne, 3, Q ** 3).permute(0, 2, 1)
+        if c == "kappa":
+            vals = kappa_eval(xyz, geom["modes"])
+        else:
+            vals = c(xyz)
+        return vals.contiguous().view(-1), 1
+
+
+def _geometry(fes, tables, modes):
+    mesh = fes.mesh
+    order = 3 if mesh.curved else 1
+    dg = order + 1
+    gt = Tables(order, tables.Q)
+    X = to_dev(mesh.nodes_evector(order))
+    return {"dg": dg, "Bg": to_dev(gt.B), "Gg": to_dev(gt.G), "X": X, "modes": modes}
+
+
+class DiffusionIntegrator(_PAIntegrator):
+    kind = _lib.GBPA_DIFFUSION
+
+    def AssemblePA(self, fes, modes=None):
+        dev = _dev()
+        p = fes.p
+        self.tables = t = Tables(p, self.quad_points(p))
+        self.fes = fes
+        self.D, self.Q, self.ne = t.D, t.Q, fes.ne
+        self.symm = True
+        geom = _geometry(fes, t, modes)
+        C, cdim = self._coefficient(fes, t, geom)
+        self.B, self.G, self.W = to_dev(t.B), to_dev(t.G), to_dev(t.W)
+        self.qdata = torch.empty(t.Q ** 3 * 6 * fes.ne, dtype=torch.float64, device=dev.torch_device)
+        check(dev.lib.gbpa_diffusion_setup3d_nodes(dev.ctx, fes.ne, geom["dg"], t.Q, cdim, _p(self.W),
+                                                   _p(geom["Bg"]), _p(geom["Gg"]), _p(geom["X"]),
+                                                   _p(C), C.numel(), _p(self.qdata)),
+              "diffusion_setup3d_nodes")
+
+    def AddMultPA(self, x, y):
+        dev = _dev()
+        check(dev.lib.gbpa_diffusion_apply3d(dev.ctx, self.ne, 1, self.D, self.Q, _p(self.B), _p(self.G),
+                                             None, None, _p(self.qdata), _p(x), _p(y)), "diffusion_apply3d")
+
+    def AssembleDiagonalPA(self, y):
+        dev = _dev()
+        check(dev.lib.gbpa_diffusion_diagonal3d(dev.ctx, self.ne, 1, self.D, self.Q, _p(self.B),
+                                                _p(self.G), _p(self.qdata), _p(y)), "diffusion_diagonal3d")
+
+
+class MassIntegrator(_PAIntegrator):
+    kind = _lib.GBPA_MASS
+
+    def AssemblePA(self, fes, modes=None):
+        dev = _dev()
+        p = fes.p
+        self.tables = t = Tables(p, self.quad_points(p))
+        self.fes = fes
+        self.D, self.Q, self.ne = t.D, t.Q, fes.ne
+        self.symm = True
+        geom = _geometry(fes, t, modes)
+        C, _ = self._coefficient(fes, t, geom)
+        self.B, self.G, self.W = to_dev(t.B), to_dev(t.G), to_dev(t.W)
+        detJ = torch.empty(t.Q ** 3 * fes.ne, dtype=torch.float64, device=dev.torch_device)
+        check(dev.lib.gbpa_geom_determinants3d(dev.ctx, fes.ne, geom["dg"], t.Q, _p(geom["Bg"]),
+                                               _p(geom["Gg"]), _p(geom["X"]), _p(detJ)), "geom_det")
+        self.qdata = torch.empty_like(detJ)
+        check(dev.lib.gbpa_mass_setup3d(dev.ctx, fes.ne, t.Q ** 3, _p(self.W), _p(detJ), _p(C), C.numel(),
+                                        1, _p(self.qdata)), "mass_setup3d")
+
+    def AddMultPA(self, x, y):
+        dev = _dev()
+        check(dev.lib.gbpa_mass_apply3d(dev.ctx, self.ne, self.D, self.Q, _p(self.B), None,
+                                        _p(self.qdata), _p(x), _p(y)), "mass_apply3d")
+
+    def AssembleDiagonalPA(self, y):
+        dev = _dev()
+        check(dev.lib.gbpa_mass_diagonal3d(dev.ctx, self.ne, self.D, self.Q, _p(self.B),
+                                           _p(self.qdata), _p(y)), "mass_diagonal3d")
+
+
+class PAOperator:
+    """The library's fused L-vector operator (restriction + integrator +
+    transpose, optionally constrained): one gbpa_operator."""
+
+    def __init__(self, kind, fes_or_maps, D, Q, B, G, qdata, ess=None, precision=_lib.GBPA_F64,
+                 symm=True, scatter=_lib.GBPA_SCATTER_CSR):
+        dev = _dev()
+        R = fes_or_maps.GetElementRestriction() if hasattr(fes_or_maps, "GetElementRestriction") else fes_or_maps
+        self.R = R
+        dt = torch.float64 if precision == _lib.GBPA_F64 else torch.float32
+        self.dtype = dt
+        self.B, self.G, self.qdata = B.to(dt).contiguous(), G.to(dt).contiguous(), qdata.to(dt).contiguous()
+        self.ess = to_dev(np.asarray(ess, np.int32)) if ess is not None and len(ess) else None
+        self.ndofs = R.ndofs
+        desc = _lib.OperatorDesc(kind, precision, R.ne, R.ndofs, D, Q, 1 if symm else 0,
+                                 self.B.data_ptr(), self.G.data_ptr(), self.qdata.data_ptr(),
+                                 R.gather_map.data_ptr(), R.offsets.data_ptr(), R.indices.data_ptr(),
+                                 self.ess.data_ptr() if self.ess is not None else None,
+                                 0 if self.ess is None else self.ess.numel(), scatter)
+        h = ctypes.c_void_p()
+        check(dev.lib.gbpa_operator_create(dev.ctx, ctypes.byref(desc), ctypes.byref(h)), "operator_create")
+        self.handle = h
+
+    def Height(self):
+        return self.ndofs
+
+    def Mult(self, x, y):
+        check(_dev().lib.gbpa_operator_mult(self.handle, _p(x), _p(y)), "operator_mult")
+
+    def AssembleDiagonal(self, diag):
+        check(_dev().lib.gbpa_operator_assemble_diagonal(self.handle, _p(diag)), "operator_assemble_diagonal")
+
+    def __del__(self):
+        try:
+            _dev().lib.gbpa_operator_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class BilinearForm:
+    """BilinearForm with AssemblyLevel::PARTIAL and one domain integrator
+    (fem/bilinearform.cpp, fem/bilinearform_ext.cpp)."""
+
+    def __init__(self, fes):
+        self.fes = fes
+        self.integs = []
+        self.level = AssemblyLevel.LEGACY
+        self.op = None
+
+    def SetAssemblyLevel(self, level):
+        if level != AssemblyLevel.PARTIAL:
+            raise NotImplementedError("only AssemblyLevel.PARTIAL is provided")
+        self.level = level
+
+    def AddDomainIntegrator(self, integ):
+        if self.integs:
+            raise NotImplementedError("one domain integrator per form")
+        self.integs.append(integ)
+
+    def Assemble(self, modes=None, precision=_lib.GBPA_F64):
+        if self.level != AssemblyLevel.PARTIAL:
+            raise RuntimeError("call SetAssemblyLevel(AssemblyLevel.PARTIAL) first")
+        integ = self.integs[0]
+        integ.AssemblePA(self.fes, modes)
+        self.op = PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
+                             precision=precision)
+
+    def Height(self):
+        return self.fes.ndofs
+
+    def Mult(self, x, y):
+        self.op.Mult(x, y)
+
+    def AssembleDiagonal(self, diag):
+        self.op.AssembleDiagonal(diag)
+
+    def ConstrainedOperator(self, ess, precision=_lib.GBPA_F64):
+        integ = self.integs[0]
+        return PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
+                          ess=ess, precision=precision)
+
+    def FormLinearSystem(self, ess_tdof_list, x, b):
+        """Operator::FormLinearSystem (linalg/operator.cpp:129-143) with the
+        ConstrainedOperator's EliminateRHS (linalg/operator.cpp:574-599):
+        B = b - A x_ess, B[ess] = x[ess]; X = x."""
+        A = self.ConstrainedOperator(ess_tdof_list)
+        ess = A.ess
+        w = torch.zeros_like(x)
+        if ess is not None:
+            w[ess.long()] = x[ess.long()]
+        z = torch.empty_like(x)
+        self.op.Mult(w, z)
+        B = b - z
+        if ess is not None:
+            B[ess.long()] = x[ess.long()]
+        return A, x.clone(), B
+
+
+class OperatorJacobiSmoother:
+    """linalg/solvers.cpp:331-452 (non-iterative mode, damping 1)."""
+
+    def __init__(self, a, ess_tdof_list, damping=1.0):
+        dev = _dev()
+        n = a.Height()
+        diag = torch.empty(n, dtype=torch.float64, device=dev.torch_device)
+        a.AssembleDiagonal(diag)
+        self.dinv = torch.empty_like(diag)
+        ess = to_dev(np.asarray(ess_tdof_list, np.int32)) if len(ess_tdof_list) else None
+        check(dev.lib.gbpa_jacobi_setup(dev.ctx, n, _p(diag), _p(ess), 0 if ess is None else ess.numel(),
+                                        damping, _p(self.dinv)), "jacobi_setup")
+
+    def Mult(self, x, y):
+        y.copy_(self.dinv * x)
+
+
+class CGSolver:
+    """linalg/solvers.cpp:869-1050 on the device (see gbpa_pcg_solve)."""
+
+    def __init__(self):
+        self.rel_tol, self.abs_tol, self.max_iter = 0.0, 0.0, 10
+        self.oper, self.prec, self.iterative_mode = None, None, False
+        self.info = _lib.SolveInfo()
+
+    def SetRelTol(self, t): self.rel_tol = t
+    def SetAbsTol(self, t): self.abs_tol = t
+    def SetMaxIter(self, m): self.max_iter = m
+    def SetOperator(self, A): self.oper = A
+    def SetPreconditioner(self, M): self.prec = M
+    def SetPrintLevel(self, _): pass
+
+    def Mult(self, b, x):
+        if self.prec is None:
+            dinv = torch.ones_like(b)
+        else:
+            dinv = self.prec.dinv
+        st = _dev().lib.gbpa_pcg_solve(self.oper.handle, _p(dinv), _p(b), _p(x), self.rel_tol,
+                                       self.abs_tol, self.max_iter, 1 if self.iterative_mode else 0,
+                                       ctypes.byref(self.info))
+        if st not in (0, -6):
+            check(st, "pcg_solve")
+
+    def GetNumIterations(self): return self.info.iterations
+    def GetFinalNorm(self): return self.info.final_norm
+    def GetConverged(self): return bool(self.info.converged)

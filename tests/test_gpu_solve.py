@@ -1,0 +1,99 @@
+"""PCG on the device against the reference's own solve of the Dirichlet
+Poisson problem (unit cube, 8^3 hexes, p = 3, Q = 4, f = 1, PCG + Jacobi,
+rel tol 1e-12): solution within 1e-10 relative L2, same iteration count
+(+-1). The mixed-precision form must reach the FP64 solution within 1e-9."""
+import numpy as np
+import pytest
+import torch
+
+from tests.conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def cfg1_operator():
+    from mfem_gb300.pa import ElementRestriction, PAOperator
+    from tests.gpu_util import T, p, call, zeros, dev
+    dev()
+    g = load_golden("cfg1_solve")
+    ne, ndofs, D, Q = (int(v) for v in g["meta"][:4])
+    qd = zeros(Q ** 3 * 6 * ne)
+    C = T(g["coeff"])
+    call("gbpa_diffusion_setup3d_nodes", ne, 2, Q, 1, p(T(g["W"])), p(T(g["Bg"])), p(T(g["Gg"])),
+         p(T(g["nodesE"])), p(C), C.numel(), p(qd))
+    R = ElementRestriction.from_maps(ne, D ** 3, ndofs, g["gather_map"], g["offsets"], g["indices"])
+    A = PAOperator(0, R, D, Q, T(g["B"]), T(g["G"]), qd, ess=g["ess_tdofs"])
+    A32 = PAOperator(0, R, D, Q, T(g["B"]), T(g["G"]), qd, ess=g["ess_tdofs"], precision=1)
+    return g, ndofs, A, A32
+
+
+def jacobi(g, A, ndofs):
+    from tests.gpu_util import T, p, call, zeros
+    diag = zeros(ndofs)
+    A.AssembleDiagonal(diag)
+    dinv = zeros(ndofs)
+    ess = T(g["ess_tdofs"])
+    call("gbpa_jacobi_setup", ndofs, p(diag), p(ess), ess.numel(), 1.0, p(dinv))
+    return diag, dinv
+
+
+def test_constrained_operator_and_jacobi():
+    from tests.gpu_util import T, H, zeros, relerr
+    g, ndofs, A, _ = cfg1_operator()
+    y = zeros(ndofs)
+    A.Mult(T(g["x"]), y)
+    assert relerr(H(y), g["Ax_constrained"]) < 1e-12
+    diag, dinv = jacobi(g, A, ndofs)
+    assert relerr(H(dinv) * g["x"], g["Mx_jacobi"]) < 1e-12
+
+
+def test_pcg_matches_reference_solve():
+    import ctypes
+    from mfem_gb300 import _lib
+    from tests.gpu_util import T, H, p, zeros, relerr, dev
+    g, ndofs, A, _ = cfg1_operator()
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 500, 0,
+                                  ctypes.byref(info))
+    assert st == 0
+    ref_it, ref_norm, ref_conv = g["cg_info"]
+    assert info.converged == 1
+    assert abs(info.iterations - int(ref_it)) <= 1
+    assert abs(info.final_norm - ref_norm) <= 0.05 * ref_norm
+    assert relerr(H(X), g["X"]) < 1e-10
+    assert info.true_rel_residual < 1e-10
+    # iterative mode from the converged solution: converges immediately
+    st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 500, 1,
+                                  ctypes.byref(info))
+    assert st == 0 and info.iterations <= 2
+
+
+def test_mixed_precision_matches_reference_solve():
+    import ctypes
+    from mfem_gb300 import _lib
+    from tests.gpu_util import T, H, p, zeros, relerr, dev
+    g, ndofs, A, A32 = cfg1_operator()
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    st = dev().lib.gbpa_pcg_solve_mixed(A.handle, A32.handle, p(dinv.float()), p(T(g["B_rhs"])), p(X),
+                                        1e-10, 1e-5, 20, 500, ctypes.byref(info))
+    assert st == 0, info.as_dict()
+    assert info.converged == 1 and info.true_rel_residual <= 1e-10
+    assert relerr(H(X), g["X"]) < 1e-9
+    assert info.outer_iterations >= 2
+
+
+def test_max_iterations_not_converged():
+    import ctypes
+    from mfem_gb300 import _lib
+    from tests.gpu_util import T, p, zeros, dev
+    g, ndofs, A, _ = cfg1_operator()
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 5, 0,
+                                  ctypes.byref(info))
+    assert st == 0 and info.converged == 0 and info.iterations == 5
