@@ -40,45 +40,26 @@ __host__ __device__ inline int mass_smem_per_elem(int D, int Q)
    return a + D * D * Q;
 }
 
-template <typename T, int TD, int TQ, bool GATHER>
-__global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
-                                       const T *__restrict__ gB,
-                                       const T *__restrict__ gG,
-                                       const T *__restrict__ qd,
-                                       const T *__restrict__ x,
-                                       const int *__restrict__ gmap,
-                                       const unsigned char *__restrict__ mask,
-                                       T *__restrict__ y, int accumulate,
-                                       const int *__restrict__ skip)
+// One element of the diffusion apply for thread (tx, ty) of its Q x Q slab.
+// sB/sG: the block's [Q][D] tables in shared memory (already loaded);
+// bufA/bufB: this element's shared buffers (diff_smem_per_elem entries).
+// part == false: the thread has no slot in the layout and only joins the
+// barriers; active == false: the slot's element is past the end (computes
+// on zeros, stores nothing). Every thread of the block must call this.
+template <typename T, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
+__device__ __forceinline__ void
+diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int ty,
+                  int symm, const T *__restrict__ sB, const T *__restrict__ sG,
+                  T *__restrict__ bufA, T *__restrict__ bufB, const T *__restrict__ qd,
+                  const T *__restrict__ x, const int *__restrict__ gmap,
+                  const unsigned char *__restrict__ mask, T *__restrict__ y, int accumulate)
 {
-   if (skip && *skip) { return; }   // uniform per launch: solver finished
-   constexpr int DM = TD ? TD : GBPA_MAX_1D;
-   constexpr int QM = TQ ? TQ : GBPA_MAX_1D;
-   const int D = TD ? TD : d1d;
-   const int Q = TQ ? TQ : q1d;
+   constexpr int DM = TD ? TD : MAXD;
+   constexpr int QM = TQ ? TQ : MAXQ;
    const int D3 = D * D * D, Q3 = Q * Q * Q;
-   const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
-   const int e = blockIdx.x * blockDim.z + tz;
-   const bool active = e < ne;
-
-   extern __shared__ __align__(16) unsigned char smem_raw[];
-   T *sB = reinterpret_cast<T *>(smem_raw);       // [Q][D]
-   T *sG = sB + Q * D;                            // [Q][D]
-   const int per = diff_smem_per_elem(D, Q);
-   T *bufA = sG + Q * D + tz * per;               // X, then T0|T1|T2
-   T *bufB = bufA + (per - 2 * D * D * Q);        // BX|GX, then U0|U12
-
-   const int tid = tx + Q * (ty + Q * tz);
-   const int nthr = Q * Q * blockDim.z;
-   for (int i = tid; i < Q * D; i += nthr)
+   if (part && active)
    {
-      const int q = i % Q, d = i / Q;
-      sB[q * D + d] = gB[i];
-      sG[q * D + d] = gG[i];
-   }
-   if (active)
-   {
-      const long long base = (long long)e * D3;
+      const long long base = e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
       {
          bufA[i] = GATHER ? gather_value(x, gmap, mask, base + i) : x[base + i];
@@ -91,12 +72,12 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
 #pragma unroll
    for (int d = 0; d < DM; ++d)
    {
-      if (d < D) { rBx[d] = sB[tx * D + d]; rGx[d] = sG[tx * D + d]; }
+      if (d < D && part) { rBx[d] = sB[tx * D + d]; rGx[d] = sG[tx * D + d]; }
    }
 
    // stage 1 (x): BX[dz][dy][qx] = sum_dx X[dz][dy][dx] B[qx][dx], GX with G
    T *BX = bufB, *GX = bufB + D * D * Q;
-   for (int dy = ty; dy < D; dy += Q)
+   for (int dy = ty; part && dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
@@ -118,97 +99,103 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    }
    __syncthreads();
 
-   // stage 2 (y) into registers: rA = G_x B_y, rBv = B_x G_y, rC = B_x B_y
-   T rA[DM], rBv[DM], rC[DM];
-#pragma unroll
-   for (int dz = 0; dz < DM; ++dz)
-   {
-      if (dz >= D) { break; }
-      T a = 0, b = 0, c = 0;
-#pragma unroll
-      for (int dy = 0; dy < DM; ++dy)
-      {
-         if (dy >= D) { break; }
-         const T bx = BX[(dz * D + dy) * Q + tx];
-         const T gx = GX[(dz * D + dy) * Q + tx];
-         const T by = sB[ty * D + dy], gy = sG[ty * D + dy];
-         a += gx * by;
-         b += bx * gy;
-         c += bx * by;
-      }
-      rA[dz] = a; rBv[dz] = b; rC[dz] = c;
-   }
-
-   // stage 3 (z) + pointwise qdata + backward z, fused per qz
    T oA[DM], oB[DM], oC[DM];
 #pragma unroll
    for (int dz = 0; dz < DM; ++dz) { oA[dz] = 0; oB[dz] = 0; oC[dz] = 0; }
-   const T *qe = qd + (long long)e * (symm ? 6 : 9) * Q3 + tx + Q * ty;
-#pragma unroll
-   for (int qz = 0; qz < QM; ++qz)
+   if (part)
    {
-      if (qz >= Q) { break; }
-      T gx = 0, gy = 0, gz = 0;
+      // stage 2 (y) into registers: rA = G_x B_y, rBv = B_x G_y, rC = B_x B_y
+      T rA[DM], rBv[DM], rC[DM];
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
-         gx += bz * rA[dz];
-         gy += bz * rBv[dz];
-         gz += gzv * rC[dz];
-      }
-      T ox = 0, oy = 0, oz = 0;
-      if (active)
-      {
-         const T *qp = qe + Q * Q * qz;
-         if (symm)
-         {
-            const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
-            const T O22 = __ldg(qp + 3 * Q3), O23 = __ldg(qp + 4 * Q3);
-            const T O33 = __ldg(qp + 5 * Q3);
-            ox = O11 * gx + O12 * gy + O13 * gz;
-            oy = O12 * gx + O22 * gy + O23 * gz;
-            oz = O13 * gx + O23 * gy + O33 * gz;
-         }
-         else
-         {
-            const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
-            const T O21 = __ldg(qp + 3 * Q3), O22 = __ldg(qp + 4 * Q3);
-            const T O23 = __ldg(qp + 5 * Q3), O31 = __ldg(qp + 6 * Q3);
-            const T O32 = __ldg(qp + 7 * Q3), O33 = __ldg(qp + 8 * Q3);
-            ox = O11 * gx + O12 * gy + O13 * gz;
-            oy = O21 * gx + O22 * gy + O23 * gz;
-            oz = O31 * gx + O32 * gy + O33 * gz;
-         }
-      }
+         T a = 0, b = 0, c = 0;
 #pragma unroll
-      for (int dz = 0; dz < DM; ++dz)
+         for (int dy = 0; dy < DM; ++dy)
+         {
+            if (dy >= D) { break; }
+            const T bx = BX[(dz * D + dy) * Q + tx];
+            const T gx = GX[(dz * D + dy) * Q + tx];
+            const T by = sB[ty * D + dy], gy = sG[ty * D + dy];
+            a += gx * by;
+            b += bx * gy;
+            c += bx * by;
+         }
+         rA[dz] = a; rBv[dz] = b; rC[dz] = c;
+      }
+
+      // stage 3 (z) + pointwise qdata + backward z, fused per qz
+      const T *qe = qd + e * (symm ? 6 : 9) * Q3 + tx + Q * ty;
+#pragma unroll
+      for (int qz = 0; qz < QM; ++qz)
       {
-         if (dz >= D) { break; }
-         const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
-         oA[dz] += bz * ox;
-         oB[dz] += bz * oy;
-         oC[dz] += gzv * oz;
+         if (qz >= Q) { break; }
+         T gx = 0, gy = 0, gz = 0;
+#pragma unroll
+         for (int dz = 0; dz < DM; ++dz)
+         {
+            if (dz >= D) { break; }
+            const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
+            gx += bz * rA[dz];
+            gy += bz * rBv[dz];
+            gz += gzv * rC[dz];
+         }
+         T ox = 0, oy = 0, oz = 0;
+         if (active)
+         {
+            const T *qp = qe + Q * Q * qz;
+            if (symm)
+            {
+               const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
+               const T O22 = __ldg(qp + 3 * Q3), O23 = __ldg(qp + 4 * Q3);
+               const T O33 = __ldg(qp + 5 * Q3);
+               ox = O11 * gx + O12 * gy + O13 * gz;
+               oy = O12 * gx + O22 * gy + O23 * gz;
+               oz = O13 * gx + O23 * gy + O33 * gz;
+            }
+            else
+            {
+               const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
+               const T O21 = __ldg(qp + 3 * Q3), O22 = __ldg(qp + 4 * Q3);
+               const T O23 = __ldg(qp + 5 * Q3), O31 = __ldg(qp + 6 * Q3);
+               const T O32 = __ldg(qp + 7 * Q3), O33 = __ldg(qp + 8 * Q3);
+               ox = O11 * gx + O12 * gy + O13 * gz;
+               oy = O21 * gx + O22 * gy + O23 * gz;
+               oz = O31 * gx + O32 * gy + O33 * gz;
+            }
+         }
+#pragma unroll
+         for (int dz = 0; dz < DM; ++dz)
+         {
+            if (dz >= D) { break; }
+            const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
+            oA[dz] += bz * ox;
+            oB[dz] += bz * oy;
+            oC[dz] += gzv * oz;
+         }
       }
    }
    // T0|T1|T2 [dz][qy][qx] in bufA (X is dead: every thread passed the
    // barrier after stage 1, and stage 2 reads only bufB)
    T *T0 = bufA, *T1 = bufA + D * Q * Q, *T2 = bufA + 2 * D * Q * Q;
-#pragma unroll
-   for (int dz = 0; dz < DM; ++dz)
+   if (part)
    {
-      if (dz >= D) { break; }
-      T0[(dz * Q + ty) * Q + tx] = oA[dz];
-      T1[(dz * Q + ty) * Q + tx] = oB[dz];
-      T2[(dz * Q + ty) * Q + tx] = oC[dz];
+#pragma unroll
+      for (int dz = 0; dz < DM; ++dz)
+      {
+         if (dz >= D) { break; }
+         T0[(dz * Q + ty) * Q + tx] = oA[dz];
+         T1[(dz * Q + ty) * Q + tx] = oB[dz];
+         T2[(dz * Q + ty) * Q + tx] = oC[dz];
+      }
    }
    __syncthreads();
 
    // stage 2^T (y): thread (qx, dy): U0 = sum_qy T0 B[qy][dy],
    // U12 = sum_qy T1 G[qy][dy] + T2 B[qy][dy]  (into bufB)
    T *U0 = bufB, *U12 = bufB + D * D * Q;
-   for (int dy = ty; dy < D; dy += Q)
+   for (int dy = ty; part && dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
@@ -231,9 +218,9 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    __syncthreads();
 
    // stage 1^T (x): thread (dx, dy): y = sum_qx G[qx][dx] U0 + B[qx][dx] U12
-   if (active)
+   if (part && active)
    {
-      const long long base = (long long)e * D3;
+      const long long base = e * D3;
       for (int dy = ty; dy < D; dy += Q)
       {
          for (int dx = tx; dx < D; dx += Q)
@@ -256,6 +243,41 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
          }
       }
    }
+}
+
+template <typename T, int TD, int TQ, bool GATHER>
+__global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
+                                       const T *__restrict__ gB,
+                                       const T *__restrict__ gG,
+                                       const T *__restrict__ qd,
+                                       const T *__restrict__ x,
+                                       const int *__restrict__ gmap,
+                                       const unsigned char *__restrict__ mask,
+                                       T *__restrict__ y, int accumulate,
+                                       const int *__restrict__ skip)
+{
+   if (skip && *skip) { return; }   // uniform per launch: solver finished
+   const int D = TD ? TD : d1d;
+   const int Q = TQ ? TQ : q1d;
+   const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+   const int e = blockIdx.x * blockDim.z + tz;
+
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   T *sB = reinterpret_cast<T *>(smem_raw);       // [Q][D]
+   T *sG = sB + Q * D;                            // [Q][D]
+   const int per = diff_smem_per_elem(D, Q);
+   T *bufA = sG + Q * D + tz * per;               // X, then T0|T1|T2
+   T *bufB = bufA + (per - 2 * D * D * Q);        // BX|GX, then U0|U12
+   const int tid = tx + Q * (ty + Q * tz);
+   const int nthr = Q * Q * blockDim.z;
+   for (int i = tid; i < Q * D; i += nthr)
+   {
+      const int q = i % Q, d = i / Q;
+      sB[q * D + d] = gB[i];
+      sG[q * D + d] = gG[i];
+   }
+   diffusion_element<T, TD, TQ, GATHER>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG, bufA, bufB,
+                                        qd, x, gmap, mask, y, accumulate);
 }
 
 template <typename T, int TD, int TQ, bool GATHER>

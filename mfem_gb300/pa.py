@@ -50,9 +50,11 @@ class Device:
         h = ctypes.c_void_p()
         check(self.lib.gbpa_create(ctypes.byref(h), device_id), "gbpa_create")
         self.ctx = h
-        # run on torch's current stream so torch-side copies are ordered with ours
-        check(self.lib.gbpa_set_stream(self.ctx, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
-              "gbpa_set_stream")
+        # run on torch's current stream so torch-side copies are ordered with
+        # ours; torch's default stream has handle 0, which the library reads as
+        # "own stream", so name the legacy default stream (handle 1) instead
+        h = torch.cuda.current_stream().cuda_stream
+        check(self.lib.gbpa_set_stream(self.ctx, ctypes.c_void_p(h if h else 1)), "gbpa_set_stream")
         Device._current = self
 
     @classmethod
