@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--p", type=int, default=4)
     ap.add_argument("--kind", default="diffusion", choices=["diffusion", "mass"])
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "x2"],
+                    help="arithmetic of the timed operator (x2: FP64 data, double-float on FP32 pipes)")
     ap.add_argument("--cpu-sample-n", type=int, default=38)
     return ap.parse_args()
 
@@ -203,9 +205,13 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     fes, integ, kid = build_problem(args.n, args.p, args.kind)
     ne, ndofs, D, Q = fes.ne, fes.ndofs, integ.D, integ.Q
-    op = PAOperator(kid, fes, D, Q, integ.B, integ.G, integ.qdata)
+    prec = {"f64": 0, "f32": 1, "x2": 2}[args.precision]
+    wbytes = 4 if prec == 1 else 8
+    op = PAOperator(kid, fes, D, Q, integ.B, integ.G, integ.qdata, precision=prec)
     from mfem_gb300 import fem
     x = torch.from_numpy(2 * fem.u01_array(2, ndofs) - 1).cuda()
+    if prec == 1:
+        x = x.float()
     y = torch.empty_like(x)
     P = lambda t: ctypes.c_void_p(t.data_ptr())
 
@@ -236,7 +242,7 @@ def run_gpu(args):
     value = world * ndofs * args.steps / (ms * 1e-3) / 1e9
 
     # ---- dominant kernel alone: gather-fused element apply (E-vector out)
-    yE = torch.empty(ne * D ** 3, dtype=torch.float64, device="cuda")
+    yE = torch.empty(ne * D ** 3, dtype=x.dtype, device="cuda")
     for _ in range(3):
         _lib.check(lib.gbpa_operator_apply_element(op.handle, P(x), P(yE)), "apply_element")
     torch.cuda.synchronize()
@@ -248,14 +254,14 @@ def run_gpu(args):
     k1.record(stream)
     torch.cuda.synchronize()
     k_ms = k0.elapsed_time(k1) / nk
-    kbytes = algorithmic_bytes(ne, ndofs, D, Q, 8, args.kind, element_only=True)
+    kbytes = algorithmic_bytes(ne, ndofs, D, Q, wbytes, args.kind, element_only=True)
     peak, peak_kind = measured_peak_hbm()
     achieved = kbytes / (k_ms * 1e-3) / 1e9
 
     # ---- end to end through the C ABI with host buffers (pinned)
-    hx = torch.empty(ndofs, dtype=torch.float64).pin_memory()
+    hx = torch.empty(ndofs, dtype=x.dtype).pin_memory()
     hx.copy_(x.cpu())
-    hy = torch.empty(ndofs, dtype=torch.float64).pin_memory()
+    hy = torch.empty(ndofs, dtype=x.dtype).pin_memory()
     dx = torch.empty_like(x)
     for _ in range(2):
         dx.copy_(hx, non_blocking=True); op.Mult(dx, y); hy.copy_(y, non_blocking=True)
@@ -276,13 +282,13 @@ def run_gpu(args):
     e2e = world * ndofs * args.steps / (e2e_ms * 1e-3) / 1e9
 
     extras = {}
-    if not args.no_extras and rank == 0:
+    if not args.no_extras and rank == 0 and prec == 0:
         extras = run_extras(args, fes, integ, op, x, y)
 
     line = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": {0: "f64", 1: "f32", 2: "f64x2"}[prec], "data": "synthetic",
         "config": {"workload": f"FP64 PA {args.kind} operator apply L->L (gather fused, CSR scatter), "
                                f"jittered hex mesh n={args.n}^3, p={args.p}, q={args.p + 2}, "
                                f"{ndofs} DOFs per GPU, x~U[-1,1]",
@@ -291,8 +297,8 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "kernel": f"{args.kind}_apply (gather fused)",
                      "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind},
-        "e2e": {"value": e2e, "unit": "GDOF/s", "h2d_bytes_per_step": ndofs * 8,
-                "d2h_bytes_per_step": ndofs * 8},
+        "e2e": {"value": e2e, "unit": "GDOF/s", "h2d_bytes_per_step": ndofs * wbytes,
+                "d2h_bytes_per_step": ndofs * wbytes},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
@@ -334,6 +340,26 @@ def run_extras(args, fes, integ, op, x, y):
     out["fp32_apply"] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
                          "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, 4, args.kind,
                                                            False) / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0]}
+    del op32, x32, y32
+    # FP64 data, double-float arithmetic on the FP32 pipes
+    opx = PAOperator(0 if args.kind == "diffusion" else 1, fes, integ.D, integ.Q, integ.B, integ.G,
+                     integ.qdata, precision=2)
+    yx = torch.empty_like(y)
+    for _ in range(3):
+        opx.Mult(x, yx)
+    op.Mult(x, y)
+    torch.cuda.synchronize()
+    rel = float(torch.linalg.norm(yx - y) / torch.linalg.norm(y))
+    a.record(s)
+    for _ in range(args.steps):
+        opx.Mult(x, yx)
+    b.record(s)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    out["f64x2_apply"] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
+                          "rel_l2_vs_native_f64": rel,
+                          "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, 8, args.kind,
+                                                            False) / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0]}
     return out
 
 

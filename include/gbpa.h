@@ -185,7 +185,12 @@ int gbpa_mass_diagonal3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
  * DIAG_ONE). The gather of x is fused into the apply kernel; the scatter is
  * the deterministic CSR sum (or atomic adds, see GBPA_SCATTER_ATOMIC). */
 enum gbpa_kind { GBPA_DIFFUSION = 0, GBPA_MASS = 1 };
-enum gbpa_precision { GBPA_F64 = 0, GBPA_F32 = 1 };
+/* GBPA_F64X2: FP64 data (qdata, B, G, x, y all FP64) applied with
+ * double-float arithmetic on the FP32 pipes -- each value is an unevaluated
+ * sum of two floats with exact product/sum error terms (~2^-44 relative per
+ * operation) -- because GB300's FP32 rate is ~58x its FP64 rate. The operator
+ * keeps an internal (hi, lo) float copy of qdata (same bytes as FP64). */
+enum gbpa_precision { GBPA_F64 = 0, GBPA_F32 = 1, GBPA_F64X2 = 2 };
 enum gbpa_scatter { GBPA_SCATTER_CSR = 0, GBPA_SCATTER_ATOMIC = 1 };
 
 typedef struct gbpa_operator_desc

@@ -15,7 +15,7 @@ I64 = ctypes.c_int64
 D = ctypes.c_double
 
 GBPA_DIFFUSION, GBPA_MASS = 0, 1
-GBPA_F64, GBPA_F32 = 0, 1
+GBPA_F64, GBPA_F32, GBPA_F64X2 = 0, 1, 2
 GBPA_SCATTER_CSR, GBPA_SCATTER_ATOMIC = 0, 1
 
 STATUS = {

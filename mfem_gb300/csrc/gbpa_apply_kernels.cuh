@@ -1,5 +1,6 @@
-// Sum-factorised 3D diffusion and mass kernels (templated on precision and on
-// compile-time (D, Q); TD = TQ = 0 selects the generic runtime-size variant).
+// Sum-factorised 3D diffusion and mass kernels, templated on an arithmetic
+// (AR) and on compile-time (D, Q); TD = TQ = 0 selects the generic
+// runtime-size variant.
 //
 // Thread layout ("2D slab"): block = (Q, Q, nbz); thread (tx, ty, tz) owns the
 // quadrature column (qx = tx, qy = ty) of element blockIdx.x*nbz + tz and keeps
@@ -9,26 +10,107 @@
 // forward; pointwise 3x3 qdata; z, y, x backward; fem/integ/
 // bilininteg_diffusion_kernels.hpp:989-1215), reorganised so the z-forward,
 // pointwise and z-backward stages fuse into one register loop over qz.
+//
+// Arithmetics:
+//   ArF64  native FP64 (the FP64 pipe: ~1.26 TFLOP/s on GB300)
+//   ArF32  native FP32
+//   ArX2   FP64-accurate "double-float": every value is an unevaluated sum
+//          hi + lo of two floats; products use the exact FMA error term and
+//          sums the exact two-sum error (Dekker 1971; Knuth TAOCP vol. 2,
+//          4.2.2), so all arithmetic runs on the FP32 pipes (58x the FP64
+//          rate on GB300) with ~2^-44 relative error per operation. Inputs and
+//          outputs stay FP64; qdata is stored pre-split as float2 (hi, lo),
+//          the same 8 bytes per entry as FP64.
 #pragma once
 #include "gbpa_internal.cuh"
 
 namespace gbpa
 {
 
-template <typename T>
-__device__ __forceinline__ T gather_value(const T *__restrict__ x,
-                                          const int *__restrict__ gmap,
-                                          const unsigned char *__restrict__ mask,
-                                          long long slot)
+struct f2
+{
+   float h, l;
+};
+
+struct ArF64
+{
+   using V = double; using In = double; using Qd = double;
+   static __device__ __forceinline__ V zero() { return 0.0; }
+   static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fma(a, b, acc); }
+   static __device__ __forceinline__ V in(In x) { return x; }
+   static __device__ __forceinline__ V neg(V a) { return -a; }
+   static __device__ __forceinline__ V fin(V a) { return a; }
+   static __device__ __forceinline__ In out(V v) { return v; }
+   static __device__ __forceinline__ V ldq(const Qd *p) { return __ldg(p); }
+};
+
+struct ArF32
+{
+   using V = float; using In = float; using Qd = float;
+   static __device__ __forceinline__ V zero() { return 0.f; }
+   static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fmaf(a, b, acc); }
+   static __device__ __forceinline__ V in(In x) { return x; }
+   static __device__ __forceinline__ V neg(V a) { return -a; }
+   static __device__ __forceinline__ V fin(V a) { return a; }
+   static __device__ __forceinline__ In out(V v) { return v; }
+   static __device__ __forceinline__ V ldq(const Qd *p) { return __ldg(p); }
+};
+
+struct ArX2
+{
+   using V = f2; using In = double; using Qd = float2;
+   static __device__ __forceinline__ V zero() { return {0.f, 0.f}; }
+   // acc += a * b. The rounded product p = a.h*b.h and its exact error
+   // fma(a.h, b.h, -p) (plus the cross terms) form the addend; acc.h + p is
+   // an exact two-sum whose error joins acc.l. acc.l is left unnormalised
+   // until fin(). The _rn intrinsics keep the compiler from contracting the
+   // rounded operations into FMAs, which would break the error terms.
+   static __device__ __forceinline__ void mac(V &acc, V a, V b)
+   {
+      const float p = __fmul_rn(a.h, b.h);
+      float e = __fmaf_rn(a.h, b.h, -p);
+      e = __fmaf_rn(a.h, b.l, e);
+      e = __fmaf_rn(a.l, b.h, e);
+      const float s = __fadd_rn(acc.h, p);
+      const float bb = __fadd_rn(s, -acc.h);
+      const float err = __fadd_rn(__fadd_rn(acc.h, -__fadd_rn(s, -bb)), __fadd_rn(p, -bb));
+      acc.l = __fadd_rn(acc.l, __fadd_rn(e, err));
+      acc.h = s;
+   }
+   static __device__ __forceinline__ V in(In x)
+   {
+      const float h = __double2float_rn(x);
+      return {h, __double2float_rn(x - (double)h)};
+   }
+   static __device__ __forceinline__ V neg(V a) { return {-a.h, -a.l}; }
+   // renormalise (fast two-sum; |l| << |h|)
+   static __device__ __forceinline__ V fin(V a)
+   {
+      const float s = __fadd_rn(a.h, a.l);
+      return {s, __fadd_rn(a.l, -__fadd_rn(s, -a.h))};
+   }
+   static __device__ __forceinline__ In out(V v) { return (double)v.h + (double)v.l; }
+   static __device__ __forceinline__ V ldq(const Qd *p)
+   {
+      const float2 t = __ldg(p);
+      return {t.x, t.y};
+   }
+};
+
+template <typename AR>
+__device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__restrict__ x,
+                                                       const int *__restrict__ gmap,
+                                                       const unsigned char *__restrict__ mask,
+                                                       long long slot)
 {
    const int g = __ldg(gmap + slot);
    const int j = g >= 0 ? g : -1 - g;
-   if (mask && __ldg(mask + j)) { return T(0); }
-   const T v = __ldg(x + j);
-   return g >= 0 ? v : -v;
+   if (mask && __ldg(mask + j)) { return AR::zero(); }
+   const typename AR::V v = AR::in(__ldg(x + j));
+   return g >= 0 ? v : AR::neg(v);
 }
 
-// Shared memory (in T units) per element for the diffusion apply.
+// Shared memory (in V units) per element for the diffusion apply.
 __host__ __device__ inline int diff_smem_per_elem(int D, int Q)
 {
    const int a = D * D * D > 3 * D * Q * Q ? D * D * D : 3 * D * Q * Q;
@@ -46,14 +128,16 @@ __host__ __device__ inline int mass_smem_per_elem(int D, int Q)
 // part == false: the thread has no slot in the layout and only joins the
 // barriers; active == false: the slot's element is past the end (computes
 // on zeros, stores nothing). Every thread of the block must call this.
-template <typename T, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
 __device__ __forceinline__ void
-diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int ty,
-                  int symm, const T *__restrict__ sB, const T *__restrict__ sG,
-                  T *__restrict__ bufA, T *__restrict__ bufB, const T *__restrict__ qd,
-                  const T *__restrict__ x, const int *__restrict__ gmap,
-                  const unsigned char *__restrict__ mask, T *__restrict__ y, int accumulate)
+diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int ty, int symm,
+                  const typename AR::V *__restrict__ sB, const typename AR::V *__restrict__ sG,
+                  typename AR::V *__restrict__ bufA, typename AR::V *__restrict__ bufB,
+                  const typename AR::Qd *__restrict__ qd, const typename AR::In *__restrict__ x,
+                  const int *__restrict__ gmap, const unsigned char *__restrict__ mask,
+                  typename AR::In *__restrict__ y, int accumulate)
 {
+   using V = typename AR::V;
    constexpr int DM = TD ? TD : MAXD;
    constexpr int QM = TQ ? TQ : MAXQ;
    const int D3 = D * D * D, Q3 = Q * Q * Q;
@@ -62,13 +146,13 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
       const long long base = e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
       {
-         bufA[i] = GATHER ? gather_value(x, gmap, mask, base + i) : x[base + i];
+         bufA[i] = GATHER ? gather_value<AR>(x, gmap, mask, base + i) : AR::in(x[base + i]);
       }
    }
    __syncthreads();
 
    // per-thread copies of row qx of B and G
-   T rBx[DM], rGx[DM];
+   V rBx[DM], rGx[DM];
 #pragma unroll
    for (int d = 0; d < DM; ++d)
    {
@@ -76,143 +160,146 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    }
 
    // stage 1 (x): BX[dz][dy][qx] = sum_dx X[dz][dy][dx] B[qx][dx], GX with G
-   T *BX = bufB, *GX = bufB + D * D * Q;
+   V *BX = bufB, *GX = bufB + D * D * Q;
    for (int dy = ty; part && dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T u = 0, v = 0;
-         const T *xr = bufA + D * (dy + D * dz);
+         V u = AR::zero(), v = AR::zero();
+         const V *xr = bufA + D * (dy + D * dz);
 #pragma unroll
          for (int dx = 0; dx < DM; ++dx)
          {
             if (dx >= D) { break; }
-            const T xv = xr[dx];
-            u += xv * rBx[dx];
-            v += xv * rGx[dx];
+            const V xv = xr[dx];
+            AR::mac(u, xv, rBx[dx]);
+            AR::mac(v, xv, rGx[dx]);
          }
-         BX[(dz * D + dy) * Q + tx] = u;
-         GX[(dz * D + dy) * Q + tx] = v;
+         BX[(dz * D + dy) * Q + tx] = AR::fin(u);
+         GX[(dz * D + dy) * Q + tx] = AR::fin(v);
       }
    }
    __syncthreads();
 
-   T oA[DM], oB[DM], oC[DM];
+   V oA[DM], oB[DM], oC[DM];
 #pragma unroll
-   for (int dz = 0; dz < DM; ++dz) { oA[dz] = 0; oB[dz] = 0; oC[dz] = 0; }
+   for (int dz = 0; dz < DM; ++dz) { oA[dz] = AR::zero(); oB[dz] = AR::zero(); oC[dz] = AR::zero(); }
    if (part)
    {
       // stage 2 (y) into registers: rA = G_x B_y, rBv = B_x G_y, rC = B_x B_y
-      T rA[DM], rBv[DM], rC[DM];
+      V rA[DM], rBv[DM], rC[DM];
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T a = 0, b = 0, c = 0;
+         V a = AR::zero(), b = AR::zero(), c = AR::zero();
 #pragma unroll
          for (int dy = 0; dy < DM; ++dy)
          {
             if (dy >= D) { break; }
-            const T bx = BX[(dz * D + dy) * Q + tx];
-            const T gx = GX[(dz * D + dy) * Q + tx];
-            const T by = sB[ty * D + dy], gy = sG[ty * D + dy];
-            a += gx * by;
-            b += bx * gy;
-            c += bx * by;
+            const V bx = BX[(dz * D + dy) * Q + tx];
+            const V gx = GX[(dz * D + dy) * Q + tx];
+            const V by = sB[ty * D + dy], gy = sG[ty * D + dy];
+            AR::mac(a, gx, by);
+            AR::mac(b, bx, gy);
+            AR::mac(c, bx, by);
          }
-         rA[dz] = a; rBv[dz] = b; rC[dz] = c;
+         rA[dz] = AR::fin(a); rBv[dz] = AR::fin(b); rC[dz] = AR::fin(c);
       }
 
       // stage 3 (z) + pointwise qdata + backward z, fused per qz
-      const T *qe = qd + e * (symm ? 6 : 9) * Q3 + tx + Q * ty;
+      const typename AR::Qd *qe = qd + e * (symm ? 6 : 9) * Q3 + tx + Q * ty;
 #pragma unroll
       for (int qz = 0; qz < QM; ++qz)
       {
          if (qz >= Q) { break; }
-         T gx = 0, gy = 0, gz = 0;
+         V gx = AR::zero(), gy = AR::zero(), gz = AR::zero();
 #pragma unroll
          for (int dz = 0; dz < DM; ++dz)
          {
             if (dz >= D) { break; }
-            const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
-            gx += bz * rA[dz];
-            gy += bz * rBv[dz];
-            gz += gzv * rC[dz];
+            const V bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
+            AR::mac(gx, bz, rA[dz]);
+            AR::mac(gy, bz, rBv[dz]);
+            AR::mac(gz, gzv, rC[dz]);
          }
-         T ox = 0, oy = 0, oz = 0;
+         gx = AR::fin(gx); gy = AR::fin(gy); gz = AR::fin(gz);
+         V ox = AR::zero(), oy = AR::zero(), oz = AR::zero();
          if (active)
          {
-            const T *qp = qe + Q * Q * qz;
+            const typename AR::Qd *qp = qe + Q * Q * qz;
             if (symm)
             {
-               const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
-               const T O22 = __ldg(qp + 3 * Q3), O23 = __ldg(qp + 4 * Q3);
-               const T O33 = __ldg(qp + 5 * Q3);
-               ox = O11 * gx + O12 * gy + O13 * gz;
-               oy = O12 * gx + O22 * gy + O23 * gz;
-               oz = O13 * gx + O23 * gy + O33 * gz;
+               const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
+               const V O22 = AR::ldq(qp + 3 * Q3), O23 = AR::ldq(qp + 4 * Q3);
+               const V O33 = AR::ldq(qp + 5 * Q3);
+               AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
+               AR::mac(oy, O12, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
+               AR::mac(oz, O13, gx); AR::mac(oz, O23, gy); AR::mac(oz, O33, gz);
             }
             else
             {
-               const T O11 = __ldg(qp), O12 = __ldg(qp + Q3), O13 = __ldg(qp + 2 * Q3);
-               const T O21 = __ldg(qp + 3 * Q3), O22 = __ldg(qp + 4 * Q3);
-               const T O23 = __ldg(qp + 5 * Q3), O31 = __ldg(qp + 6 * Q3);
-               const T O32 = __ldg(qp + 7 * Q3), O33 = __ldg(qp + 8 * Q3);
-               ox = O11 * gx + O12 * gy + O13 * gz;
-               oy = O21 * gx + O22 * gy + O23 * gz;
-               oz = O31 * gx + O32 * gy + O33 * gz;
+               const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
+               const V O21 = AR::ldq(qp + 3 * Q3), O22 = AR::ldq(qp + 4 * Q3);
+               const V O23 = AR::ldq(qp + 5 * Q3), O31 = AR::ldq(qp + 6 * Q3);
+               const V O32 = AR::ldq(qp + 7 * Q3), O33 = AR::ldq(qp + 8 * Q3);
+               AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
+               AR::mac(oy, O21, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
+               AR::mac(oz, O31, gx); AR::mac(oz, O32, gy); AR::mac(oz, O33, gz);
             }
+            ox = AR::fin(ox); oy = AR::fin(oy); oz = AR::fin(oz);
          }
 #pragma unroll
          for (int dz = 0; dz < DM; ++dz)
          {
             if (dz >= D) { break; }
-            const T bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
-            oA[dz] += bz * ox;
-            oB[dz] += bz * oy;
-            oC[dz] += gzv * oz;
+            const V bz = sB[qz * D + dz], gzv = sG[qz * D + dz];
+            AR::mac(oA[dz], bz, ox);
+            AR::mac(oB[dz], bz, oy);
+            AR::mac(oC[dz], gzv, oz);
          }
       }
    }
    // T0|T1|T2 [dz][qy][qx] in bufA (X is dead: every thread passed the
    // barrier after stage 1, and stage 2 reads only bufB)
-   T *T0 = bufA, *T1 = bufA + D * Q * Q, *T2 = bufA + 2 * D * Q * Q;
+   V *T0 = bufA, *T1 = bufA + D * Q * Q, *T2 = bufA + 2 * D * Q * Q;
    if (part)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T0[(dz * Q + ty) * Q + tx] = oA[dz];
-         T1[(dz * Q + ty) * Q + tx] = oB[dz];
-         T2[(dz * Q + ty) * Q + tx] = oC[dz];
+         T0[(dz * Q + ty) * Q + tx] = AR::fin(oA[dz]);
+         T1[(dz * Q + ty) * Q + tx] = AR::fin(oB[dz]);
+         T2[(dz * Q + ty) * Q + tx] = AR::fin(oC[dz]);
       }
    }
    __syncthreads();
 
    // stage 2^T (y): thread (qx, dy): U0 = sum_qy T0 B[qy][dy],
    // U12 = sum_qy T1 G[qy][dy] + T2 B[qy][dy]  (into bufB)
-   T *U0 = bufB, *U12 = bufB + D * D * Q;
+   V *U0 = bufB, *U12 = bufB + D * D * Q;
    for (int dy = ty; part && dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T a = 0, b = 0;
+         V a = AR::zero(), b = AR::zero();
 #pragma unroll
          for (int qy = 0; qy < QM; ++qy)
          {
             if (qy >= Q) { break; }
-            const T by = sB[qy * D + dy], gy = sG[qy * D + dy];
+            const V by = sB[qy * D + dy], gy = sG[qy * D + dy];
             const int o = (dz * Q + qy) * Q + tx;
-            a += T0[o] * by;
-            b += T1[o] * gy + T2[o] * by;
+            AR::mac(a, T0[o], by);
+            AR::mac(b, T1[o], gy);
+            AR::mac(b, T2[o], by);
          }
-         U0[(dz * D + dy) * Q + tx] = a;
-         U12[(dz * D + dy) * Q + tx] = b;
+         U0[(dz * D + dy) * Q + tx] = AR::fin(a);
+         U12[(dz * D + dy) * Q + tx] = AR::fin(b);
       }
    }
    __syncthreads();
@@ -229,33 +316,36 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             for (int dz = 0; dz < DM; ++dz)
             {
                if (dz >= D) { break; }
-               T v = 0;
+               V v = AR::zero();
 #pragma unroll
                for (int qx = 0; qx < QM; ++qx)
                {
                   if (qx >= Q) { break; }
                   const int o = (dz * D + dy) * Q + qx;
-                  v += sG[qx * D + dx] * U0[o] + sB[qx * D + dx] * U12[o];
+                  AR::mac(v, sG[qx * D + dx], U0[o]);
+                  AR::mac(v, sB[qx * D + dx], U12[o]);
                }
                const long long k = base + dx + D * (dy + D * dz);
-               y[k] = accumulate ? y[k] + v : v;
+               const typename AR::In r = AR::out(AR::fin(v));
+               y[k] = accumulate ? y[k] + r : r;
             }
          }
       }
    }
 }
 
-template <typename T, int TD, int TQ, bool GATHER>
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
 __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
-                                       const T *__restrict__ gB,
-                                       const T *__restrict__ gG,
-                                       const T *__restrict__ qd,
-                                       const T *__restrict__ x,
+                                       const typename AR::In *__restrict__ gB,
+                                       const typename AR::In *__restrict__ gG,
+                                       const typename AR::Qd *__restrict__ qd,
+                                       const typename AR::In *__restrict__ x,
                                        const int *__restrict__ gmap,
                                        const unsigned char *__restrict__ mask,
-                                       T *__restrict__ y, int accumulate,
+                                       typename AR::In *__restrict__ y, int accumulate,
                                        const int *__restrict__ skip)
 {
+   using V = typename AR::V;
    if (skip && *skip) { return; }   // uniform per launch: solver finished
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
@@ -263,36 +353,37 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    const int e = blockIdx.x * blockDim.z + tz;
 
    extern __shared__ __align__(16) unsigned char smem_raw[];
-   T *sB = reinterpret_cast<T *>(smem_raw);       // [Q][D]
-   T *sG = sB + Q * D;                            // [Q][D]
+   V *sB = reinterpret_cast<V *>(smem_raw);       // [Q][D]
+   V *sG = sB + Q * D;                            // [Q][D]
    const int per = diff_smem_per_elem(D, Q);
-   T *bufA = sG + Q * D + tz * per;               // X, then T0|T1|T2
-   T *bufB = bufA + (per - 2 * D * D * Q);        // BX|GX, then U0|U12
+   V *bufA = sG + Q * D + tz * per;               // X, then T0|T1|T2
+   V *bufB = bufA + (per - 2 * D * D * Q);        // BX|GX, then U0|U12
    const int tid = tx + Q * (ty + Q * tz);
    const int nthr = Q * Q * blockDim.z;
    for (int i = tid; i < Q * D; i += nthr)
    {
       const int q = i % Q, d = i / Q;
-      sB[q * D + d] = gB[i];
-      sG[q * D + d] = gG[i];
+      sB[q * D + d] = AR::in(gB[i]);
+      sG[q * D + d] = AR::in(gG[i]);
    }
-   diffusion_element<T, TD, TQ, GATHER>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG, bufA, bufB,
-                                        qd, x, gmap, mask, y, accumulate);
+   diffusion_element<AR, TD, TQ, GATHER, MAXD, MAXQ>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG,
+                                                     bufA, bufB, qd, x, gmap, mask, y, accumulate);
 }
 
-template <typename T, int TD, int TQ, bool GATHER>
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
 __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
-                                  const T *__restrict__ gB,
-                                  const T *__restrict__ qd,
-                                  const T *__restrict__ x,
+                                  const typename AR::In *__restrict__ gB,
+                                  const typename AR::Qd *__restrict__ qd,
+                                  const typename AR::In *__restrict__ x,
                                   const int *__restrict__ gmap,
                                   const unsigned char *__restrict__ mask,
-                                  T *__restrict__ y, int accumulate,
+                                  typename AR::In *__restrict__ y, int accumulate,
                                   const int *__restrict__ skip)
 {
+   using V = typename AR::V;
    if (skip && *skip) { return; }
-   constexpr int DM = TD ? TD : GBPA_MAX_1D;
-   constexpr int QM = TQ ? TQ : GBPA_MAX_1D;
+   constexpr int DM = TD ? TD : MAXD;
+   constexpr int QM = TQ ? TQ : MAXQ;
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
    const int D3 = D * D * D, Q3 = Q * Q * Q;
@@ -301,89 +392,91 @@ __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
    const bool active = e < ne;
 
    extern __shared__ __align__(16) unsigned char smem_raw[];
-   T *sB = reinterpret_cast<T *>(smem_raw);
+   V *sB = reinterpret_cast<V *>(smem_raw);
    const int per = mass_smem_per_elem(D, Q);
-   T *bufA = sB + Q * D + tz * per;
-   T *bufB = bufA + (per - D * D * Q);
+   V *bufA = sB + Q * D + tz * per;
+   V *bufB = bufA + (per - D * D * Q);
 
    const int tid = tx + Q * (ty + Q * tz);
    const int nthr = Q * Q * blockDim.z;
-   for (int i = tid; i < Q * D; i += nthr) { sB[(i % Q) * D + i / Q] = gB[i]; }
+   for (int i = tid; i < Q * D; i += nthr) { sB[(i % Q) * D + i / Q] = AR::in(gB[i]); }
    if (active)
    {
       const long long base = (long long)e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
       {
-         bufA[i] = GATHER ? gather_value(x, gmap, mask, base + i) : x[base + i];
+         bufA[i] = GATHER ? gather_value<AR>(x, gmap, mask, base + i) : AR::in(x[base + i]);
       }
    }
    __syncthreads();
-   T rBx[DM];
+   V rBx[DM];
 #pragma unroll
    for (int d = 0; d < DM; ++d) { if (d < D) { rBx[d] = sB[tx * D + d]; } }
-   T *BX = bufB;
+   V *BX = bufB;
    for (int dy = ty; dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T u = 0;
-         const T *xr = bufA + D * (dy + D * dz);
+         V u = AR::zero();
+         const V *xr = bufA + D * (dy + D * dz);
 #pragma unroll
-         for (int dx = 0; dx < DM; ++dx) { if (dx >= D) { break; } u += xr[dx] * rBx[dx]; }
-         BX[(dz * D + dy) * Q + tx] = u;
+         for (int dx = 0; dx < DM; ++dx) { if (dx >= D) { break; } AR::mac(u, xr[dx], rBx[dx]); }
+         BX[(dz * D + dy) * Q + tx] = AR::fin(u);
       }
    }
    __syncthreads();
-   T r[DM];
+   V r[DM];
 #pragma unroll
    for (int dz = 0; dz < DM; ++dz)
    {
       if (dz >= D) { break; }
-      T a = 0;
+      V a = AR::zero();
 #pragma unroll
       for (int dy = 0; dy < DM; ++dy)
       {
          if (dy >= D) { break; }
-         a += BX[(dz * D + dy) * Q + tx] * sB[ty * D + dy];
+         AR::mac(a, BX[(dz * D + dy) * Q + tx], sB[ty * D + dy]);
       }
-      r[dz] = a;
+      r[dz] = AR::fin(a);
    }
-   T o[DM];
+   V o[DM];
 #pragma unroll
-   for (int dz = 0; dz < DM; ++dz) { o[dz] = 0; }
-   const T *qe = qd + (long long)e * Q3 + tx + Q * ty;
+   for (int dz = 0; dz < DM; ++dz) { o[dz] = AR::zero(); }
+   const typename AR::Qd *qe = qd + (long long)e * Q3 + tx + Q * ty;
 #pragma unroll
    for (int qz = 0; qz < QM; ++qz)
    {
       if (qz >= Q) { break; }
-      T v = 0;
+      V v = AR::zero();
 #pragma unroll
-      for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } v += sB[qz * D + dz] * r[dz]; }
-      v = active ? v * __ldg(qe + Q * Q * qz) : T(0);
+      for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } AR::mac(v, sB[qz * D + dz], r[dz]); }
+      V w = AR::zero();
+      if (active) { AR::mac(w, AR::fin(v), AR::ldq(qe + Q * Q * qz)); }
+      w = AR::fin(w);
 #pragma unroll
-      for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } o[dz] += sB[qz * D + dz] * v; }
+      for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } AR::mac(o[dz], sB[qz * D + dz], w); }
    }
-   T *T0 = bufA;
+   V *T0 = bufA;
 #pragma unroll
-   for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } T0[(dz * Q + ty) * Q + tx] = o[dz]; }
+   for (int dz = 0; dz < DM; ++dz) { if (dz >= D) { break; } T0[(dz * Q + ty) * Q + tx] = AR::fin(o[dz]); }
    __syncthreads();
-   T *U = bufB;
+   V *U = bufB;
    for (int dy = ty; dy < D; dy += Q)
    {
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
          if (dz >= D) { break; }
-         T a = 0;
+         V a = AR::zero();
 #pragma unroll
          for (int qy = 0; qy < QM; ++qy)
          {
             if (qy >= Q) { break; }
-            a += T0[(dz * Q + qy) * Q + tx] * sB[qy * D + dy];
+            AR::mac(a, T0[(dz * Q + qy) * Q + tx], sB[qy * D + dy]);
          }
-         U[(dz * D + dy) * Q + tx] = a;
+         U[(dz * D + dy) * Q + tx] = AR::fin(a);
       }
    }
    __syncthreads();
@@ -397,15 +490,16 @@ __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
             for (int dz = 0; dz < DM; ++dz)
             {
                if (dz >= D) { break; }
-               T v = 0;
+               V v = AR::zero();
 #pragma unroll
                for (int qx = 0; qx < QM; ++qx)
                {
                   if (qx >= Q) { break; }
-                  v += sB[qx * D + dx] * U[(dz * D + dy) * Q + qx];
+                  AR::mac(v, sB[qx * D + dx], U[(dz * D + dy) * Q + qx]);
                }
                const long long k = base + dx + D * (dy + D * dz);
-               y[k] = accumulate ? y[k] + v : v;
+               const typename AR::In rr = AR::out(AR::fin(v));
+               y[k] = accumulate ? y[k] + rr : rr;
             }
          }
    }

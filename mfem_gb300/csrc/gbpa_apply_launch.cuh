@@ -1,0 +1,81 @@
+// Launchers for the apply kernels, templated on the arithmetic. Each
+// gbpa_apply_<arith>_<kind>.cu instantiates them for one arithmetic so the
+// translation units compile in parallel.
+//   GEN    largest D1D/Q1D of the generic (runtime-size) kernel
+//   PLAIN  also instantiate the E-vector-input kernels (no gather); the
+//          double-float arithmetic is only used by the fused L-vector
+//          operator, which always gathers
+#pragma once
+#include "gbpa_apply_kernels.cuh"
+#include "gbpa_dispatch.cuh"
+
+namespace gbpa
+{
+
+template <typename AR, bool GATHER, int GEN>
+static const void *diffusion_kernel_for(int D, int Q)
+{
+#define GBPA_CASE(d, q) \
+   if (D == d && Q == q) { return (const void *)diffusion_apply_kernel<AR, d, q, GATHER>; }
+   GBPA_DQ_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return (const void *)diffusion_apply_kernel<AR, 0, 0, GATHER, GEN, GEN>;
+}
+
+template <typename AR, bool GATHER, int GEN>
+static const void *mass_kernel_for(int D, int Q)
+{
+#define GBPA_CASE(d, q) \
+   if (D == d && Q == q) { return (const void *)mass_apply_kernel<AR, d, q, GATHER>; }
+   GBPA_DQ_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return (const void *)mass_apply_kernel<AR, 0, 0, GATHER, GEN, GEN>;
+}
+
+template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
+int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
+                        const typename AR::In *B, const typename AR::In *G,
+                        const typename AR::Qd *qd, const typename AR::In *x,
+                        const int *gather_map, const unsigned char *ess_mask,
+                        typename AR::In *y, bool accumulate, const int *skip)
+{
+   if (ne == 0) { return GBPA_SUCCESS; }
+   if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
+   const void *k = nullptr;
+   if (gather_map) { k = diffusion_kernel_for<AR, true, GEN>(D, Q); }
+   else if constexpr (PLAIN) { k = diffusion_kernel_for<AR, false, GEN>(D, Q); }
+   else { return GBPA_ERR_UNSUPPORTED; }
+   const int nbz = elements_per_block(GBPA_DIFFUSION, prec, D, Q);
+   const size_t smem = sizeof(typename AR::V) *
+                       (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+   int acc = accumulate ? 1 : 0;
+   void *args[] = {&ne, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd,
+                   (void *)&x, (void *)&gather_map, (void *)&ess_mask, &y, &acc,
+                   (void *)&skip};
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
+                         args, smem, "diffusion_apply");
+}
+
+template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
+int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
+                   const typename AR::In *B, const typename AR::Qd *qd,
+                   const typename AR::In *x, const int *gather_map,
+                   const unsigned char *ess_mask, typename AR::In *y,
+                   bool accumulate, const int *skip)
+{
+   if (ne == 0) { return GBPA_SUCCESS; }
+   if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
+   const void *k = nullptr;
+   if (gather_map) { k = mass_kernel_for<AR, true, GEN>(D, Q); }
+   else if constexpr (PLAIN) { k = mass_kernel_for<AR, false, GEN>(D, Q); }
+   else { return GBPA_ERR_UNSUPPORTED; }
+   const int nbz = elements_per_block(GBPA_MASS, prec, D, Q);
+   const size_t smem = sizeof(typename AR::V) * (Q * D + (size_t)nbz * mass_smem_per_elem(D, Q));
+   int acc = accumulate ? 1 : 0;
+   void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&qd, (void *)&x,
+                   (void *)&gather_map, (void *)&ess_mask, &y, &acc, (void *)&skip};
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
+                         args, smem, "mass_apply");
+}
+
+} // namespace gbpa

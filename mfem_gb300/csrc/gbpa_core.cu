@@ -75,7 +75,7 @@ static std::mutex g_nbz_mu;
 static std::unordered_map<int, int> g_nbz;
 static int nbz_key(int kind, int prec, int D, int Q)
 {
-   return ((kind * 2 + prec) * 32 + D) * 32 + Q;
+   return ((kind * 4 + prec) * 32 + D) * 32 + Q;
 }
 
 int elements_per_block(int kind, int prec, int D, int Q)
@@ -90,7 +90,7 @@ int elements_per_block(int kind, int prec, int D, int Q)
    const int q2 = Q * Q;
    int nbz = 256 / q2;
    if (nbz < 1) { nbz = 1; }
-   const size_t w = prec == GBPA_F64 ? 8 : 4;
+   const size_t w = prec == GBPA_F32 ? 4 : 8;
    const int per = kind == GBPA_DIFFUSION ? 0 : 1;
    (void)per;
    while (nbz > 1)
@@ -363,6 +363,7 @@ extern "C" int gbpa_destroy(gbpa_ctx_t ctx)
    if (ctx->d_counter) { cudaFree(ctx->d_counter); }
    if (ctx->d_partials) { cudaFree(ctx->d_partials); }
    if (ctx->own_stream) { cudaStreamDestroy(ctx->own_stream); }
+   if (ctx->capture_stream) { cudaStreamDestroy(ctx->capture_stream); }
    delete ctx;
    return GBPA_SUCCESS;
 }
@@ -661,7 +662,7 @@ extern "C" int gbpa_jacobi_setup(gbpa_ctx_t ctx, int64_t n, const double *diag, 
 
 extern "C" int gbpa_set_elements_per_block(int kind, int precision, int d1d, int q1d, int nbz)
 {
-   if (kind < 0 || kind > 1 || precision < 0 || precision > 1 || d1d < 1 || q1d < 1 ||
+   if (kind < 0 || kind > 1 || precision < 0 || precision > 2 || d1d < 1 || q1d < 1 ||
        d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || nbz < 0 || nbz * q1d * q1d > 1024)
    {
       return GBPA_ERR_INVALID_ARGUMENT;
@@ -674,6 +675,6 @@ extern "C" int gbpa_set_elements_per_block(int kind, int precision, int d1d, int
 
 extern "C" int gbpa_get_elements_per_block(int kind, int precision, int d1d, int q1d)
 {
-   if (kind < 0 || kind > 1 || precision < 0 || precision > 1) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (kind < 0 || kind > 1 || precision < 0 || precision > 2) { return GBPA_ERR_INVALID_ARGUMENT; }
    return elements_per_block(kind, precision, d1d, q1d);
 }

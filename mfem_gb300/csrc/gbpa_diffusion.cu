@@ -1,51 +1,10 @@
 // Diffusion PA kernels: apply (E->E and gather-fused), diagonal, and their
 // C-ABI entry points. Reference: fem/integ/bilininteg_diffusion_pa.cpp,
 // fem/integ/bilininteg_diffusion_kernels.hpp.
-#include "gbpa_apply_kernels.cuh"
 #include "gbpa_dispatch.cuh"
 
 namespace gbpa
 {
-
-template <typename T, bool GATHER>
-static const void *diffusion_kernel(int D, int Q)
-{
-#define GBPA_CASE(d, q) \
-   if (D == d && Q == q) { return (const void *)diffusion_apply_kernel<T, d, q, GATHER>; }
-   GBPA_DQ_LIST(GBPA_CASE)
-#undef GBPA_CASE
-   return (const void *)diffusion_apply_kernel<T, 0, 0, GATHER>;
-}
-
-template <typename T>
-int launch_diffusion_apply(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
-                           const T *B, const T *G, const T *qd, const T *x,
-                           const int *gather_map, const unsigned char *ess_mask,
-                           T *y, bool accumulate, const int *skip)
-{
-   if (ne == 0) { return GBPA_SUCCESS; }
-   const int prec = sizeof(T) == 8 ? GBPA_F64 : GBPA_F32;
-   const int nbz = elements_per_block(GBPA_DIFFUSION, prec, D, Q);
-   const void *k = gather_map ? diffusion_kernel<T, true>(D, Q)
-                              : diffusion_kernel<T, false>(D, Q);
-   const size_t smem = sizeof(T) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
-   int acc = accumulate ? 1 : 0;
-   void *args[] = {&ne, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd,
-                   (void *)&x, (void *)&gather_map, (void *)&ess_mask, &y, &acc,
-                   (void *)&skip};
-   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
-                         args, smem, "diffusion_apply");
-}
-template int launch_diffusion_apply<double>(gbpa_ctx *, int, int, int, int,
-                                            const double *, const double *,
-                                            const double *, const double *,
-                                            const int *, const unsigned char *,
-                                            double *, bool, const int *);
-template int launch_diffusion_apply<float>(gbpa_ctx *, int, int, int, int,
-                                           const float *, const float *,
-                                           const float *, const float *,
-                                           const int *, const unsigned char *,
-                                           float *, bool, const int *);
 
 // Diagonal (2D slab). For pair (i, j) of gradient directions the element
 // diagonal gains sum_q L_i O_ij R_j where, per direction t, the 1D factor is

@@ -14,6 +14,8 @@ struct gbpa_ctx
    int num_sms = 0;
    cudaStream_t own_stream = nullptr;
    cudaStream_t stream = nullptr;
+   cudaStream_t capture_stream = nullptr; // private stream for CUDA-graph capture
+                                          // (the legacy default stream cannot be captured)
    int *d_flags = nullptr;           // sticky device error flags
    double *h_pinned = nullptr;       // small pinned host staging area (64 doubles)
    double *d_scalars = nullptr;      // small device scalar area (64 doubles)
@@ -63,6 +65,32 @@ int launch_mass_apply(gbpa_ctx *ctx, int ne, int D, int Q, const T *B,
                       const T *qd, const T *x, const int *gather_map,
                       const unsigned char *ess_mask, T *y, bool accumulate,
                       const int *skip = nullptr);
+template <>
+int launch_diffusion_apply<double>(gbpa_ctx *, int, int, int, int, const double *, const double *,
+                                   const double *, const double *, const int *,
+                                   const unsigned char *, double *, bool, const int *);
+template <>
+int launch_diffusion_apply<float>(gbpa_ctx *, int, int, int, int, const float *, const float *,
+                                  const float *, const float *, const int *,
+                                  const unsigned char *, float *, bool, const int *);
+template <>
+int launch_mass_apply<double>(gbpa_ctx *, int, int, int, const double *, const double *,
+                              const double *, const int *, const unsigned char *, double *, bool,
+                              const int *);
+template <>
+int launch_mass_apply<float>(gbpa_ctx *, int, int, int, const float *, const float *,
+                             const float *, const int *, const unsigned char *, float *, bool,
+                             const int *);
+// FP64-accurate double-float arithmetic on the FP32 pipes (qdata split into
+// float2 (hi, lo) by launch_split_x2).
+int launch_diffusion_apply_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
+                              const double *G, const float2 *qd, const double *x,
+                              const int *gather_map, const unsigned char *ess_mask, double *y,
+                              bool accumulate, const int *skip = nullptr);
+int launch_mass_apply_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const float2 *qd,
+                         const double *x, const int *gather_map, const unsigned char *ess_mask,
+                         double *y, bool accumulate, const int *skip = nullptr);
+int launch_split_x2(gbpa_ctx *ctx, int64_t n, const double *a, float2 *b);
 int launch_diffusion_diagonal(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
                               const double *B, const double *G,
                               const double *qd, double *y);

@@ -1,45 +1,10 @@
 // Mass PA kernels: apply (E->E and gather-fused), diagonal, setup entry
 // points. Reference: fem/integ/bilininteg_mass_pa.cpp,
 // fem/integ/bilininteg_mass_kernels.hpp.
-#include "gbpa_apply_kernels.cuh"
 #include "gbpa_dispatch.cuh"
 
 namespace gbpa
 {
-
-template <typename T, bool GATHER>
-static const void *mass_kernel(int D, int Q)
-{
-#define GBPA_CASE(d, q) \
-   if (D == d && Q == q) { return (const void *)mass_apply_kernel<T, d, q, GATHER>; }
-   GBPA_DQ_LIST(GBPA_CASE)
-#undef GBPA_CASE
-   return (const void *)mass_apply_kernel<T, 0, 0, GATHER>;
-}
-
-template <typename T>
-int launch_mass_apply(gbpa_ctx *ctx, int ne, int D, int Q, const T *B,
-                      const T *qd, const T *x, const int *gather_map,
-                      const unsigned char *ess_mask, T *y, bool accumulate, const int *skip)
-{
-   if (ne == 0) { return GBPA_SUCCESS; }
-   const int prec = sizeof(T) == 8 ? GBPA_F64 : GBPA_F32;
-   const int nbz = elements_per_block(GBPA_MASS, prec, D, Q);
-   const void *k = gather_map ? mass_kernel<T, true>(D, Q) : mass_kernel<T, false>(D, Q);
-   const size_t smem = sizeof(T) * (Q * D + (size_t)nbz * mass_smem_per_elem(D, Q));
-   int acc = accumulate ? 1 : 0;
-   void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&qd, (void *)&x,
-                   (void *)&gather_map, (void *)&ess_mask, &y, &acc,
-                   (void *)&skip};
-   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
-                         args, smem, "mass_apply");
-}
-template int launch_mass_apply<double>(gbpa_ctx *, int, int, int, const double *,
-                                       const double *, const double *, const int *,
-                                       const unsigned char *, double *, bool, const int *);
-template int launch_mass_apply<float>(gbpa_ctx *, int, int, int, const float *,
-                                      const float *, const float *, const int *,
-                                      const unsigned char *, float *, bool, const int *);
 
 // Diagonal: sum_q B^2 (x) B^2 (x) B^2 . D, contracted z, y, x
 // (fem/integ/bilininteg_mass_kernels.hpp:262-416).

@@ -26,6 +26,7 @@ struct gbpa_operator
    gbpa_operator_desc d{};
    unsigned char *mask = nullptr;   // ess mask (ndofs) or null
    void *yE = nullptr;              // E-vector scratch in the operator's precision
+   float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
    // PCG workspace (vectors in the operator's precision)
    void *r = nullptr, *dv = nullptr, *z = nullptr;
    double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)
@@ -278,7 +279,12 @@ static int64_t evec_size(const gbpa_operator_desc &d)
 {
    return (int64_t)d.ne * d.d1d * d.d1d * d.d1d;
 }
-static size_t elem_bytes(const gbpa_operator_desc &d) { return d.precision == GBPA_F64 ? 8 : 4; }
+static size_t elem_bytes(const gbpa_operator_desc &d) { return d.precision == GBPA_F32 ? 4 : 8; }
+static int64_t qdata_size(const gbpa_operator_desc &d)
+{
+   const int64_t q3 = (int64_t)d.q1d * d.q1d * d.q1d;
+   return (int64_t)d.ne * q3 * (d.kind == GBPA_DIFFUSION ? (d.symm ? 6 : 9) : 1);
+}
 
 extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
                                     gbpa_operator_t *out)
@@ -287,8 +293,13 @@ extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *de
    *out = nullptr;
    const gbpa_operator_desc &d = *desc;
    if (d.kind != GBPA_DIFFUSION && d.kind != GBPA_MASS) { return GBPA_ERR_INVALID_ARGUMENT; }
-   if (d.precision != GBPA_F64 && d.precision != GBPA_F32) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (d.precision != GBPA_F64 && d.precision != GBPA_F32 && d.precision != GBPA_F64X2)
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
    if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0) { return GBPA_ERR_INVALID_ARGUMENT; }
+   // the double-float kernels are built for D1D, Q1D <= 10 (p <= 9)
+   if (d.precision == GBPA_F64X2 && (d.d1d > 10 || d.q1d > 10)) { return GBPA_ERR_UNSUPPORTED; }
    if (d.d1d < 1 || d.q1d < 1 || d.d1d > GBPA_MAX_1D || d.q1d > GBPA_MAX_1D) { return GBPA_ERR_UNSUPPORTED; }
    if (d.ne > 0 && (!d.B || !d.qdata || !d.gather_map || !d.offsets || !d.indices)) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (d.kind == GBPA_DIFFUSION && d.ne > 0 && !d.G) { return GBPA_ERR_INVALID_ARGUMENT; }
@@ -301,6 +312,12 @@ extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *de
    int rc = GBPA_SUCCESS;
    const int64_t nE = evec_size(d);
    if (nE > 0) { rc = check_cuda(cudaMalloc(&op->yE, elem_bytes(d) * nE), "cudaMalloc(yE)"); }
+   if (!rc && d.precision == GBPA_F64X2 && d.ne > 0)
+   {
+      const int64_t nq = qdata_size(d);
+      rc = check_cuda(cudaMalloc(&op->qd2, sizeof(float2) * nq), "cudaMalloc(qdata x2)");
+      if (!rc) { rc = launch_split_x2(ctx, nq, (const double *)d.qdata, op->qd2); }
+   }
    if (!rc && d.n_ess > 0)
    {
       rc = check_cuda(cudaMalloc(&op->mask, d.ndofs), "cudaMalloc(mask)");
@@ -325,7 +342,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    if (!op) { return GBPA_SUCCESS; }
    cudaStreamSynchronize(op->ctx->stream);
    if (op->graph) { cudaGraphExecDestroy(op->graph); }
-   cudaFree(op->yE); cudaFree(op->mask);
+   cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->qd2);
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
    cudaFree(op->r64); cudaFree(op->t64);
@@ -338,6 +355,18 @@ template <typename T>
 static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
 {
    const gbpa_operator_desc &d = op->d;
+   if (d.precision == GBPA_F64X2)
+   {
+      const double *xd = (const double *)x;
+      if (d.kind == GBPA_DIFFUSION)
+      {
+         return launch_diffusion_apply_x2(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
+                                          (const double *)d.B, (const double *)d.G, op->qd2, xd,
+                                          d.gather_map, op->mask, (double *)op->yE, false, skip);
+      }
+      return launch_mass_apply_x2(op->ctx, d.ne, d.d1d, d.q1d, (const double *)d.B, op->qd2, xd,
+                                  d.gather_map, op->mask, (double *)op->yE, false, skip);
+   }
    if (d.kind == GBPA_DIFFUSION)
    {
       return launch_diffusion_apply<T>(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
@@ -362,7 +391,7 @@ extern "C" int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y)
 {
    if (!op || (op->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (op->d.ndofs == 0) { return GBPA_SUCCESS; }
-   if (op->d.precision == GBPA_F64) { return op_mult<double>(op, (const double *)x, (double *)y); }
+   if (op->d.precision != GBPA_F32) { return op_mult<double>(op, (const double *)x, (double *)y); }
    return op_mult<float>(op, (const float *)x, (float *)y);
 }
 
@@ -372,7 +401,7 @@ extern "C" int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, vo
    if (op->d.ne == 0) { return GBPA_SUCCESS; }
    void *saved = op->yE;
    op->yE = yE;
-   const int rc = op->d.precision == GBPA_F64 ? apply_evec<double>(op, (const double *)x, nullptr)
+   const int rc = op->d.precision != GBPA_F32 ? apply_evec<double>(op, (const double *)x, nullptr)
                                               : apply_evec<float>(op, (const float *)x, nullptr);
    op->yE = saved;
    return rc;
@@ -383,7 +412,7 @@ extern "C" int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag)
    if (!op || (op->d.ndofs > 0 && !diag)) { return GBPA_ERR_INVALID_ARGUMENT; }
    const gbpa_operator_desc &d = op->d;
    if (d.ndofs == 0) { return GBPA_SUCCESS; }
-   if (d.precision != GBPA_F64) { return GBPA_ERR_UNSUPPORTED; }
+   if (d.precision == GBPA_F32) { return GBPA_ERR_UNSUPPORTED; }
    gbpa_ctx *ctx = op->ctx;
    const int64_t nE = evec_size(d);
    int rc = check_cuda(cudaMemsetAsync(op->yE, 0, sizeof(double) * nE, ctx->stream), "memset");
@@ -497,13 +526,29 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
    if (!op->graph || op->graph_x != (const void *)x || op->graph_dinv != (const void *)dinv)
    {
       if (op->graph) { cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
-      cudaGraph_t g;
-      rc = check_cuda(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
+      // Capture on a private non-blocking stream (the context's stream may be
+      // the legacy default stream, which cannot be captured); the graph is
+      // then launched on the context's stream.
+      if (!ctx->capture_stream)
+      {
+         rc = check_cuda(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking),
+                         "cudaStreamCreate(capture)");
+         if (rc) { return rc; }
+      }
+      cudaGraph_t g = nullptr;
+      cudaStream_t saved = ctx->stream;
+      rc = check_cuda(cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal),
                       "cudaStreamBeginCapture");
       if (rc) { return rc; }
+      ctx->stream = ctx->capture_stream;
       for (int k = 0; k < K && !rc; ++k) { rc = pcg_iteration<T>(op, x, dinv, grid); }
-      const int rc2 = check_cuda(cudaStreamEndCapture(ctx->stream, &g), "cudaStreamEndCapture");
-      if (rc || rc2) { return rc ? rc : rc2; }
+      ctx->stream = saved;
+      const int rc2 = check_cuda(cudaStreamEndCapture(ctx->capture_stream, &g), "cudaStreamEndCapture");
+      if (rc || rc2)
+      {
+         if (g) { cudaGraphDestroy(g); }
+         return rc ? rc : rc2;
+      }
       rc = check_cuda(cudaGraphInstantiate(&op->graph, g, 0), "cudaGraphInstantiate");
       cudaGraphDestroy(g);
       if (rc) { return rc; }
@@ -580,7 +625,7 @@ extern "C" int gbpa_pcg_solve(gbpa_operator_t A, const double *dinv, const doubl
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
-   if (A->d.precision != GBPA_F64) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (A->d.precision == GBPA_F32) { return GBPA_ERR_INVALID_ARGUMENT; }
    gbpa_solve_info tmp{};
    gbpa_solve_info *inf = info ? info : &tmp;
    memset(inf, 0, sizeof(*inf));
@@ -599,7 +644,7 @@ extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, co
                                     double inner_rel_tol, int max_outer, int max_inner,
                                     gbpa_solve_info *info)
 {
-   if (!A64 || !A32 || A64->d.precision != GBPA_F64 || A32->d.precision != GBPA_F32 ||
+   if (!A64 || !A32 || A64->d.precision == GBPA_F32 || A32->d.precision != GBPA_F32 ||
        A64->d.ndofs != A32->d.ndofs || A64->ctx != A32->ctx || max_outer < 1 || max_inner < 1)
    {
       return GBPA_ERR_INVALID_ARGUMENT;

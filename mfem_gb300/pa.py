@@ -290,7 +290,8 @@ class PAOperator:
         dev = _dev()
         R = fes_or_maps.GetElementRestriction() if hasattr(fes_or_maps, "GetElementRestriction") else fes_or_maps
         self.R = R
-        dt = torch.float64 if precision == _lib.GBPA_F64 else torch.float32
+        # GBPA_F64X2 keeps FP64 data (the library splits qdata internally)
+        dt = torch.float32 if precision == _lib.GBPA_F32 else torch.float64
         self.dtype = dt
         self.B, self.G, self.qdata = B.to(dt).contiguous(), G.to(dt).contiguous(), qdata.to(dt).contiguous()
         self.ess = to_dev(np.asarray(ess, np.int32)) if ess is not None and len(ess) else None

@@ -29,13 +29,23 @@ def H(t):
     return t.detach().cpu().numpy()
 
 
+_keep = []
+
+
 def p(t):
-    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+    """Device pointer of t; t is kept alive until the next call() returns, so
+    a temporary's memory cannot be handed to another argument of the same
+    call by the caching allocator."""
+    if t is None:
+        return None
+    _keep.append(t)
+    return ctypes.c_void_p(t.data_ptr())
 
 
 def call(name, *args):
     d = dev()
     st = getattr(d.lib, name)(d.ctx, *args)
+    _keep.clear()
     _lib.check(st, name)
     return st
 

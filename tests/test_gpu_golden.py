@@ -148,3 +148,28 @@ def test_mass_setup_apply_diagonal(case):
     y32 = zeros(ne * D ** 3, torch.float32)
     call("gbpa_mass_apply3d_f32", ne, D, Q, p(B.float()), p(qm.float()), p(T(g["xE"]).float()), p(y32))
     assert relerr(H(y32), g["yE_mass"]) < 1e-5
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("kind", ["diffusion", "mass"])
+def test_double_float_operator(case, kind):
+    """GBPA_F64X2: FP64 data applied with double-float arithmetic on the FP32
+    pipes must meet the FP64 parity bar (1e-12 relative L2) against the
+    reference's BilinearForm::Mult."""
+    from mfem_gb300.pa import ElementRestriction, PAOperator
+    from tests.gpu_util import T, H, zeros, relerr, dev
+    dev()
+    g = load_golden(case)
+    ne, ndofs, D, Q, cdim = meta(g)
+    if D > 10 or Q > 10:
+        pytest.skip("double-float kernels cover D1D, Q1D <= 10")
+    R = ElementRestriction.from_maps(ne, D ** 3, ndofs, g["gather_map"], g["offsets"], g["indices"])
+    if kind == "diffusion":
+        op = PAOperator(0, R, D, Q, T(g["B"]), T(g["G"]), T(g["qdata_diff"]), symm=(cdim != 9), precision=2)
+        ref = g["y_diff"]
+    else:
+        op = PAOperator(1, R, D, Q, T(g["B"]), T(g["G"]), T(g["qdata_mass"]), precision=2)
+        ref = g["y_mass"]
+    y = zeros(ndofs)
+    op.Mult(T(g["x"]), y)
+    assert relerr(H(y), ref) < 1e-12

@@ -97,3 +97,22 @@ def test_max_iterations_not_converged():
     st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 5, 0,
                                   ctypes.byref(info))
     assert st == 0 and info.converged == 0 and info.iterations == 5
+
+
+def test_double_float_pcg_matches_reference_solve():
+    import ctypes
+    from mfem_gb300 import _lib
+    from mfem_gb300.pa import ElementRestriction, PAOperator
+    from tests.gpu_util import T, H, p, zeros, relerr, dev
+    g, ndofs, A, _ = cfg1_operator()
+    ne, _, D, Q = (int(v) for v in g["meta"][:4])
+    R = ElementRestriction.from_maps(ne, D ** 3, ndofs, g["gather_map"], g["offsets"], g["indices"])
+    A2 = PAOperator(0, R, D, Q, A.B, A.G, A.qdata, ess=g["ess_tdofs"], precision=2)
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    st = dev().lib.gbpa_pcg_solve(A2.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 500, 0,
+                                  ctypes.byref(info))
+    assert st == 0 and info.converged == 1
+    assert abs(info.iterations - int(g["cg_info"][0])) <= 1
+    assert relerr(H(X), g["X"]) < 1e-10
