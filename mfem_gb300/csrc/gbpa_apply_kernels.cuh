@@ -97,7 +97,10 @@ struct ArX2
    }
 };
 
-template <typename AR>
+// COH: x was written earlier in the same launch by other blocks (persistent
+// solvers), so it is read through L2 (__ldcg) instead of the non-coherent
+// read-only path.
+template <typename AR, bool COH = false>
 __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__restrict__ x,
                                                        const int *__restrict__ gmap,
                                                        const unsigned char *__restrict__ mask,
@@ -106,7 +109,7 @@ __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__
    const int g = __ldg(gmap + slot);
    const int j = g >= 0 ? g : -1 - g;
    if (mask && __ldg(mask + j)) { return AR::zero(); }
-   const typename AR::V v = AR::in(__ldg(x + j));
+   const typename AR::V v = AR::in(COH ? __ldcg(x + j) : __ldg(x + j));
    return g >= 0 ? v : AR::neg(v);
 }
 
@@ -128,7 +131,8 @@ __host__ __device__ inline int mass_smem_per_elem(int D, int Q)
 // part == false: the thread has no slot in the layout and only joins the
 // barriers; active == false: the slot's element is past the end (computes
 // on zeros, stores nothing). Every thread of the block must call this.
-template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D,
+          bool COH = false>
 __device__ __forceinline__ void
 diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int ty, int symm,
                   const typename AR::V *__restrict__ sB, const typename AR::V *__restrict__ sG,
@@ -146,7 +150,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
       const long long base = e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
       {
-         bufA[i] = GATHER ? gather_value<AR>(x, gmap, mask, base + i) : AR::in(x[base + i]);
+         bufA[i] = GATHER ? gather_value<AR, COH>(x, gmap, mask, base + i) : AR::in(x[base + i]);
       }
    }
    __syncthreads();

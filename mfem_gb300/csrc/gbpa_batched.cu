@@ -1,11 +1,483 @@
-// Batched PCG over many independent problems (batching form).
-#include "gbpa_internal.cuh"
+// Batched PCG (batching form): many independent Dirichlet Poisson problems of
+// uneven size and order solved together in ONE persistent cooperative launch.
+// Each problem follows CGSolver::Mult with OperatorJacobiSmoother
+// (linalg/solvers.cpp:869-1050, 427-452) on its ConstrainedOperator-wrapped
+// PA diffusion operator (linalg/operator.cpp:601-661,
+// fem/bilinearform_ext.cpp:487-564); a converged problem drops out of the work
+// tables while the others continue.
+//
+// Work decomposition (built on the host once per call):
+//   element batches  (problem, first element, count): one block processes a
+//                    batch with the 2D-slab layout (Q, Q, nbz) of that
+//                    problem's order, nbz chosen per Q (tuning table)
+//   dof chunks       (problem, first dof, last dof): vector phases and the CSR
+//                    scatter; each chunk writes one partial sum
+// Per-problem dots sum their chunks' partials in chunk order, so results do
+// not depend on the grid size or on scheduling.
+//
+// The grid barrier is a generation counter with a bounded spin: a barrier that
+// does not complete within the spin budget raises GBPA_FLAG_TIMEOUT and every
+// block leaves the solve loop, so the kernel always terminates. The launch is
+// cooperative, so all blocks are co-resident and the barrier completes in
+// normal operation.
+#include "gbpa_apply_kernels.cuh"
+#include "gbpa_dispatch.cuh"
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace gbpa
+{
+constexpr int BATCH_THREADS = 256;
+constexpr int BATCH_MAXD = 7;    // p <= 6
+constexpr int BATCH_MAXQ = 8;
+constexpr int CHUNK = 2048;
+constexpr int GBPA_FLAG_TIMEOUT = 16;
+
+struct BProb
+{
+   int ne, ndofs, D, Q, nbz;
+   const double *B, *G, *qd, *dinv, *b;
+   double *x;
+   const int *gmap, *off, *ind;
+   const unsigned char *mask;
+   double *r, *d, *z, *yE;
+   int chunk0, nchunk;
+};
+// Per-problem solver scalars. They are written by one thread and read by all
+// blocks across grid barriers, so every access goes through a volatile
+// pointer (L2, never a stale L1 line).
+struct BScal
+{
+   double nom, nom0, den, betanom, alpha, beta, r0;
+   int iter, done, converged, final_iter;
+};
+struct BBatch { int prob, e0, count; };
+struct BChunk { int prob, i0, i1; };
+
+struct BParams
+{
+   const BProb *probs;
+   BScal *scal;
+   int nprob;
+   const BBatch *batches;
+   int nbatch;
+   const BChunk *chunks;
+   int nchunk;
+   double *partials;
+   double rel2, abs2;
+   int max_it;
+   unsigned int *bar_count;
+   unsigned int *bar_gen;
+   int *flags;
+   int *n_active;
+   int *abort;
+   long long spin_limit;
+};
+
+// Sense-free generation barrier over all blocks, bounded spin.
+__device__ bool grid_barrier(const BParams &P)
+{
+   __syncthreads();
+   __shared__ int ok;
+   if (threadIdx.x == 0)
+   {
+      ok = 1;
+      volatile unsigned int *gen = P.bar_gen;
+      const unsigned int g = *gen;
+      __threadfence();
+      if (atomicAdd(P.bar_count, 1u) == gridDim.x - 1)
+      {
+         *P.bar_count = 0;
+         __threadfence();
+         atomicAdd(P.bar_gen, 1u);
+      }
+      else
+      {
+         long long spins = 0;
+         while (*gen == g)
+         {
+            if (*(volatile int *)P.abort) { ok = 0; break; }
+            if (++spins > P.spin_limit)
+            {
+               atomicOr(P.flags, GBPA_FLAG_TIMEOUT);
+               atomicExch(P.abort, 1);
+               ok = 0;
+               break;
+            }
+            __nanosleep(32);
+         }
+      }
+      __threadfence();
+   }
+   __syncthreads();
+   return ok != 0;
+}
+
+__device__ __forceinline__ double bwarp_sum(double v)
+{
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) { v += __shfl_down_sync(0xffffffffu, v, o); }
+   return v;
+}
+__device__ double bblock_sum(double v)
+{
+   __shared__ double ws[32];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+   v = bwarp_sum(v);
+   if (lane == 0) { ws[wid] = v; }
+   __syncthreads();
+   v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+   if (wid == 0) { v = bwarp_sum(v); }
+   __syncthreads();
+   return v;
+}
+
+// partials were written by other blocks: read through L2
+__device__ double problem_sum(const BParams &P, const BProb &pr)
+{
+   double s = 0.0;
+   for (int c = 0; c < pr.nchunk; ++c) { s += __ldcg(P.partials + pr.chunk0 + c); }
+   return s;
+}
+
+__global__ void __launch_bounds__(BATCH_THREADS)
+batched_pcg_kernel(BParams P)
+{
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   double *sm = reinterpret_cast<double *>(smem_raw);
+   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+   const int gthreads = gridDim.x * blockDim.x;
+   volatile BScal *S = P.scal;
+
+   // ---- init: r = b, x = 0, z = dinv r, d = z, partial (z, r)
+   for (int c = blockIdx.x; c < P.nchunk; c += gridDim.x)
+   {
+      const BChunk ch = P.chunks[c];
+      const BProb &pr = P.probs[ch.prob];
+      double s = 0.0;
+      for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+      {
+         const double ri = pr.b[i];
+         pr.x[i] = 0.0;
+         pr.r[i] = ri;
+         const double zi = pr.dinv[i] * ri;
+         pr.z[i] = zi;
+         pr.d[i] = zi;
+         s += zi * ri;
+      }
+      s = bblock_sum(s);
+      if (threadIdx.x == 0) { P.partials[c] = s; }
+   }
+   if (gtid == 0) { *(volatile int *)P.n_active = 0; }
+   if (!grid_barrier(P)) { return; }
+   for (int k = gtid; k < P.nprob; k += gthreads)
+   {
+      volatile BScal &sc = S[k];
+      const double nom = problem_sum(P, P.probs[k]);
+      sc.nom = nom; sc.nom0 = nom; sc.betanom = nom;
+      sc.iter = 1; sc.converged = 0; sc.final_iter = 0;
+      int done = 0;
+      if (!isfinite(nom)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); done = 1; }
+      else if (nom < 0.0) { done = 1; }
+      else
+      {
+         sc.r0 = fmax(nom * P.rel2, P.abs2);
+         if (nom <= sc.r0) { sc.converged = 1; done = 1; }
+      }
+      sc.done = done;
+      if (!done) { atomicAdd(P.n_active, 1); }
+   }
+   if (!grid_barrier(P)) { return; }
+
+   for (int it = 0; ; ++it)
+   {
+      if (*(volatile int *)P.n_active == 0) { break; }
+      // ---- A: yE = A_e d (gather of d, written by other blocks, via L2)
+      for (int bi = blockIdx.x; bi < P.nbatch; bi += gridDim.x)
+      {
+         const BBatch bt = P.batches[bi];
+         if (S[bt.prob].done) { continue; }      // uniform over the block
+         const BProb &pr = P.probs[bt.prob];
+         const int D = pr.D, Q = pr.Q;
+         __syncthreads();                         // previous batch done with smem
+         double *sB = sm, *sG = sm + Q * D;
+         for (int i = threadIdx.x; i < Q * D; i += blockDim.x)
+         {
+            sB[(i % Q) * D + i / Q] = pr.B[i];
+            sG[(i % Q) * D + i / Q] = pr.G[i];
+         }
+         const int t = threadIdx.x;
+         const int tz = t / (Q * Q), tx = t % Q, ty = (t / Q) % Q;
+         const bool part = tz < pr.nbz;
+         const int per = diff_smem_per_elem(D, Q);
+         double *bufA = sm + 2 * Q * D + (part ? tz : 0) * per;
+         double *bufB = bufA + (per - 2 * D * D * Q);
+         diffusion_element<ArF64, 0, 0, true, BATCH_MAXD, BATCH_MAXQ, true>(
+            (long long)bt.e0 + tz, part && tz < bt.count, part, D, Q, tx, ty, 1, sB, sG, bufA,
+            bufB, pr.qd, pr.d, pr.gmap, pr.mask, pr.yE, 0);
+      }
+      if (!grid_barrier(P)) { return; }
+      // ---- S: z = R^T yE (z[ess] = d[ess]); partial (d, z). yE comes from
+      // other blocks (L2 loads); d and z of a chunk belong to this block.
+      for (int c = blockIdx.x; c < P.nchunk; c += gridDim.x)
+      {
+         const BChunk ch = P.chunks[c];
+         if (S[ch.prob].done) { continue; }
+         const BProb &pr = P.probs[ch.prob];
+         double s = 0.0;
+         for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+         {
+            double v;
+            if (pr.mask && pr.mask[i]) { v = pr.d[i]; }
+            else
+            {
+               v = 0.0;
+               for (int j = pr.off[i]; j < pr.off[i + 1]; ++j)
+               {
+                  const int sj = pr.ind[j];
+                  const double a = __ldcg(pr.yE + (sj >= 0 ? sj : -1 - sj));
+                  v += sj >= 0 ? a : -a;
+               }
+            }
+            pr.z[i] = v;
+            s += pr.d[i] * v;
+         }
+         s = bblock_sum(s);
+         if (threadIdx.x == 0) { P.partials[c] = s; }
+      }
+      if (!grid_barrier(P)) { return; }
+      for (int k = gtid; k < P.nprob; k += gthreads)
+      {
+         volatile BScal &sc = S[k];
+         if (sc.done) { continue; }
+         const double den = problem_sum(P, P.probs[k]);
+         sc.den = den;
+         if (!isfinite(den)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); sc.final_iter = sc.iter; sc.done = 1; }
+         else if (den == 0.0) { sc.final_iter = sc.iter; sc.done = 1; }
+         else
+         {
+            if (it > 0) { sc.nom = sc.betanom; }
+            sc.alpha = sc.nom / den;
+         }
+      }
+      if (gtid == 0) { *(volatile int *)P.n_active = 0; }
+      if (!grid_barrier(P)) { return; }
+      // ---- U: x += alpha d; r -= alpha z; z = dinv r; partial (r, z)
+      for (int c = blockIdx.x; c < P.nchunk; c += gridDim.x)
+      {
+         const BChunk ch = P.chunks[c];
+         if (S[ch.prob].done) { continue; }
+         const BProb &pr = P.probs[ch.prob];
+         const double alpha = S[ch.prob].alpha;
+         double s = 0.0;
+         for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+         {
+            pr.x[i] += alpha * pr.d[i];
+            const double ri = pr.r[i] - alpha * pr.z[i];
+            pr.r[i] = ri;
+            const double zi = pr.dinv[i] * ri;
+            pr.z[i] = zi;
+            s += ri * zi;
+         }
+         s = bblock_sum(s);
+         if (threadIdx.x == 0) { P.partials[c] = s; }
+      }
+      if (!grid_barrier(P)) { return; }
+      for (int k = gtid; k < P.nprob; k += gthreads)
+      {
+         volatile BScal &sc = S[k];
+         if (sc.done) { continue; }
+         const double bn = problem_sum(P, P.probs[k]);
+         sc.betanom = bn;
+         int done = 0;
+         if (!isfinite(bn)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); sc.final_iter = sc.iter; done = 1; }
+         else if (bn < 0.0) { sc.final_iter = sc.iter; done = 1; }
+         else if (bn <= sc.r0) { sc.converged = 1; sc.final_iter = sc.iter; done = 1; }
+         else
+         {
+            const int iter = sc.iter + 1;
+            sc.iter = iter;
+            if (iter > P.max_it) { sc.final_iter = P.max_it; done = 1; }
+            else { sc.beta = bn / sc.nom; }
+         }
+         sc.done = done;
+         if (!done) { atomicAdd(P.n_active, 1); }
+      }
+      if (!grid_barrier(P)) { return; }
+      // ---- direction: d = z + beta d (chunk-owned vectors)
+      for (int c = blockIdx.x; c < P.nchunk; c += gridDim.x)
+      {
+         const BChunk ch = P.chunks[c];
+         if (S[ch.prob].done) { continue; }
+         const BProb &pr = P.probs[ch.prob];
+         const double beta = S[ch.prob].beta;
+         for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+         {
+            pr.d[i] = pr.z[i] + beta * pr.d[i];
+         }
+      }
+      if (!grid_barrier(P)) { return; }
+   }
+}
+
+__global__ void batched_mask_kernel(int n, const int *ess, unsigned char *mask, int ndofs, int *flags)
+{
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+   {
+      const int k = ess[i];
+      if (k < 0 || k >= ndofs) { atomicOr(flags, GBPA_FLAG_INDEX); continue; }
+      mask[k] = 1;
+   }
+}
+
+} // namespace gbpa
+
+using namespace gbpa;
 
 extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
                                       double rel_tol, double abs_tol, int max_it, int *iterations,
                                       int *converged, double *final_norms, double *seconds)
 {
-   (void)ctx; (void)nprob; (void)probs; (void)rel_tol; (void)abs_tol; (void)max_it;
-   (void)iterations; (void)converged; (void)final_norms; (void)seconds;
-   return GBPA_ERR_UNSUPPORTED;
+   if (!ctx || nprob < 0 || (nprob > 0 && !probs) || max_it < 0 || rel_tol < 0 || abs_tol < 0)
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   if (nprob == 0) { return GBPA_SUCCESS; }
+   // ---- host tables
+   std::vector<BProb> hp(nprob);
+   std::vector<BBatch> batches;
+   std::vector<BChunk> chunks;
+   size_t ws_doubles = 0, mask_bytes = 0;
+   size_t smem_max = 0;
+   for (int k = 0; k < nprob; ++k)
+   {
+      const gbpa_problem_desc &d = probs[k];
+      if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0) { return GBPA_ERR_INVALID_ARGUMENT; }
+      if (d.d1d < 1 || d.q1d < 1 || d.d1d > BATCH_MAXD || d.q1d > BATCH_MAXQ) { return GBPA_ERR_UNSUPPORTED; }
+      if (d.ne > 0 && (!d.B || !d.G || !d.qdata || !d.gather_map || !d.offsets || !d.indices)) { return GBPA_ERR_INVALID_ARGUMENT; }
+      if (d.ndofs > 0 && (!d.dinv || !d.b || !d.x)) { return GBPA_ERR_INVALID_ARGUMENT; }
+      if (d.n_ess > 0 && !d.ess) { return GBPA_ERR_INVALID_ARGUMENT; }
+      const int Q = d.q1d, D = d.d1d;
+      int nbz = std::min(elements_per_block(GBPA_DIFFUSION, GBPA_F64, D, Q), BATCH_THREADS / (Q * Q));
+      if (nbz < 1) { nbz = 1; }
+      BProb &p = hp[k];
+      p = BProb{};
+      p.ne = d.ne; p.ndofs = d.ndofs; p.D = D; p.Q = Q; p.nbz = nbz;
+      p.B = d.B; p.G = d.G; p.qd = d.qdata; p.dinv = d.dinv; p.b = d.b; p.x = d.x;
+      p.gmap = d.gather_map; p.off = d.offsets; p.ind = d.indices;
+      for (int e0 = 0; e0 < d.ne; e0 += nbz) { batches.push_back({k, e0, std::min(nbz, d.ne - e0)}); }
+      p.chunk0 = (int)chunks.size();
+      for (int i0 = 0; i0 < d.ndofs; i0 += CHUNK) { chunks.push_back({k, i0, std::min(d.ndofs, i0 + CHUNK)}); }
+      p.nchunk = (int)chunks.size() - p.chunk0;
+      ws_doubles += 3 * (size_t)d.ndofs + (size_t)d.ne * D * D * D;
+      if (d.n_ess > 0) { mask_bytes += (size_t)d.ndofs; }
+      const size_t sm = sizeof(double) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+      smem_max = std::max(smem_max, sm);
+   }
+   // ---- device workspace: one allocation for everything
+   const size_t nb = batches.size(), nc = chunks.size();
+   size_t off = 0;
+   auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+   const size_t o_probs = take(sizeof(BProb) * nprob);
+   const size_t o_scal = take(sizeof(BScal) * nprob);
+   const size_t o_batch = take(sizeof(BBatch) * (nb ? nb : 1));
+   const size_t o_chunk = take(sizeof(BChunk) * (nc ? nc : 1));
+   const size_t o_part = take(sizeof(double) * (nc ? nc : 1));
+   const size_t o_sync = take(sizeof(unsigned int) * 64);
+   const size_t o_ws = take(sizeof(double) * ws_doubles);
+   const size_t o_mask = take(mask_bytes ? mask_bytes : 1);
+   unsigned char *base = (unsigned char *)scratch(ctx, SLOT_BATCH, off);
+   if (!base) { return GBPA_ERR_OUT_OF_MEMORY; }
+   double *ws = (double *)(base + o_ws);
+   unsigned char *mk = base + o_mask;
+   int rc = check_cuda(cudaMemsetAsync(base + o_sync, 0, sizeof(unsigned int) * 64, ctx->stream), "memset");
+   if (!rc && mask_bytes) { rc = check_cuda(cudaMemsetAsync(mk, 0, mask_bytes, ctx->stream), "memset"); }
+   if (rc) { return rc; }
+   for (int k = 0; k < nprob; ++k)
+   {
+      BProb &p = hp[k];
+      const gbpa_problem_desc &d = probs[k];
+      p.r = ws; p.d = ws + d.ndofs; p.z = ws + 2 * (size_t)d.ndofs; p.yE = ws + 3 * (size_t)d.ndofs;
+      ws += 3 * (size_t)d.ndofs + (size_t)d.ne * d.d1d * d.d1d * d.d1d;
+      p.mask = nullptr;
+      if (d.n_ess > 0)
+      {
+         batched_mask_kernel<<<grid_for(d.n_ess, 256), 256, 0, ctx->stream>>>(d.n_ess, d.ess, mk, d.ndofs,
+                                                                            ctx->d_flags);
+         rc = last_launch(ctx, "batched_mask");
+         if (rc) { return rc; }
+         p.mask = mk;
+         mk += d.ndofs;
+      }
+   }
+   rc = check_cuda(cudaMemcpyAsync(base + o_probs, hp.data(), sizeof(BProb) * nprob, cudaMemcpyHostToDevice, ctx->stream), "copy");
+   if (!rc && nb) { rc = check_cuda(cudaMemcpyAsync(base + o_batch, batches.data(), sizeof(BBatch) * nb, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
+   if (!rc && nc) { rc = check_cuda(cudaMemcpyAsync(base + o_chunk, chunks.data(), sizeof(BChunk) * nc, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
+   if (rc) { return rc; }
+   int flags0 = 0;
+   rc = gbpa_get_error_flags(ctx, &flags0);   // syncs: host tables may go out of scope after
+   if (rc) { return rc; }
+   if (flags0 & GBPA_FLAG_INDEX) { return GBPA_ERR_INDEX; }
+
+   BParams P;
+   P.probs = (const BProb *)(base + o_probs);
+   P.scal = (BScal *)(base + o_scal);
+   P.nprob = nprob;
+   P.batches = (const BBatch *)(base + o_batch);
+   P.nbatch = (int)nb;
+   P.chunks = (const BChunk *)(base + o_chunk);
+   P.nchunk = (int)nc;
+   P.partials = (double *)(base + o_part);
+   P.rel2 = rel_tol * rel_tol;
+   P.abs2 = abs_tol * abs_tol;
+   P.max_it = max_it;
+   unsigned int *sync = (unsigned int *)(base + o_sync);
+   P.bar_count = sync;
+   P.bar_gen = sync + 32;
+   P.flags = ctx->d_flags;
+   P.n_active = (int *)(sync + 1);
+   P.abort = (int *)(sync + 2);
+   P.spin_limit = 1LL << 26;   // ~2 s of 32 ns sleeps
+
+   const void *kfn = (const void *)batched_pcg_kernel;
+   rc = ensure_smem(kfn, smem_max);
+   if (rc) { return rc; }
+   int per_sm = 0;
+   rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_pcg_kernel,
+                                                                 BATCH_THREADS, smem_max),
+                   "occupancy");
+   if (rc) { return rc; }
+   if (per_sm < 1) { return GBPA_ERR_UNSUPPORTED; }
+   const int grid = per_sm * ctx->num_sms;
+   void *args[] = {&P};
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   rc = check_cuda(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(BATCH_THREADS), args, smem_max,
+                                               ctx->stream), "cudaLaunchCooperativeKernel");
+   ctx->launches++;
+   cudaEventRecord(e1, ctx->stream);
+   if (!rc) { rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize"); }
+   float ms = 0.f;
+   if (!rc) { cudaEventElapsedTime(&ms, e0, e1); }
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   if (rc) { return rc; }
+   if (seconds) { *seconds = ms * 1e-3; }
+   std::vector<BScal> hs(nprob);
+   rc = check_cuda(cudaMemcpy(hs.data(), base + o_scal, sizeof(BScal) * nprob, cudaMemcpyDeviceToHost),
+                   "copy back");
+   if (rc) { return rc; }
+   int flags = 0;
+   rc = gbpa_get_error_flags(ctx, &flags);
+   if (rc) { return rc; }
+   for (int k = 0; k < nprob; ++k)
+   {
+      if (iterations) { iterations[k] = hs[k].final_iter; }
+      if (converged) { converged[k] = hs[k].converged; }
+      if (final_norms) { final_norms[k] = hs[k].betanom >= 0 ? sqrt(hs[k].betanom) : hs[k].betanom; }
+   }
+   if (flags & GBPA_FLAG_TIMEOUT) { return GBPA_ERR_TIMEOUT; }
+   if (flags & GBPA_FLAG_NOT_FINITE) { return GBPA_ERR_NOT_FINITE; }
+   return GBPA_SUCCESS;
 }

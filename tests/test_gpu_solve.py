@@ -61,7 +61,10 @@ def test_pcg_matches_reference_solve():
     ref_it, ref_norm, ref_conv = g["cg_info"]
     assert info.converged == 1
     assert abs(info.iterations - int(ref_it)) <= 1
-    assert abs(info.final_norm - ref_norm) <= 0.05 * ref_norm
+    # the last preconditioned residual is rounding-dominated at 1e-12: check
+    # the stopping rule and the order of magnitude, not its digits
+    assert info.final_norm <= 1e-12 * info.initial_norm
+    assert 0.5 * ref_norm <= info.final_norm <= 2.0 * ref_norm
     assert relerr(H(X), g["X"]) < 1e-10
     assert info.true_rel_residual < 1e-10
     # iterative mode from the converged solution: converges immediately
