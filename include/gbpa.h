@@ -225,6 +225,26 @@ int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, void *yE);
  * diag is always FP64. */
 int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag);
 
+/* ------------------------------------------------- allocation-free apply */
+/* No counterpart in the reference. Computes y = R^T A_e R x for FP64
+ * diffusion -- what gbpa_operator_mult computes for an unconstrained FP64
+ * diffusion operator -- for callers that cannot allocate device memory: an
+ * application whose device memory is owned by its own pool allocator, or a
+ * path that must not trigger the device synchronisation cudaMalloc/cudaFree
+ * can cause. The E-vector scratch is a fixed static device array of
+ * GBPA_NOALLOC_MAX_EVEC doubles (16 MiB, held by every GPU that loads the
+ * library until the process exits); ne*d1d^3 beyond it returns
+ * GBPA_ERR_UNSUPPORTED. Work goes on `stream` (NULL: the legacy default
+ * stream). All calls share the scratch, so calls that overlap on the GPU race:
+ * serialise them. The first call on each device looks up the scratch's device
+ * address; make it before any stream capture. */
+#define GBPA_NOALLOC_MAX_EVEC (1 << 21)
+int gbpa_diffusion_mult_noalloc(void *stream, int ne, int ndofs, int d1d, int q1d,
+                                int symm, const double *B, const double *G,
+                                const double *qdata, const int *gather_map,
+                                const int *offsets, const int *indices,
+                                const double *x, double *y);
+
 /* -------------------------------------------------------- vector kernels */
 /* Vector::operator* (linalg/vector.cpp:1079-1106) with reduce()
  * (general/reducers.hpp:531-594): host out *result. Warp-shuffle tree,
