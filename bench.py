@@ -43,6 +43,11 @@ def parse():
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "x2"],
                     help="arithmetic of the timed operator (x2: FP64 data, double-float on FP32 pipes)")
     ap.add_argument("--cpu-sample-n", type=int, default=38)
+    ap.add_argument("--no-pcg", action="store_true", help="skip the precision-form PCG comparison")
+    ap.add_argument("--pcg-n", type=int, default=40,
+                    help="mesh size of the precision-form PCG comparison (77: ~29.5 M DOFs at p=4)")
+    ap.add_argument("--pcg-only", action="store_true", help="run only the precision-form PCG comparison")
+    ap.add_argument("--pcg-max-it", type=int, default=20000)
     return ap.parse_args()
 
 
@@ -284,6 +289,8 @@ def run_gpu(args):
     extras = {}
     if not args.no_extras and rank == 0 and prec == 0:
         extras = run_extras(args, fes, integ, op, x, y)
+        if not args.no_pcg:
+            extras["pcg"] = run_pcg_form(args.pcg_n, args.p, args.pcg_max_it)
 
     line = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
@@ -363,10 +370,71 @@ def run_extras(args, fes, integ, op, x, y):
     return out
 
 
+def run_pcg_form(n, p, max_it=2000):
+    """Precision form on the jittered mesh with kappa = exp(16 random Fourier
+    modes, amplitude 0.5), RHS ~ U[0,1] (seed 4), homogeneous Dirichlet
+    boundary: plain FP64 Jacobi-PCG, the same with the double-float operator,
+    and FP32-apply PCG inside FP64 defect correction. Every solve stops at a
+    relative residual of 1e-10 (preconditioned norm for PCG, true FP64
+    residual for the defect correction); the true FP64 residual and the
+    error against the FP64 solution are reported for each."""
+    import torch
+    from mfem_gb300 import _lib, fem
+    from mfem_gb300.pa import (DiffusionIntegrator, FiniteElementSpace, OperatorJacobiSmoother,
+                               PAOperator, Device)
+    dev = Device.get()
+    mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
+    fes = FiniteElementSpace(mesh, p)
+    integ = DiffusionIntegrator("kappa")
+    integ.AssemblePA(fes, modes=fem.kappa_modes(3))
+    ess = fes.GetBoundaryTrueDofs()
+    A64 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess)
+    M = OperatorJacobiSmoother(A64, ess)
+    nd = fes.ndofs
+    b = torch.from_numpy(fem.u01_array(4, nd)).cuda()
+    b[torch.from_numpy(ess).long().cuda()] = 0.0
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    out = {"workload": f"Dirichlet Poisson, lognormal kappa, jittered n={n}^3, p={p}, q={p + 2}, "
+                       f"{nd} DOFs, RHS~U[0,1]", "rel_tol": 1e-10}
+    info = _lib.SolveInfo()
+    X64 = torch.zeros_like(b)
+    st = dev.lib.gbpa_pcg_solve(A64.handle, P(M.dinv), P(b), P(X64), 1e-10, 0.0, max_it, 0,
+                                ctypes.byref(info))
+    out["fp64_pcg"] = {"status": st, "seconds": info.seconds, "iterations": info.iterations,
+                       "true_rel_residual": info.true_rel_residual}
+    Ax2 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=2)
+    Xx2 = torch.zeros_like(b)
+    st = dev.lib.gbpa_pcg_solve(Ax2.handle, P(M.dinv), P(b), P(Xx2), 1e-10, 0.0, max_it, 0,
+                                ctypes.byref(info))
+    out["f64x2_pcg"] = {"status": st, "seconds": info.seconds, "iterations": info.iterations,
+                        "true_rel_residual": info.true_rel_residual,
+                        "rel_l2_vs_fp64": float(torch.linalg.norm(Xx2 - X64) / torch.linalg.norm(X64))}
+    del Xx2
+    A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=1)
+    d32 = M.dinv.float()
+    for name, outer in (("mixed_f32_in_f64", A64), ("mixed_f32_in_f64x2", Ax2)):
+        Xm = torch.zeros_like(b)
+        st = dev.lib.gbpa_pcg_solve_mixed(outer.handle, A32.handle, P(d32), P(b), P(Xm), 1e-10, 1e-5,
+                                          30, max_it, ctypes.byref(info))
+        out[name] = {"status": st, "seconds": info.seconds, "outer": info.outer_iterations,
+                     "inner_iterations": info.inner_iterations,
+                     "true_rel_residual": info.true_rel_residual,
+                     "rel_l2_vs_fp64": float(torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64))}
+    t64 = out["fp64_pcg"]["seconds"]
+    out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64x2"]["seconds"], 1e-30)
+    out["speedup_mixed_f64outer_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.pcg_only:
+        from mfem_gb300.pa import Device
+        Device("cuda", dist_info()[2])
+        print(json.dumps({"pcg": run_pcg_form(args.pcg_n, args.p, args.pcg_max_it)}), flush=True)
+        return 0
     return run_gpu(args)
 
 

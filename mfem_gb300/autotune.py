@@ -1,0 +1,140 @@
+"""Autotuner for the apply kernels' block shape.
+
+For each (integrator, arithmetic, order p) the 2D-slab apply kernel runs with
+block (Q, Q, nbz); nbz -- elements per block -- sets the block size, the
+shared memory per block and therefore the occupancy. The tuner times the
+gather-fused element kernel on a synthetic jittered mesh for every feasible
+nbz and keeps the fastest. The table is saved as JSON (mfem_gb300/tuning.json)
+and applied by Device() on start-up through gbpa_set_elements_per_block.
+
+    python -m mfem_gb300.autotune [--orders 1-8] [--dofs 2e6] [--out path]
+"""
+import argparse
+import ctypes
+import json
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TUNING = os.path.join(HERE, "tuning.json")
+
+KINDS = {"diffusion": 0, "mass": 1}
+PRECS = {"f64": 0, "f32": 1, "f64x2": 2}
+
+
+def key(kind, prec, D, Q):
+    return f"{kind}:{prec}:{D}:{Q}"
+
+
+def apply_table(lib, table):
+    """Install a tuning table into the library (kind/prec names as in KINDS, PRECS)."""
+    n = 0
+    for k, nbz in table.items():
+        kind, prec, D, Q = k.split(":")
+        if lib.gbpa_set_elements_per_block(KINDS[kind], PRECS[prec], int(D), int(Q), int(nbz)) == 0:
+            n += 1
+    return n
+
+
+def load_default(lib):
+    if os.path.exists(TUNING):
+        with open(TUNING) as f:
+            return apply_table(lib, json.load(f).get("nbz", {}))
+    return 0
+
+
+def smem_bytes(kind, w, D, Q, nbz):
+    if kind == "diffusion":
+        per = max(D ** 3, 3 * D * Q * Q) + 2 * D * D * Q
+        return w * (2 * Q * D + nbz * per)
+    per = max(D ** 3, D * Q * Q) + D * D * Q
+    return w * (Q * D + nbz * per)
+
+
+def candidates(kind, prec, D, Q):
+    w = 4 if prec == "f32" else 8
+    out = []
+    for nbz in range(1, 65):
+        if nbz * Q * Q > 1024 or smem_bytes(kind, w, D, Q, nbz) > 200 * 1024:
+            break
+        out.append(nbz)
+    return out
+
+
+def time_nbz(lib, op, x, yE, reps):
+    import torch
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    for _ in range(2):
+        lib.gbpa_operator_apply_element(op.handle, P(x), P(yE))
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        st = lib.gbpa_operator_apply_element(op.handle, P(x), P(yE))
+        if st != 0:
+            return float("inf")
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "f64x2"),
+         target_dofs=2e6, reps=10, verbose=True):
+    import torch
+    from . import fem
+    from .pa import DiffusionIntegrator, Device, FiniteElementSpace, MassIntegrator, PAOperator
+    dev = Device.get()
+    lib = dev.lib
+    table, timings = {}, {}
+    for p in orders:
+        n = max(2, int(round((target_dofs ** (1 / 3) - 1) / p)))
+        mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
+        fes = FiniteElementSpace(mesh, p)
+        for kind in kinds:
+            integ = DiffusionIntegrator() if kind == "diffusion" else MassIntegrator()
+            integ.AssemblePA(fes)
+            D, Q = integ.D, integ.Q
+            for prec in precs:
+                if prec == "f64x2" and (D > 10 or Q > 10):
+                    continue
+                pid = PRECS[prec]
+                op = PAOperator(KINDS[kind], fes, D, Q, integ.B, integ.G, integ.qdata, precision=pid)
+                dt = torch.float32 if prec == "f32" else torch.float64
+                x = (torch.rand(fes.ndofs, device="cuda") - 0.5).to(dt)
+                yE = torch.empty(fes.ne * D ** 3, dtype=dt, device="cuda")
+                best = (float("inf"), None)
+                res = {}
+                for nbz in candidates(kind, prec, D, Q):
+                    lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, nbz)
+                    ms = time_nbz(lib, op, x, yE, reps)
+                    res[nbz] = ms
+                    best = min(best, (ms, nbz))
+                lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, 0)
+                if best[1] is not None:
+                    table[key(kind, prec, D, Q)] = best[1]
+                    timings[key(kind, prec, D, Q)] = {"ne": fes.ne, "ndofs": fes.ndofs, "ms": res}
+                    if verbose:
+                        default = lib.gbpa_get_elements_per_block(KINDS[kind], pid, D, Q)
+                        print(f"{kind:9s} {prec:6s} p={p} D={D} Q={Q}: best nbz={best[1]} "
+                              f"{best[0]:.4f} ms (default nbz={default}: {res.get(default, float('nan')):.4f} ms)",
+                              flush=True)
+                del op, x, yE
+            del integ
+    return table, timings
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--orders", default="1-8")
+    ap.add_argument("--dofs", type=float, default=2e6)
+    ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--out", default=TUNING)
+    args = ap.parse_args()
+    lo, hi = (int(v) for v in args.orders.split("-"))
+    table, timings = tune(range(lo, hi + 1), target_dofs=args.dofs, reps=args.reps)
+    with open(args.out, "w") as f:
+        json.dump({"nbz": table, "timings_ms": timings}, f, indent=1, sort_keys=True)
+    print(f"wrote {args.out} ({len(table)} entries)")
+
+
+if __name__ == "__main__":
+    main()

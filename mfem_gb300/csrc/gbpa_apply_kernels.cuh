@@ -34,6 +34,7 @@ struct f2
 
 struct ArF64
 {
+   static constexpr bool kPrefetch = false;
    using V = double; using In = double; using Qd = double;
    static __device__ __forceinline__ V zero() { return 0.0; }
    static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fma(a, b, acc); }
@@ -46,6 +47,10 @@ struct ArF64
 
 struct ArF32
 {
+   // FP32 is bound by memory latency, not arithmetic: each thread loads its
+   // column of symmetric qdata (6 Q values) into registers before the x/y
+   // contractions, so those loads overlap the first two stages.
+   static constexpr bool kPrefetch = true;
    using V = float; using In = float; using Qd = float;
    static __device__ __forceinline__ V zero() { return 0.f; }
    static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fmaf(a, b, acc); }
@@ -58,6 +63,7 @@ struct ArF32
 
 struct ArX2
 {
+   static constexpr bool kPrefetch = false;
    using V = f2; using In = double; using Qd = float2;
    static __device__ __forceinline__ V zero() { return {0.f, 0.f}; }
    // acc += a * b. The rounded product p = a.h*b.h and its exact error
@@ -145,6 +151,20 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    constexpr int DM = TD ? TD : MAXD;
    constexpr int QM = TQ ? TQ : MAXQ;
    const int D3 = D * D * D, Q3 = Q * Q * Q;
+   // register prefetch of this thread's symmetric qdata column (kPrefetch)
+   constexpr bool PF = AR::kPrefetch && TQ > 0;
+   V qpre[PF ? 6 : 1][PF ? QM : 1];
+   if constexpr (PF)
+   {
+      if (part && active && symm)
+      {
+         const typename AR::Qd *qe = qd + e * 6 * Q3 + tx + Q * ty;
+#pragma unroll
+         for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int qz = 0; qz < QM; ++qz) { qpre[k][qz] = AR::ldq(qe + k * Q3 + Q * Q * qz); }
+      }
+   }
    if (part && active)
    {
       const long long base = e * D3;
@@ -236,9 +256,17 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             const typename AR::Qd *qp = qe + Q * Q * qz;
             if (symm)
             {
-               const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
-               const V O22 = AR::ldq(qp + 3 * Q3), O23 = AR::ldq(qp + 4 * Q3);
-               const V O33 = AR::ldq(qp + 5 * Q3);
+               V O11, O12, O13, O22, O23, O33;
+               if constexpr (PF)
+               {
+                  O11 = qpre[0][qz]; O12 = qpre[1][qz]; O13 = qpre[2][qz];
+                  O22 = qpre[3][qz]; O23 = qpre[4][qz]; O33 = qpre[5][qz];
+               }
+               else
+               {
+                  O11 = AR::ldq(qp); O12 = AR::ldq(qp + Q3); O13 = AR::ldq(qp + 2 * Q3);
+                  O22 = AR::ldq(qp + 3 * Q3); O23 = AR::ldq(qp + 4 * Q3); O33 = AR::ldq(qp + 5 * Q3);
+               }
                AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
                AR::mac(oy, O12, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
                AR::mac(oz, O13, gx); AR::mac(oz, O23, gy); AR::mac(oz, O33, gz);

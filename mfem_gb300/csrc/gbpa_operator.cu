@@ -493,7 +493,9 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
    int rc = ensure_pcg_workspace(op);
    if (rc) { return rc; }
    T *r = (T *)op->r, *d = (T *)op->dv, *z = (T *)op->z;
-   const unsigned grid = grid_for(n, PCG_BLOCK, 2 * ctx->num_sms);
+   // 4 blocks of 512 threads per SM: full occupancy for the streaming vector
+   // phases (partials buffer holds 2048 entries per reduction)
+   const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
    cudaEvent_t e0, e1;
    cudaEventCreate(&e0); cudaEventCreate(&e1);
    cudaEventRecord(e0, ctx->stream);

@@ -55,6 +55,9 @@ class Device:
         # "own stream", so name the legacy default stream (handle 1) instead
         h = torch.cuda.current_stream().cuda_stream
         check(self.lib.gbpa_set_stream(self.ctx, ctypes.c_void_p(h if h else 1)), "gbpa_set_stream")
+        # block shapes chosen by the autotuner (mfem_gb300/tuning.json), if present
+        from .autotune import load_default
+        self.tuned_entries = load_default(self.lib)
         Device._current = self
 
     @classmethod

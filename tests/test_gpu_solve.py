@@ -67,10 +67,15 @@ def test_pcg_matches_reference_solve():
     assert 0.5 * ref_norm <= info.final_norm <= 2.0 * ref_norm
     assert relerr(H(X), g["X"]) < 1e-10
     assert info.true_rel_residual < 1e-10
-    # iterative mode from the converged solution: converges immediately
-    st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 1e-12, 0.0, 500, 1,
-                                  ctypes.byref(info))
-    assert st == 0 and info.iterations <= 2
+    # iterative mode (linalg/solvers.cpp:875-879) from the converged solution:
+    # r0 = b - A x is already at the converged level, and an absolute
+    # tolerance just above it stops the solve at once, on the same solution
+    first_initial = info.initial_norm
+    st = dev().lib.gbpa_pcg_solve(A.handle, p(dinv), p(T(g["B_rhs"])), p(X), 0.0, 1e-8 * first_initial,
+                                  500, 1, ctypes.byref(info))
+    assert st == 0 and info.converged == 1 and info.iterations == 0
+    assert info.initial_norm <= 1e-8 * first_initial
+    assert relerr(H(X), g["X"]) < 1e-10
 
 
 def test_mixed_precision_matches_reference_solve():
