@@ -421,8 +421,12 @@ def run_pcg_form(n, p, max_it=2000):
                      "true_rel_residual": info.true_rel_residual,
                      "rel_l2_vs_fp64": float(torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64))}
     t64 = out["fp64_pcg"]["seconds"]
-    out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64x2"]["seconds"], 1e-30)
-    out["speedup_mixed_f64outer_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
+    # the precision form proper: FP32 apply inside FP64 defect correction whose
+    # true residual uses the native FP64 operator (the double-float outer
+    # operator's ~1e-14 error, amplified by the condition number, can stall the
+    # true residual above 1e-10 on ill-conditioned problems; reported beside)
+    out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
+    out["speedup_mixed_vs_f64x2_pcg"] = out["f64x2_pcg"]["seconds"] / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
     return out
 
 

@@ -292,6 +292,27 @@ int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
                          double outer_rel_tol, double inner_rel_tol,
                          int max_outer, int max_inner, gbpa_solve_info *info);
 
+/* ------------------------------------------- several right-hand sides */
+/* R = nrhs right-hand sides stored interleaved (v[i*R + r]), R in {1, 2, 4,
+ * 8}; diffusion operators only. The block apply reads each element's qdata
+ * once for all R vectors (BilinearForm::Mult applied to R vectors,
+ * fem/bilinearform_ext.cpp:487-564). */
+int gbpa_operator_mult_block(gbpa_operator_t op, int nrhs, const void *x, void *y);
+/* R independent CGSolver::Mult recurrences (linalg/solvers.cpp:869-1050),
+ * one set of scalars and one stopping test per right-hand side, sharing the
+ * block apply. FP64 (or F64X2) operator; info has nrhs entries. */
+int gbpa_pcg_solve_block(gbpa_operator_t A, int nrhs, const double *dinv,
+                         const double *b, double *x, double rel_tol,
+                         double abs_tol, int max_it, gbpa_solve_info *info);
+/* Mixed precision per right-hand side: FP32 block PCG inner solves inside
+ * FP64 defect correction with FP64 true residuals (b - A64 x), until every
+ * right-hand side reaches outer_rel_tol. */
+int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
+                               int nrhs, const float *dinv32, const double *b,
+                               double *x, double outer_rel_tol,
+                               double inner_rel_tol, int max_outer,
+                               int max_inner, gbpa_solve_info *info);
+
 /* ---------------------------------------------------------- batched PCG */
 /* Batching form: many independent Dirichlet problems of uneven size and
  * order, solved together. Each problem owns its maps, qdata and vectors

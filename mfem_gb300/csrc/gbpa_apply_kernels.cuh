@@ -47,10 +47,11 @@ struct ArF64
 
 struct ArF32
 {
-   // FP32 is bound by memory latency, not arithmetic: each thread loads its
-   // column of symmetric qdata (6 Q values) into registers before the x/y
-   // contractions, so those loads overlap the first two stages.
-   static constexpr bool kPrefetch = true;
+   // Register prefetch of the qdata column (6 Q values per thread, loaded
+   // before the x/y contractions) measured slower on GB300 at p=4 (1.59 vs
+   // 1.49 ms per 29.5 M-DOF apply: the extra registers cost occupancy), so it
+   // is off; the code path stays for other orders and tuning.
+   static constexpr bool kPrefetch = false;
    using V = float; using In = float; using Qd = float;
    static __device__ __forceinline__ V zero() { return 0.f; }
    static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fmaf(a, b, acc); }
@@ -110,12 +111,13 @@ template <typename AR, bool COH = false>
 __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__restrict__ x,
                                                        const int *__restrict__ gmap,
                                                        const unsigned char *__restrict__ mask,
-                                                       long long slot)
+                                                       long long slot, int xs = 1)
 {
    const int g = __ldg(gmap + slot);
    const int j = g >= 0 ? g : -1 - g;
    if (mask && __ldg(mask + j)) { return AR::zero(); }
-   const typename AR::V v = AR::in(COH ? __ldcg(x + j) : __ldg(x + j));
+   const typename AR::In *p = x + (long long)j * xs;
+   const typename AR::V v = AR::in(COH ? __ldcg(p) : __ldg(p));
    return g >= 0 ? v : AR::neg(v);
 }
 
@@ -145,8 +147,10 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                   typename AR::V *__restrict__ bufA, typename AR::V *__restrict__ bufB,
                   const typename AR::Qd *__restrict__ qd, const typename AR::In *__restrict__ x,
                   const int *__restrict__ gmap, const unsigned char *__restrict__ mask,
-                  typename AR::In *__restrict__ y, int accumulate)
+                  typename AR::In *__restrict__ y, int accumulate, int xs = 1, int ys = 1)
 {
+   // xs, ys: element strides of the gathered L-vector and of the output
+   // E-vector (> 1 for right-hand sides stored interleaved)
    using V = typename AR::V;
    constexpr int DM = TD ? TD : MAXD;
    constexpr int QM = TQ ? TQ : MAXQ;
@@ -170,7 +174,8 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
       const long long base = e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
       {
-         bufA[i] = GATHER ? gather_value<AR, COH>(x, gmap, mask, base + i) : AR::in(x[base + i]);
+         bufA[i] = GATHER ? gather_value<AR, COH>(x, gmap, mask, base + i, xs)
+                          : AR::in(x[(base + i) * xs]);
       }
    }
    __syncthreads();
@@ -357,7 +362,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                   AR::mac(v, sG[qx * D + dx], U0[o]);
                   AR::mac(v, sB[qx * D + dx], U12[o]);
                }
-               const long long k = base + dx + D * (dy + D * dz);
+               const long long k = (base + dx + D * (dy + D * dz)) * ys;
                const typename AR::In r = AR::out(AR::fin(v));
                y[k] = accumulate ? y[k] + r : r;
             }
@@ -400,6 +405,47 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    }
    diffusion_element<AR, TD, TQ, GATHER, MAXD, MAXQ>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG,
                                                      bufA, bufB, qd, x, gmap, mask, y, accumulate);
+}
+
+// R right-hand sides stored interleaved (x[j*R + r], E-vector out
+// y[(e*D^3 + k)*R + r]). Block (Q, Q, nbz*R): slab tz handles right-hand side
+// tz % R of element blockIdx.x*nbz + tz / R, so the R slabs of an element sit
+// in one block and HBM delivers its qdata once for all R vectors (the other
+// R-1 reads hit L1).
+template <typename AR, int TD, int TQ>
+__global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d, int q1d,
+                                             const typename AR::In *__restrict__ gB,
+                                             const typename AR::In *__restrict__ gG,
+                                             const typename AR::Qd *__restrict__ qd,
+                                             const typename AR::In *__restrict__ x,
+                                             const int *__restrict__ gmap,
+                                             const unsigned char *__restrict__ mask,
+                                             typename AR::In *__restrict__ y,
+                                             const int *__restrict__ skip)
+{
+   using V = typename AR::V;
+   if (skip && *skip) { return; }
+   const int D = TD ? TD : d1d;
+   const int Q = TQ ? TQ : q1d;
+   const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+   const int e = blockIdx.x * (blockDim.z / nrhs) + tz / nrhs;
+   const int r = tz % nrhs;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   V *sB = reinterpret_cast<V *>(smem_raw);
+   V *sG = sB + Q * D;
+   const int per = diff_smem_per_elem(D, Q);
+   V *bufA = sG + Q * D + tz * per;
+   V *bufB = bufA + (per - 2 * D * D * Q);
+   const int tid = tx + Q * (ty + Q * tz);
+   const int nthr = Q * Q * blockDim.z;
+   for (int i = tid; i < Q * D; i += nthr)
+   {
+      const int q = i % Q, d = i / Q;
+      sB[q * D + d] = AR::in(gB[i]);
+      sG[q * D + d] = AR::in(gG[i]);
+   }
+   diffusion_element<AR, TD, TQ, true>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG, bufA, bufB,
+                                       qd, x + r, gmap, mask, y + r, 0, nrhs, nrhs);
 }
 
 template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>

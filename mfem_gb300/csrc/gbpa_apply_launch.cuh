@@ -56,6 +56,38 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
                          args, smem, "diffusion_apply");
 }
 
+// Block (multi right-hand side) diffusion apply: compile-time kernels for
+// Q = D + 1, the generic kernel otherwise.
+template <typename AR>
+static const void *diffusion_block_kernel_for(int D, int Q)
+{
+#define GBPA_CASE(d) \
+   if (D == d && Q == d + 1) { return (const void *)diffusion_apply_block_kernel<AR, d, d + 1>; }
+   GBPA_CASE(2) GBPA_CASE(3) GBPA_CASE(4) GBPA_CASE(5) GBPA_CASE(6) GBPA_CASE(7) GBPA_CASE(8)
+#undef GBPA_CASE
+   return (const void *)diffusion_apply_block_kernel<AR, 0, 0>;
+}
+
+template <typename AR>
+int launch_diffusion_block_ar(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, int Q,
+                              const typename AR::In *B, const typename AR::In *G,
+                              const typename AR::Qd *qd, const typename AR::In *x,
+                              const int *gather_map, const unsigned char *ess_mask,
+                              typename AR::In *y, const int *skip)
+{
+   if (ne == 0) { return GBPA_SUCCESS; }
+   const size_t per_slab = sizeof(typename AR::V) * diff_smem_per_elem(D, Q);
+   const size_t tables = sizeof(typename AR::V) * 2 * Q * D;
+   if (Q * Q * nrhs > 1024 || tables + nrhs * per_slab > 200 * 1024) { return GBPA_ERR_UNSUPPORTED; }
+   int nbz = 1;
+   while ((nbz + 1) * Q * Q * nrhs <= 1024 && tables + (nbz + 1) * nrhs * per_slab <= 110 * 1024) { ++nbz; }
+   const size_t smem = tables + (size_t)nbz * nrhs * per_slab;
+   void *args[] = {&ne, &nrhs, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd, (void *)&x,
+                   (void *)&gather_map, (void *)&ess_mask, &y, (void *)&skip};
+   return launch_generic(ctx, diffusion_block_kernel_for<AR>(D, Q), dim3((ne + nbz - 1) / nbz),
+                         dim3(Q, Q, nbz * nrhs), args, smem, "diffusion_apply_block");
+}
+
 template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
 int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
                    const typename AR::In *B, const typename AR::Qd *qd,

@@ -58,14 +58,38 @@ int ensure_smem(const void *kernel, size_t bytes)
    return rc;
 }
 
+// Largest block the kernel can launch with (register-limited), cached.
+static int max_threads_for(const void *kernel)
+{
+   static std::mutex mu;
+   static std::unordered_map<const void *, int> cache;
+   std::lock_guard<std::mutex> lock(mu);
+   auto it = cache.find(kernel);
+   if (it != cache.end()) { return it->second; }
+   cudaFuncAttributes a;
+   int m = 1024;
+   if (cudaFuncGetAttributes(&a, kernel) == cudaSuccess) { m = a.maxThreadsPerBlock; }
+   else { cudaGetLastError(); }
+   cache[kernel] = m;
+   return m;
+}
+
 int launch_generic(gbpa_ctx *ctx, const void *kernel, dim3 grid, dim3 block,
                    void **args, size_t smem, const char *what)
 {
    if (smem > 227 * 1024) { return GBPA_ERR_UNSUPPORTED; }
-   if (block.x * block.y * block.z > 1024) { return GBPA_ERR_UNSUPPORTED; }
+   const int threads = (int)(block.x * block.y * block.z);
+   if (threads > 1024 || threads > max_threads_for(kernel)) { return GBPA_ERR_UNSUPPORTED; }
    int rc = ensure_smem(kernel, smem);
    if (rc) { return rc; }
-   rc = check_cuda(cudaLaunchKernel(kernel, grid, block, args, smem, ctx->stream), what);
+   const cudaError_t e = cudaLaunchKernel(kernel, grid, block, args, smem, ctx->stream);
+   if (e != cudaSuccess)
+   {
+      // a refused launch sets the runtime's last-error; clear it so a later,
+      // unrelated check does not report it again
+      cudaGetLastError();
+   }
+   rc = check_cuda(e, what);
    ctx->launches++;
    return rc;
 }

@@ -5,38 +5,11 @@
 //   ConstrainedOperator (DIAG_ONE)    linalg/operator.cpp:526-661
 //   CGSolver::Mult                    linalg/solvers.cpp:869-1050
 //   OperatorJacobiSmoother::Mult      linalg/solvers.cpp:427-452
-#include "gbpa_dispatch.cuh"
+#include "gbpa_operator.cuh"
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <new>
-
-struct PcgState
-{
-   double nom, nom0, den, betanom, alpha, beta, r0;
-   double rel_tol2, abs_tol2;
-   int iter, done, converged, status, final_iter, max_it;
-   unsigned int counter_den, counter_beta, counter_init;
-   int pad;
-};
-
-struct gbpa_operator
-{
-   gbpa_ctx *ctx = nullptr;
-   gbpa_operator_desc d{};
-   unsigned char *mask = nullptr;   // ess mask (ndofs) or null
-   void *yE = nullptr;              // E-vector scratch in the operator's precision
-   float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
-   // PCG workspace (vectors in the operator's precision)
-   void *r = nullptr, *dv = nullptr, *z = nullptr;
-   double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)
-   PcgState *state = nullptr;
-   int64_t ws_n = 0;
-   cudaGraphExec_t graph = nullptr;
-   const void *graph_x = nullptr, *graph_dinv = nullptr;
-   // mixed-precision helpers (FP64 vectors)
-   double *r64 = nullptr, *t64 = nullptr;
-};
 
 namespace gbpa
 {
@@ -345,7 +318,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->qd2);
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
-   cudaFree(op->r64); cudaFree(op->t64);
+   cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb);
    delete op;
    return GBPA_SUCCESS;
 }

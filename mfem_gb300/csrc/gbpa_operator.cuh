@@ -1,0 +1,34 @@
+// Operator object shared by the operator and block-solver translation units.
+#pragma once
+#include "gbpa_dispatch.cuh"
+
+struct PcgState
+{
+   double nom, nom0, den, betanom, alpha, beta, r0;
+   double rel_tol2, abs_tol2;
+   int iter, done, converged, status, final_iter, max_it;
+   unsigned int counter_den, counter_beta, counter_init;
+   int pad;
+};
+
+struct gbpa_operator
+{
+   gbpa_ctx *ctx = nullptr;
+   gbpa_operator_desc d{};
+   unsigned char *mask = nullptr;   // ess mask (ndofs) or null
+   void *yE = nullptr;              // E-vector scratch in the operator's precision
+   float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
+   // PCG workspace (vectors in the operator's precision)
+   void *r = nullptr, *dv = nullptr, *z = nullptr;
+   double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)
+   PcgState *state = nullptr;
+   int64_t ws_n = 0;
+   cudaGraphExec_t graph = nullptr;
+   const void *graph_x = nullptr, *graph_dinv = nullptr;
+   // mixed-precision helpers (FP64 vectors)
+   double *r64 = nullptr, *t64 = nullptr;
+   // block (multi right-hand side) scratch: E-vector for nrhs interleaved
+   void *yEb = nullptr;
+   int yEb_nrhs = 0;
+};
+
