@@ -43,6 +43,8 @@ struct ArF64
    static __device__ __forceinline__ V fin(V a) { return a; }
    static __device__ __forceinline__ In out(V v) { return v; }
    static __device__ __forceinline__ V ldq(const Qd *p) { return __ldg(p); }
+   static __device__ __forceinline__ V lds(const Qd *p) { return *p; }
+   static constexpr bool kTmaQd = false;   // FP64-pipe bound: no staging
 };
 
 struct ArF32
@@ -60,6 +62,9 @@ struct ArF32
    static __device__ __forceinline__ V fin(V a) { return a; }
    static __device__ __forceinline__ In out(V v) { return v; }
    static __device__ __forceinline__ V ldq(const Qd *p) { return __ldg(p); }
+   static __device__ __forceinline__ V lds(const Qd *p) { return *p; }
+   // memory-latency bound: stage the block's qdata with one TMA bulk copy
+   static constexpr bool kTmaQd = true;
 };
 
 struct ArX2
@@ -102,11 +107,57 @@ struct ArX2
       const float2 t = __ldg(p);
       return {t.x, t.y};
    }
+   static __device__ __forceinline__ V lds(const Qd *p)
+   {
+      const float2 t = *p;
+      return {t.x, t.y};
+   }
+   static constexpr bool kTmaQd = false;
 };
 
 // COH: x was written earlier in the same launch by other blocks (persistent
 // solvers), so it is read through L2 (__ldcg) instead of the non-coherent
 // read-only path.
+// ------------------------------------------------ TMA bulk copy + mbarrier
+// A block's qdata (nbz consecutive elements) is one contiguous range, so one
+// thread stages it into shared memory with a single cp.async.bulk that
+// completes on an mbarrier; the other threads meanwhile gather x and run the
+// x/y contractions. The source must start on a 16-byte boundary and the size
+// be a multiple of 16 bytes (the host checks both).
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+   return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void *sdst, const void *gsrc, unsigned bytes,
+                                            unsigned long long *bar)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+// Wait for phase `parity` of the mbarrier with a bounded number of polls.
+// Returns false on expiry; the caller then writes NaN for its element, so a
+// copy that never lands shows up as a non-finite result (PCG reports
+// GBPA_ERR_NOT_FINITE) and the kernel always terminates.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+   for (long long it = 0; it < (1LL << 24); ++it)
+   {
+      unsigned ok;
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                   " selp.u32 %0, 1, 0, p;\n}"
+                   : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+      if (ok) { return true; }
+   }
+   return false;
+}
+
 template <typename AR, bool COH = false>
 __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__restrict__ x,
                                                        const int *__restrict__ gmap,
@@ -147,10 +198,13 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                   typename AR::V *__restrict__ bufA, typename AR::V *__restrict__ bufB,
                   const typename AR::Qd *__restrict__ qd, const typename AR::In *__restrict__ x,
                   const int *__restrict__ gmap, const unsigned char *__restrict__ mask,
-                  typename AR::In *__restrict__ y, int accumulate, int xs = 1, int ys = 1)
+                  typename AR::In *__restrict__ y, int accumulate, int xs = 1, int ys = 1,
+                  const typename AR::Qd *sQ = nullptr, unsigned long long *qbar = nullptr)
 {
    // xs, ys: element strides of the gathered L-vector and of the output
-   // E-vector (> 1 for right-hand sides stored interleaved)
+   // E-vector (> 1 for right-hand sides stored interleaved).
+   // sQ, qbar: this element's qdata staged in shared memory by a TMA bulk
+   // copy completing on qbar (phase 0); nullptr reads qdata from global.
    using V = typename AR::V;
    constexpr int DM = TD ? TD : MAXD;
    constexpr int QM = TQ ? TQ : MAXQ;
@@ -215,6 +269,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    V oA[DM], oB[DM], oC[DM];
 #pragma unroll
    for (int dz = 0; dz < DM; ++dz) { oA[dz] = AR::zero(); oB[dz] = AR::zero(); oC[dz] = AR::zero(); }
+   bool qok = true;   // false if the staged qdata never arrived
    if (part)
    {
       // stage 2 (y) into registers: rA = G_x B_y, rBv = B_x G_y, rC = B_x B_y
@@ -239,7 +294,10 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
       }
 
       // stage 3 (z) + pointwise qdata + backward z, fused per qz
-      const typename AR::Qd *qe = qd + e * (symm ? 6 : 9) * Q3 + tx + Q * ty;
+      if (sQ && active) { qok = mbar_wait(qbar, 0); }
+      const typename AR::Qd *qe = (sQ ? sQ : qd + e * (symm ? 6 : 9) * Q3) + tx + Q * ty;
+      // staged qdata is read from shared memory; otherwise read-only global
+      auto LQ = [sQ](const typename AR::Qd *p) { return sQ ? AR::lds(p) : AR::ldq(p); };
 #pragma unroll
       for (int qz = 0; qz < QM; ++qz)
       {
@@ -269,8 +327,8 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                }
                else
                {
-                  O11 = AR::ldq(qp); O12 = AR::ldq(qp + Q3); O13 = AR::ldq(qp + 2 * Q3);
-                  O22 = AR::ldq(qp + 3 * Q3); O23 = AR::ldq(qp + 4 * Q3); O33 = AR::ldq(qp + 5 * Q3);
+                  O11 = LQ(qp); O12 = LQ(qp + Q3); O13 = LQ(qp + 2 * Q3);
+                  O22 = LQ(qp + 3 * Q3); O23 = LQ(qp + 4 * Q3); O33 = LQ(qp + 5 * Q3);
                }
                AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
                AR::mac(oy, O12, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
@@ -278,10 +336,10 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             }
             else
             {
-               const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
-               const V O21 = AR::ldq(qp + 3 * Q3), O22 = AR::ldq(qp + 4 * Q3);
-               const V O23 = AR::ldq(qp + 5 * Q3), O31 = AR::ldq(qp + 6 * Q3);
-               const V O32 = AR::ldq(qp + 7 * Q3), O33 = AR::ldq(qp + 8 * Q3);
+               const V O11 = LQ(qp), O12 = LQ(qp + Q3), O13 = LQ(qp + 2 * Q3);
+               const V O21 = LQ(qp + 3 * Q3), O22 = LQ(qp + 4 * Q3);
+               const V O23 = LQ(qp + 5 * Q3), O31 = LQ(qp + 6 * Q3);
+               const V O32 = LQ(qp + 7 * Q3), O33 = LQ(qp + 8 * Q3);
                AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
                AR::mac(oy, O21, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
                AR::mac(oz, O31, gx); AR::mac(oz, O32, gy); AR::mac(oz, O33, gz);
@@ -363,7 +421,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                   AR::mac(v, sB[qx * D + dx], U12[o]);
                }
                const long long k = (base + dx + D * (dy + D * dz)) * ys;
-               const typename AR::In r = AR::out(AR::fin(v));
+               const typename AR::In r = qok ? AR::out(AR::fin(v)) : (typename AR::In)NAN;
                y[k] = accumulate ? y[k] + r : r;
             }
          }
@@ -380,14 +438,17 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
                                        const int *__restrict__ gmap,
                                        const unsigned char *__restrict__ mask,
                                        typename AR::In *__restrict__ y, int accumulate,
-                                       const int *__restrict__ skip)
+                                       const int *__restrict__ skip, int tma)
 {
    using V = typename AR::V;
+   using Qd = typename AR::Qd;
    if (skip && *skip) { return; }   // uniform per launch: solver finished
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
-   const int e = blockIdx.x * blockDim.z + tz;
+   const int nbz = blockDim.z;
+   const int e0 = blockIdx.x * nbz;
+   const int e = e0 + tz;
 
    extern __shared__ __align__(16) unsigned char smem_raw[];
    V *sB = reinterpret_cast<V *>(smem_raw);       // [Q][D]
@@ -396,7 +457,28 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    V *bufA = sG + Q * D + tz * per;               // X, then T0|T1|T2
    V *bufB = bufA + (per - 2 * D * D * Q);        // BX|GX, then U0|U12
    const int tid = tx + Q * (ty + Q * tz);
-   const int nthr = Q * Q * blockDim.z;
+   const int nthr = Q * Q * nbz;
+   // optional TMA staging of the block's qdata: [tile | mbarrier] after the buffers
+   const int S = symm ? 6 : 9;
+   const int Q3 = Q * Q * Q;
+   Qd *sQ = nullptr;
+   unsigned long long *bar = nullptr;
+   if (AR::kTmaQd && tma)
+   {
+      size_t off = sizeof(V) * (2 * Q * D + (size_t)nbz * per);
+      off = (off + 15) & ~size_t(15);
+      sQ = reinterpret_cast<Qd *>(smem_raw + off);
+      off += sizeof(Qd) * (size_t)nbz * S * Q3;
+      off = (off + 7) & ~size_t(7);
+      bar = reinterpret_cast<unsigned long long *>(smem_raw + off);
+      if (tid == 0) { mbar_init(bar, 1); }
+      __syncthreads();
+      if (tid == 0)
+      {
+         const int cnt = min(nbz, ne - e0);
+         tma_load_1d(sQ, qd + (long long)e0 * S * Q3, (unsigned)(sizeof(Qd) * cnt * S * Q3), bar);
+      }
+   }
    for (int i = tid; i < Q * D; i += nthr)
    {
       const int q = i % Q, d = i / Q;
@@ -404,7 +486,9 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
       sG[q * D + d] = AR::in(gG[i]);
    }
    diffusion_element<AR, TD, TQ, GATHER, MAXD, MAXQ>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG,
-                                                     bufA, bufB, qd, x, gmap, mask, y, accumulate);
+                                                     bufA, bufB, qd, x, gmap, mask, y, accumulate,
+                                                     1, 1, sQ ? sQ + (size_t)tz * S * Q3 : nullptr,
+                                                     bar);
 }
 
 // R right-hand sides stored interleaved (x[j*R + r], E-vector out

@@ -8,6 +8,7 @@
 #pragma once
 #include "gbpa_apply_kernels.cuh"
 #include "gbpa_dispatch.cuh"
+#include <algorithm>
 
 namespace gbpa
 {
@@ -45,13 +46,24 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
    if (gather_map) { k = diffusion_kernel_for<AR, true, GEN>(D, Q); }
    else if constexpr (PLAIN) { k = diffusion_kernel_for<AR, false, GEN>(D, Q); }
    else { return GBPA_ERR_UNSUPPORTED; }
-   const int nbz = elements_per_block(GBPA_DIFFUSION, prec, D, Q);
-   const size_t smem = sizeof(typename AR::V) *
-                       (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+   // tuned elements per block, clamped to the kernel's register-limited size
+   const int nbz = std::max(1, std::min(elements_per_block(GBPA_DIFFUSION, prec, D, Q),
+                                        max_threads_for(k) / (Q * Q)));
+   size_t smem = sizeof(typename AR::V) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+   // TMA staging of the block's qdata when the arithmetic asks for it and the
+   // copy meets the bulk-copy rules: 16-byte aligned start, size multiple of 16
+   const size_t qbytes = sizeof(typename AR::Qd) * (symm ? 6 : 9) * (size_t)Q * Q * Q;
+   int tma = (AR::kTmaQd && ((uintptr_t)qd % 16 == 0) && (qbytes % 16 == 0)) ? 1 : 0;
+   if (tma)
+   {
+      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 16;
+      if (with <= 200 * 1024) { smem = with; }
+      else { tma = 0; }
+   }
    int acc = accumulate ? 1 : 0;
    void *args[] = {&ne, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd,
                    (void *)&x, (void *)&gather_map, (void *)&ess_mask, &y, &acc,
-                   (void *)&skip};
+                   (void *)&skip, &tma};
    return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
                          args, smem, "diffusion_apply");
 }
@@ -78,14 +90,19 @@ int launch_diffusion_block_ar(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, 
    if (ne == 0) { return GBPA_SUCCESS; }
    const size_t per_slab = sizeof(typename AR::V) * diff_smem_per_elem(D, Q);
    const size_t tables = sizeof(typename AR::V) * 2 * Q * D;
-   if (Q * Q * nrhs > 1024 || tables + nrhs * per_slab > 200 * 1024) { return GBPA_ERR_UNSUPPORTED; }
+   const void *k = diffusion_block_kernel_for<AR>(D, Q);
+   const int max_thr = max_threads_for(k);   // register-limited block size
+   if (Q * Q * nrhs > max_thr || tables + nrhs * per_slab > 200 * 1024) { return GBPA_ERR_UNSUPPORTED; }
+   // elements per block: up to ~256 threads, within the register and
+   // shared-memory limits
    int nbz = 1;
-   while ((nbz + 1) * Q * Q * nrhs <= 1024 && tables + (nbz + 1) * nrhs * per_slab <= 110 * 1024) { ++nbz; }
+   while ((nbz + 1) * Q * Q * nrhs <= std::min(max_thr, 256) &&
+          tables + (nbz + 1) * nrhs * per_slab <= 110 * 1024) { ++nbz; }
    const size_t smem = tables + (size_t)nbz * nrhs * per_slab;
    void *args[] = {&ne, &nrhs, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd, (void *)&x,
                    (void *)&gather_map, (void *)&ess_mask, &y, (void *)&skip};
-   return launch_generic(ctx, diffusion_block_kernel_for<AR>(D, Q), dim3((ne + nbz - 1) / nbz),
-                         dim3(Q, Q, nbz * nrhs), args, smem, "diffusion_apply_block");
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz * nrhs), args, smem,
+                         "diffusion_apply_block");
 }
 
 template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
@@ -101,7 +118,8 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
    if (gather_map) { k = mass_kernel_for<AR, true, GEN>(D, Q); }
    else if constexpr (PLAIN) { k = mass_kernel_for<AR, false, GEN>(D, Q); }
    else { return GBPA_ERR_UNSUPPORTED; }
-   const int nbz = elements_per_block(GBPA_MASS, prec, D, Q);
+   const int nbz = std::max(1, std::min(elements_per_block(GBPA_MASS, prec, D, Q),
+                                        max_threads_for(k) / (Q * Q)));
    const size_t smem = sizeof(typename AR::V) * (Q * D + (size_t)nbz * mass_smem_per_elem(D, Q));
    int acc = accumulate ? 1 : 0;
    void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&qd, (void *)&x,

@@ -59,7 +59,7 @@ int ensure_smem(const void *kernel, size_t bytes)
 }
 
 // Largest block the kernel can launch with (register-limited), cached.
-static int max_threads_for(const void *kernel)
+int max_threads_for(const void *kernel)
 {
    static std::mutex mu;
    static std::unordered_map<const void *, int> cache;

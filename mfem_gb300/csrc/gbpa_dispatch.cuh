@@ -18,4 +18,6 @@ namespace gbpa
 int ensure_smem(const void *kernel, size_t bytes);
 int launch_generic(gbpa_ctx *ctx, const void *kernel, dim3 grid, dim3 block,
                    void **args, size_t smem, const char *what);
+// Largest block size the kernel can be launched with (register-limited).
+int max_threads_for(const void *kernel);
 } // namespace gbpa
