@@ -48,6 +48,11 @@ def parse():
                     help="mesh size of the precision-form PCG comparison (77: ~29.5 M DOFs at p=4)")
     ap.add_argument("--pcg-only", action="store_true", help="run only the precision-form PCG comparison")
     ap.add_argument("--pcg-max-it", type=int, default=20000)
+    ap.add_argument("--batched", action="store_true", help="run only the batching-form comparison")
+    ap.add_argument("--nprob", type=int, default=256)
+    ap.add_argument("--combined", action="store_true", help="run only the combined-form comparison")
+    ap.add_argument("--combined-n", type=int, default=24, help="54: ~19.9 M DOFs at p=5")
+    ap.add_argument("--no-reference", action="store_true", help="combined form: skip the FP64 reference solve")
     return ap.parse_args()
 
 
@@ -56,6 +61,24 @@ def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(ms, world):
+    """Slowest rank's time (the job's time): all_reduce MAX over the process
+    group (NCCL tensors on the GPU, gloo on the CPU)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(ndofs_per_rank, steps, world, ms):
+    """Whole-job GDOF/s: every rank applies its own replica (weak scaling)."""
+    return world * ndofs_per_rank * steps / (ms * 1e-3) / 1e9
 
 
 def algorithmic_bytes(ne, ndofs, D, Q, w, kind, element_only):
@@ -117,6 +140,24 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def profiled_traffic(precision, kind, p, ne):
+    """DRAM bytes per launch of the element kernel from the committed ncu
+    summary of the same kernel on the 24^3 case (profiles/), scaled by the
+    element count (traffic grows with elements: qdata, map and E-vector are
+    per element, the gathered x is ~1 dof per element)."""
+    if kind != "diffusion" or p != 4:
+        return None, None
+    name = {"f64": "f64", "x2": "f64x2", "f32": "f32"}[precision]
+    path = os.path.join(REPO, "profiles", f"diffusion_apply_{name}_p4_n24.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_element:"):
+                return float(line.split(":")[1]) * ne, os.path.relpath(path, REPO)
+    except OSError:
+        pass
+    return None, None
 
 
 def measured_peak_hbm():
@@ -240,11 +281,8 @@ def run_gpu(args):
         barrier()
     ms = e0.elapsed_time(e1)
     launches = dev.launches() - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ndofs * args.steps / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(ms, world)
+    value = job_throughput(ndofs, args.steps, world, ms)
 
     # ---- dominant kernel alone: gather-fused element apply (E-vector out)
     yE = torch.empty(ne * D ** 3, dtype=x.dtype, device="cuda")
@@ -262,6 +300,7 @@ def run_gpu(args):
     kbytes = algorithmic_bytes(ne, ndofs, D, Q, wbytes, args.kind, element_only=True)
     peak, peak_kind = measured_peak_hbm()
     achieved = kbytes / (k_ms * 1e-3) / 1e9
+    traffic, traffic_src = profiled_traffic(args.precision, args.kind, args.p, ne)
 
     # ---- end to end through the C ABI with host buffers (pinned)
     hx = torch.empty(ndofs, dtype=x.dtype).pin_memory()
@@ -279,12 +318,8 @@ def run_gpu(args):
         hy.copy_(y, non_blocking=True)
     t1.record(stream)
     barrier()
-    e2e_ms = t0.elapsed_time(t1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = world * ndofs * args.steps / (e2e_ms * 1e-3) / 1e9
+    e2e_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    e2e = job_throughput(ndofs, args.steps, world, e2e_ms)
 
     extras = {}
     if not args.no_extras and rank == 0 and prec == 0:
@@ -302,8 +337,12 @@ def run_gpu(args):
                    "ne": ne, "ndofs": ndofs, "p": args.p, "q1d": Q, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (qdata %.2f GB); no flush" % (integ.qdata.numel() * 8 / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": f"{args.kind}_apply (gather fused)",
-                     "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind},
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "kernel": f"{args.kind}_apply (gather fused)",
+                     "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind,
+                     "note": ("native FP64 is FP64-pipe bound on GB300 (1.26 TFLOP/s; ncu: FP64 pipe "
+                              "91.5% active); see f64x2_apply for the double-float form")
+                     if prec == 0 else None},
         "e2e": {"value": e2e, "unit": "GDOF/s", "h2d_bytes_per_step": ndofs * wbytes,
                 "d2h_bytes_per_step": ndofs * wbytes},
         "gpu_launches": int(launches),
@@ -430,6 +469,123 @@ def run_pcg_form(n, p, max_it=2000):
     return out
 
 
+def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
+    """Batching form: nprob independent Dirichlet Poisson problems, each a
+    jittered Cartesian hex mesh of n^3 elements with n uniform in [4, 16] and
+    order p uniform in {2,...,6} (splitmix64 stream, seed 5), lognormal kappa
+    and RHS ~ U[0,1] per problem; all solved to 1e-10 in one persistent
+    launch, against solving them one after another with the single-problem
+    device PCG (CUDA-graph captured iterations)."""
+    import torch
+    from mfem_gb300 import _lib, fem
+    from mfem_gb300.pa import (DiffusionIntegrator, Device, FiniteElementSpace,
+                               OperatorJacobiSmoother, PAOperator)
+    dev = Device.get()
+    u = fem.u01_stream(seed, 2 * nprob)
+    probs, descs = [], []
+    total = 0
+    for k in range(nprob):
+        n = 4 + int(u[2 * k] * 13)
+        p = 2 + int(u[2 * k + 1] * 5)
+        mesh = fem.CartesianMesh(n, jitter=0.1, seed=1000 + k)
+        fes = FiniteElementSpace(mesh, p)
+        integ = DiffusionIntegrator("kappa")
+        integ.AssemblePA(fes, modes=fem.kappa_modes(3 + k))
+        ess = fes.GetBoundaryTrueDofs()
+        A = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess)
+        M = OperatorJacobiSmoother(A, ess)
+        b = torch.from_numpy(fem.u01_array(100 + k, fes.ndofs)).cuda()
+        b[torch.from_numpy(ess).long().cuda()] = 0.0
+        e = torch.from_numpy(ess).cuda()
+        x = torch.zeros_like(b)
+        R = fes.GetElementRestriction()
+        probs.append(dict(A=A, dinv=M.dinv, b=b, x=x, ess=e, integ=integ, R=R, n=n, p=p))
+        descs.append(_lib.ProblemDesc(fes.ne, fes.ndofs, integ.D, integ.Q, integ.B.data_ptr(),
+                                      integ.G.data_ptr(), integ.qdata.data_ptr(), R.gather_map.data_ptr(),
+                                      R.offsets.data_ptr(), R.indices.data_ptr(), e.data_ptr(), e.numel(),
+                                      M.dinv.data_ptr(), b.data_ptr(), x.data_ptr()))
+        total += fes.ndofs
+    arr = (_lib.ProblemDesc * nprob)(*descs)
+    its = (ctypes.c_int * nprob)()
+    conv = (ctypes.c_int * nprob)()
+    secs = ctypes.c_double(0)
+    st = dev.lib.gbpa_batched_pcg_solve(dev.ctx, nprob, arr, rel_tol, 0.0, max_it, its, conv, None,
+                                        ctypes.byref(secs))
+    torch.cuda.synchronize()
+    seq = 0.0
+    worst = 0.0
+    info = _lib.SolveInfo()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    for k, pr in enumerate(probs):
+        X = torch.zeros_like(pr["x"])
+        s2 = dev.lib.gbpa_pcg_solve(pr["A"].handle, P(pr["dinv"]), P(pr["b"]), P(X), rel_tol, 0.0, max_it, 0,
+                                    ctypes.byref(info))
+        seq += info.seconds
+        worst = max(worst, float(torch.linalg.norm(pr["x"] - X) / torch.linalg.norm(X)))
+    orders = [pr["p"] for pr in probs]
+    return {"workload": f"{nprob} Dirichlet Poisson problems, n~U[4,16], p~U{{2..6}}, lognormal kappa, "
+                        f"{total} DOFs total", "status": st, "seconds_one_launch": secs.value,
+            "seconds_sequential_pcg": seq, "speedup_vs_sequential": seq / max(secs.value, 1e-30),
+            "converged": int(sum(conv)), "iterations_max": max(its), "iterations_min": min(its),
+            "max_rel_l2_vs_sequential": worst, "dofs_total": total,
+            "problems_per_order": {str(q): orders.count(q) for q in range(2, 7)}}
+
+
+def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
+    """Combined form: unit cube mapped by x -> x + 0.05 sin(2 pi x) sin(2 pi y)
+    sin(2 pi z) per component (order-3 geometry), H1 order p, lognormal kappa,
+    nrhs right-hand sides ~ U[-1,1] solved together: FP32 block PCG inside FP64
+    defect correction to 1e-10 per right-hand side. Reference: FP64 block PCG
+    to 1e-12; per-right-hand-side relative L2 error reported."""
+    import torch
+    from mfem_gb300 import _lib, fem
+    from mfem_gb300.pa import (DiffusionIntegrator, Device, FiniteElementSpace,
+                               OperatorJacobiSmoother, PAOperator)
+    dev = Device.get()
+    mesh = fem.CartesianMesh(n, curved=True)
+    fes = FiniteElementSpace(mesh, p)
+    integ = DiffusionIntegrator("kappa")
+    integ.AssemblePA(fes, modes=fem.kappa_modes(3))
+    ess = fes.GetBoundaryTrueDofs()
+    A64 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess)
+    A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=1)
+    M = OperatorJacobiSmoother(A64, ess)
+    nd = fes.ndofs
+    B = torch.from_numpy(2 * fem.u01_array(6, nd * nrhs) - 1).cuda().view(nd, nrhs)
+    B[torch.from_numpy(ess).long().cuda()] = 0.0
+    B = B.contiguous()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    X = torch.zeros_like(B)
+    info = (_lib.SolveInfo * nrhs)()
+    st = dev.lib.gbpa_pcg_solve_block_mixed(A64.handle, A32.handle, nrhs, P(M.dinv.float()), P(B), P(X),
+                                            1e-10, 1e-5, 30, 20000, info)
+    out = {"workload": f"curved order-3 geometry, n={n}^3, p={p}, q={p + 2}, {nd} DOFs, lognormal kappa, "
+                       f"{nrhs} RHS~U[-1,1]", "status": st, "seconds_block_mixed": info[0].seconds,
+           "outer": [info[r].outer_iterations for r in range(nrhs)],
+           "inner_iterations": [info[r].inner_iterations for r in range(nrhs)],
+           "true_rel_residual": [info[r].true_rel_residual for r in range(nrhs)]}
+    # the same right-hand sides one at a time (single-vector mixed solves)
+    seq = 0.0
+    si = _lib.SolveInfo()
+    for r in range(nrhs):
+        xr = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        b = B[:, r].contiguous()
+        dev.lib.gbpa_pcg_solve_mixed(A64.handle, A32.handle, P(M.dinv.float()), P(b), P(xr), 1e-10, 1e-5,
+                                     30, 20000, ctypes.byref(si))
+        seq += si.seconds
+    out["seconds_sequential_mixed"] = seq
+    out["speedup_block_vs_sequential"] = seq / max(info[0].seconds, 1e-30)
+    if with_reference:
+        X64 = torch.zeros_like(B)
+        i64 = (_lib.SolveInfo * nrhs)()
+        st2 = dev.lib.gbpa_pcg_solve_block(A64.handle, nrhs, P(M.dinv), P(B), P(X64), 1e-12, 0.0, 50000, i64)
+        out["fp64_block_pcg"] = {"status": st2, "seconds": i64[0].seconds,
+                                 "iterations": [i64[r].iterations for r in range(nrhs)]}
+        out["rel_l2_vs_fp64"] = [float(torch.linalg.norm(X[:, r] - X64[:, r]) / torch.linalg.norm(X64[:, r]))
+                                 for r in range(nrhs)]
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -438,6 +594,17 @@ def main():
         from mfem_gb300.pa import Device
         Device("cuda", dist_info()[2])
         print(json.dumps({"pcg": run_pcg_form(args.pcg_n, args.p, args.pcg_max_it)}), flush=True)
+        return 0
+    if args.batched:
+        from mfem_gb300.pa import Device
+        Device("cuda", dist_info()[2])
+        print(json.dumps({"batched": run_batched_form(args.nprob)}), flush=True)
+        return 0
+    if args.combined:
+        from mfem_gb300.pa import Device
+        Device("cuda", dist_info()[2])
+        print(json.dumps({"combined": run_combined_form(args.combined_n, 5, 8, not args.no_reference)}),
+              flush=True)
         return 0
     return run_gpu(args)
 
