@@ -509,9 +509,18 @@ def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
     its = (ctypes.c_int * nprob)()
     conv = (ctypes.c_int * nprob)()
     secs = ctypes.c_double(0)
+    # double-float arithmetic first (its solutions are overwritten by the FP64 run)
+    secs_x2 = ctypes.c_double(0)
+    conv_x2 = (ctypes.c_int * nprob)()
+    st_x2 = dev.lib.gbpa_batched_pcg_solve_precision(dev.ctx, nprob, arr, 2, rel_tol, 0.0, max_it, None,
+                                                     conv_x2, None, ctypes.byref(secs_x2))
+    x2_sols = [pr["x"].clone() for pr in probs]
     st = dev.lib.gbpa_batched_pcg_solve(dev.ctx, nprob, arr, rel_tol, 0.0, max_it, its, conv, None,
                                         ctypes.byref(secs))
     torch.cuda.synchronize()
+    x2_err = max(float(torch.linalg.norm(xs - pr["x"]) / torch.linalg.norm(pr["x"]))
+                 for xs, pr in zip(x2_sols, probs))
+    del x2_sols
     seq = 0.0
     worst = 0.0
     info = _lib.SolveInfo()
@@ -528,6 +537,9 @@ def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
             "seconds_sequential_pcg": seq, "speedup_vs_sequential": seq / max(secs.value, 1e-30),
             "converged": int(sum(conv)), "iterations_max": max(its), "iterations_min": min(its),
             "max_rel_l2_vs_sequential": worst, "dofs_total": total,
+            "f64x2": {"status": st_x2, "seconds_one_launch": secs_x2.value, "converged": int(sum(conv_x2)),
+                      "speedup_vs_sequential_fp64": seq / max(secs_x2.value, 1e-30),
+                      "max_rel_l2_vs_fp64_batched": x2_err},
             "problems_per_order": {str(q): orders.count(q) for q in range(2, 7)}}
 
 

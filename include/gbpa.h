@@ -335,6 +335,15 @@ int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob,
                            double abs_tol, int max_it, int *iterations,
                            int *converged, double *final_norms,
                            double *seconds);
+/* Same, with the element arithmetic chosen: GBPA_F64 (as above) or
+ * GBPA_F64X2 (FP64 data, double-float arithmetic on the FP32 pipes; the
+ * library splits each problem's qdata into its workspace). */
+int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
+                                     const gbpa_problem_desc *probs,
+                                     int precision, double rel_tol,
+                                     double abs_tol, int max_it,
+                                     int *iterations, int *converged,
+                                     double *final_norms, double *seconds);
 
 /* --------------------------------------------------------------- tuning */
 /* Elements per thread block used by the apply kernels for (kind, precision,

@@ -97,6 +97,8 @@ SIGNATURES = {
     "gbpa_pcg_solve_block_mixed": (I, [P, P, I, P, P, P, D, D, I, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_batched_pcg_solve":(I, [P, I, ctypes.POINTER(ProblemDesc), D, D, I, P, P, P,
                                    ctypes.POINTER(D)]),
+    "gbpa_batched_pcg_solve_precision": (I, [P, I, ctypes.POINTER(ProblemDesc), I, D, D, I, P, P, P,
+                                             ctypes.POINTER(D)]),
     "gbpa_set_elements_per_block": (I, [I, I, I, I, I]),
     "gbpa_get_elements_per_block": (I, [I, I, I, I]),
 }

@@ -274,6 +274,12 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    {
       // stage 2 (y) into registers: rA = G_x B_y, rBv = B_x G_y, rC = B_x B_y
       V rA[DM], rBv[DM], rC[DM];
+      V rBy[DM], rGy[DM];   // row qy = ty of B and G, reused for every dz
+#pragma unroll
+      for (int dy = 0; dy < DM; ++dy)
+      {
+         if (dy < D) { rBy[dy] = sB[ty * D + dy]; rGy[dy] = sG[ty * D + dy]; }
+      }
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
@@ -285,7 +291,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             if (dy >= D) { break; }
             const V bx = BX[(dz * D + dy) * Q + tx];
             const V gx = GX[(dz * D + dy) * Q + tx];
-            const V by = sB[ty * D + dy], gy = sG[ty * D + dy];
+            const V by = rBy[dy], gy = rGy[dy];
             AR::mac(a, gx, by);
             AR::mac(b, bx, gy);
             AR::mac(c, bx, by);
@@ -378,6 +384,12 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    V *U0 = bufB, *U12 = bufB + D * D * Q;
    for (int dy = ty; part && dy < D; dy += Q)
    {
+      V cBy[QM], cGy[QM];   // column dy of B and G, reused for every dz
+#pragma unroll
+      for (int qy = 0; qy < QM; ++qy)
+      {
+         if (qy < Q) { cBy[qy] = sB[qy * D + dy]; cGy[qy] = sG[qy * D + dy]; }
+      }
 #pragma unroll
       for (int dz = 0; dz < DM; ++dz)
       {
@@ -387,7 +399,7 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
          for (int qy = 0; qy < QM; ++qy)
          {
             if (qy >= Q) { break; }
-            const V by = sB[qy * D + dy], gy = sG[qy * D + dy];
+            const V by = cBy[qy], gy = cGy[qy];
             const int o = (dz * Q + qy) * Q + tx;
             AR::mac(a, T0[o], by);
             AR::mac(b, T1[o], gy);
@@ -407,6 +419,12 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
       {
          for (int dx = tx; dx < D; dx += Q)
          {
+            V cBx[QM], cGx[QM];   // column dx of B and G, reused for every dz
+#pragma unroll
+            for (int qx = 0; qx < QM; ++qx)
+            {
+               if (qx < Q) { cBx[qx] = sB[qx * D + dx]; cGx[qx] = sG[qx * D + dx]; }
+            }
 #pragma unroll
             for (int dz = 0; dz < DM; ++dz)
             {
@@ -417,8 +435,8 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                {
                   if (qx >= Q) { break; }
                   const int o = (dz * D + dy) * Q + qx;
-                  AR::mac(v, sG[qx * D + dx], U0[o]);
-                  AR::mac(v, sB[qx * D + dx], U12[o]);
+                  AR::mac(v, cGx[qx], U0[o]);
+                  AR::mac(v, cBx[qx], U12[o]);
                }
                const long long k = (base + dx + D * (dy + D * dz)) * ys;
                const typename AR::In r = qok ? AR::out(AR::fin(v)) : (typename AR::In)NAN;
@@ -492,10 +510,11 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
 }
 
 // R right-hand sides stored interleaved (x[j*R + r], E-vector out
-// y[(e*D^3 + k)*R + r]). Block (Q, Q, nbz*R): slab tz handles right-hand side
-// tz % R of element blockIdx.x*nbz + tz / R, so the R slabs of an element sit
-// in one block and HBM delivers its qdata once for all R vectors (the other
-// R-1 reads hit L1).
+// y[(e*D^3 + k)*R + r]). Same layout as the single-vector kernel, block
+// (Q, Q, nbz); each slab applies its element to the R vectors in turn. The
+// block's qdata is staged once in shared memory (TMA bulk copy, when the
+// 16-byte rules hold) and reused for all R vectors, so HBM delivers it once
+// per R applies; otherwise the R passes re-read it through L1/L2.
 template <typename AR, int TD, int TQ>
 __global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d, int q1d,
                                              const typename AR::In *__restrict__ gB,
@@ -505,15 +524,17 @@ __global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d
                                              const int *__restrict__ gmap,
                                              const unsigned char *__restrict__ mask,
                                              typename AR::In *__restrict__ y,
-                                             const int *__restrict__ skip)
+                                             const int *__restrict__ skip, int tma)
 {
    using V = typename AR::V;
+   using Qd = typename AR::Qd;
    if (skip && *skip) { return; }
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
-   const int e = blockIdx.x * (blockDim.z / nrhs) + tz / nrhs;
-   const int r = tz % nrhs;
+   const int nbz = blockDim.z;
+   const int e0 = blockIdx.x * nbz;
+   const int e = e0 + tz;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    V *sB = reinterpret_cast<V *>(smem_raw);
    V *sG = sB + Q * D;
@@ -521,15 +542,40 @@ __global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d
    V *bufA = sG + Q * D + tz * per;
    V *bufB = bufA + (per - 2 * D * D * Q);
    const int tid = tx + Q * (ty + Q * tz);
-   const int nthr = Q * Q * blockDim.z;
+   const int nthr = Q * Q * nbz;
+   const int S = symm ? 6 : 9;
+   const int Q3 = Q * Q * Q;
+   Qd *sQ = nullptr;
+   unsigned long long *bar = nullptr;
+   if (tma)
+   {
+      size_t off = sizeof(V) * (2 * Q * D + (size_t)nbz * per);
+      off = (off + 15) & ~size_t(15);
+      sQ = reinterpret_cast<Qd *>(smem_raw + off);
+      off += sizeof(Qd) * (size_t)nbz * S * Q3;
+      off = (off + 7) & ~size_t(7);
+      bar = reinterpret_cast<unsigned long long *>(smem_raw + off);
+      if (tid == 0) { mbar_init(bar, 1); }
+      __syncthreads();
+      if (tid == 0)
+      {
+         const int cnt = min(nbz, ne - e0);
+         tma_load_1d(sQ, qd + (long long)e0 * S * Q3, (unsigned)(sizeof(Qd) * cnt * S * Q3), bar);
+      }
+   }
    for (int i = tid; i < Q * D; i += nthr)
    {
       const int q = i % Q, d = i / Q;
       sB[q * D + d] = AR::in(gB[i]);
       sG[q * D + d] = AR::in(gG[i]);
    }
-   diffusion_element<AR, TD, TQ, true>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG, bufA, bufB,
-                                       qd, x + r, gmap, mask, y + r, 0, nrhs, nrhs);
+   for (int r = 0; r < nrhs; ++r)
+   {
+      if (r > 0) { __syncthreads(); }   // previous pass done with this slab's buffers
+      diffusion_element<AR, TD, TQ, true>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG, bufA, bufB,
+                                          qd, x + r, gmap, mask, y + r, 0, nrhs, nrhs,
+                                          sQ ? sQ + (size_t)tz * S * Q3 : nullptr, bar);
+   }
 }
 
 template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>

@@ -88,20 +88,24 @@ int launch_diffusion_block_ar(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, 
                               typename AR::In *y, const int *skip)
 {
    if (ne == 0) { return GBPA_SUCCESS; }
-   const size_t per_slab = sizeof(typename AR::V) * diff_smem_per_elem(D, Q);
-   const size_t tables = sizeof(typename AR::V) * 2 * Q * D;
    const void *k = diffusion_block_kernel_for<AR>(D, Q);
    const int max_thr = max_threads_for(k);   // register-limited block size
-   if (Q * Q * nrhs > max_thr || tables + nrhs * per_slab > 200 * 1024) { return GBPA_ERR_UNSUPPORTED; }
-   // elements per block: up to ~256 threads, within the register and
-   // shared-memory limits
-   int nbz = 1;
-   while ((nbz + 1) * Q * Q * nrhs <= std::min(max_thr, 256) &&
-          tables + (nbz + 1) * nrhs * per_slab <= 110 * 1024) { ++nbz; }
-   const size_t smem = tables + (size_t)nbz * nrhs * per_slab;
+   if (Q * Q > max_thr) { return GBPA_ERR_UNSUPPORTED; }
+   const int prec = sizeof(typename AR::V) == 4 ? GBPA_F32 : GBPA_F64;
+   const int nbz = std::max(1, std::min(elements_per_block(GBPA_DIFFUSION, prec, D, Q), max_thr / (Q * Q)));
+   size_t smem = sizeof(typename AR::V) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+   // qdata staged once per block for all right-hand sides (TMA rules permitting)
+   const size_t qbytes = sizeof(typename AR::Qd) * (symm ? 6 : 9) * (size_t)Q * Q * Q;
+   int tma = ((uintptr_t)qd % 16 == 0 && qbytes % 16 == 0) ? 1 : 0;
+   if (tma)
+   {
+      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 16;
+      if (with <= 200 * 1024) { smem = with; }
+      else { tma = 0; }
+   }
    void *args[] = {&ne, &nrhs, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd, (void *)&x,
-                   (void *)&gather_map, (void *)&ess_mask, &y, (void *)&skip};
-   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz * nrhs), args, smem,
+                   (void *)&gather_map, (void *)&ess_mask, &y, (void *)&skip, &tma};
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz), args, smem,
                          "diffusion_apply_block");
 }
 

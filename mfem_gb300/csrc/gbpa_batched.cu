@@ -38,6 +38,7 @@ struct BProb
 {
    int ne, ndofs, D, Q, nbz;
    const double *B, *G, *qd, *dinv, *b;
+   const float2 *qd2;   // qdata split into (hi, lo) floats for the double-float arithmetic
    double *x;
    const int *gmap, *off, *ind;
    const unsigned char *mask;
@@ -141,11 +142,28 @@ __device__ double problem_sum(const BParams &P, const BProb &pr)
    return s;
 }
 
+// One batch's element apply: runtime-size code bounded by p <= 6 (a single
+// variant keeps the persistent kernel free of register spills; per-order
+// compile-time variants in one kernel spilled heavily).
+template <typename AR>
+__device__ __forceinline__ void batched_element(int D, int Q, long long e, bool active, bool part,
+                                                int tx, int ty, const typename AR::V *sB,
+                                                const typename AR::V *sG, typename AR::V *bufA,
+                                                typename AR::V *bufB, const typename AR::Qd *qd,
+                                                const double *d, const int *gmap,
+                                                const unsigned char *mask, double *yE)
+{
+   diffusion_element<AR, 0, 0, true, BATCH_MAXD, BATCH_MAXQ, true>(
+      e, active, part, D, Q, tx, ty, 1, sB, sG, bufA, bufB, qd, d, gmap, mask, yE, 0);
+}
+
+template <typename AR>
 __global__ void __launch_bounds__(BATCH_THREADS)
 batched_pcg_kernel(BParams P)
 {
+   using V = typename AR::V;
    extern __shared__ __align__(16) unsigned char smem_raw[];
-   double *sm = reinterpret_cast<double *>(smem_raw);
+   V *sm = reinterpret_cast<V *>(smem_raw);
    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
    const int gthreads = gridDim.x * blockDim.x;
    volatile BScal *S = P.scal;
@@ -201,21 +219,23 @@ batched_pcg_kernel(BParams P)
          const BProb &pr = P.probs[bt.prob];
          const int D = pr.D, Q = pr.Q;
          __syncthreads();                         // previous batch done with smem
-         double *sB = sm, *sG = sm + Q * D;
+         V *sB = sm, *sG = sm + Q * D;
          for (int i = threadIdx.x; i < Q * D; i += blockDim.x)
          {
-            sB[(i % Q) * D + i / Q] = pr.B[i];
-            sG[(i % Q) * D + i / Q] = pr.G[i];
+            sB[(i % Q) * D + i / Q] = AR::in(pr.B[i]);
+            sG[(i % Q) * D + i / Q] = AR::in(pr.G[i]);
          }
          const int t = threadIdx.x;
          const int tz = t / (Q * Q), tx = t % Q, ty = (t / Q) % Q;
          const bool part = tz < pr.nbz;
          const int per = diff_smem_per_elem(D, Q);
-         double *bufA = sm + 2 * Q * D + (part ? tz : 0) * per;
-         double *bufB = bufA + (per - 2 * D * D * Q);
-         diffusion_element<ArF64, 0, 0, true, BATCH_MAXD, BATCH_MAXQ, true>(
-            (long long)bt.e0 + tz, part && tz < bt.count, part, D, Q, tx, ty, 1, sB, sG, bufA,
-            bufB, pr.qd, pr.d, pr.gmap, pr.mask, pr.yE, 0);
+         V *bufA = sm + 2 * Q * D + (part ? tz : 0) * per;
+         V *bufB = bufA + (per - 2 * D * D * Q);
+         const typename AR::Qd *qd;
+         if constexpr (sizeof(typename AR::Qd) == sizeof(float2)) { qd = (const typename AR::Qd *)pr.qd2; }
+         else { qd = (const typename AR::Qd *)pr.qd; }
+         batched_element<AR>(D, Q, (long long)bt.e0 + tz, part && tz < bt.count, part, tx, ty, sB, sG,
+                             bufA, bufB, qd, pr.d, pr.gmap, pr.mask, pr.yE);
       }
       if (!grid_barrier(P)) { return; }
       // ---- S: z = R^T yE (z[ess] = d[ess]); partial (d, z). yE comes from
@@ -335,10 +355,13 @@ __global__ void batched_mask_kernel(int n, const int *ess, unsigned char *mask, 
 
 using namespace gbpa;
 
-extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
-                                      double rel_tol, double abs_tol, int max_it, int *iterations,
-                                      int *converged, double *final_norms, double *seconds)
+extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
+                                                const gbpa_problem_desc *probs, int precision,
+                                                double rel_tol, double abs_tol, int max_it,
+                                                int *iterations, int *converged,
+                                                double *final_norms, double *seconds)
 {
+   if (precision != GBPA_F64 && precision != GBPA_F64X2) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (!ctx || nprob < 0 || (nprob > 0 && !probs) || max_it < 0 || rel_tol < 0 || abs_tol < 0)
    {
       return GBPA_ERR_INVALID_ARGUMENT;
@@ -371,6 +394,7 @@ extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_prob
       for (int i0 = 0; i0 < d.ndofs; i0 += CHUNK) { chunks.push_back({k, i0, std::min(d.ndofs, i0 + CHUNK)}); }
       p.nchunk = (int)chunks.size() - p.chunk0;
       ws_doubles += 3 * (size_t)d.ndofs + (size_t)d.ne * D * D * D;
+      if (precision == GBPA_F64X2) { ws_doubles += (size_t)d.ne * 6 * Q * Q * Q; }   // split qdata
       if (d.n_ess > 0) { mask_bytes += (size_t)d.ndofs; }
       const size_t sm = sizeof(double) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
       smem_max = std::max(smem_max, sm);
@@ -400,6 +424,15 @@ extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_prob
       const gbpa_problem_desc &d = probs[k];
       p.r = ws; p.d = ws + d.ndofs; p.z = ws + 2 * (size_t)d.ndofs; p.yE = ws + 3 * (size_t)d.ndofs;
       ws += 3 * (size_t)d.ndofs + (size_t)d.ne * d.d1d * d.d1d * d.d1d;
+      p.qd2 = nullptr;
+      if (precision == GBPA_F64X2)
+      {
+         const int64_t nq = (int64_t)d.ne * 6 * d.q1d * d.q1d * d.q1d;
+         p.qd2 = (const float2 *)ws;
+         rc = launch_split_x2(ctx, nq, d.qdata, (float2 *)ws);
+         if (rc) { return rc; }
+         ws += nq;
+      }
       p.mask = nullptr;
       if (d.n_ess > 0)
       {
@@ -440,12 +473,12 @@ extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_prob
    P.abort = (int *)(sync + 2);
    P.spin_limit = 1LL << 26;   // ~2 s of 32 ns sleeps
 
-   const void *kfn = (const void *)batched_pcg_kernel;
+   const void *kfn = precision == GBPA_F64X2 ? (const void *)batched_pcg_kernel<ArX2>
+                                             : (const void *)batched_pcg_kernel<ArF64>;
    rc = ensure_smem(kfn, smem_max);
    if (rc) { return rc; }
    int per_sm = 0;
-   rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_pcg_kernel,
-                                                                 BATCH_THREADS, smem_max),
+   rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BATCH_THREADS, smem_max),
                    "occupancy");
    if (rc) { return rc; }
    if (per_sm < 1) { return GBPA_ERR_UNSUPPORTED; }
@@ -480,4 +513,12 @@ extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_prob
    if (flags & GBPA_FLAG_TIMEOUT) { return GBPA_ERR_TIMEOUT; }
    if (flags & GBPA_FLAG_NOT_FINITE) { return GBPA_ERR_NOT_FINITE; }
    return GBPA_SUCCESS;
+}
+
+extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
+                                      double rel_tol, double abs_tol, int max_it, int *iterations,
+                                      int *converged, double *final_norms, double *seconds)
+{
+   return gbpa_batched_pcg_solve_precision(ctx, nprob, probs, GBPA_F64, rel_tol, abs_tol, max_it,
+                                           iterations, converged, final_norms, seconds);
 }

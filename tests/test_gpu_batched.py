@@ -100,3 +100,25 @@ def test_batched_rejects_unsupported_order():
     arr = (_lib.ProblemDesc * 1)(desc(pr))
     st = d.lib.gbpa_batched_pcg_solve(d.ctx, 1, arr, 1e-10, 0.0, 100, None, None, None, None)
     assert st == -2
+
+
+def test_batched_double_float_matches_single_solves():
+    """GBPA_F64X2 arithmetic in the persistent batched solve reaches the same
+    solutions as the single-problem FP64 PCG (1e-10)."""
+    from mfem_gb300 import _lib
+    from tests.gpu_util import dev
+    d = dev()
+    specs = [(3, 2, None), (4, 4, "kappa"), (2, 6, "kappa")]
+    probs = [make_problem(n, p, c, s) for s, (n, p, c) in enumerate(specs)]
+    arr = (_lib.ProblemDesc * len(probs))(*[desc(pr) for pr in probs])
+    conv = (ctypes.c_int * len(probs))()
+    st = d.lib.gbpa_batched_pcg_solve_precision(d.ctx, len(probs), arr, 2, 1e-10, 0.0, 1000, None, conv,
+                                                None, None)
+    assert st == 0 and all(conv[k] == 1 for k in range(len(probs)))
+    for pr in probs:
+        X = torch.zeros_like(pr["x"])
+        info = _lib.SolveInfo()
+        assert d.lib.gbpa_pcg_solve(pr["A"].handle, ctypes.c_void_p(pr["dinv"].data_ptr()),
+                                    ctypes.c_void_p(pr["b"].data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                    1e-10, 0.0, 1000, 0, ctypes.byref(info)) == 0
+        assert float(torch.linalg.norm(pr["x"] - X) / torch.linalg.norm(X)) < 1e-9
