@@ -158,6 +158,30 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
    return false;
 }
 
+// Stage the qdata of elements [e0, e0 + cnt) (eb bytes each) into `tile` with
+// one bulk copy of the enclosing 16-byte-aligned byte range of the array (the
+// extra bytes on either side belong to neighbouring elements of the same
+// array), completing on `bar`. Returns element e0's qdata inside the tile, or
+// nullptr when the rounded range would end past the array (then the block
+// reads global memory). The array base must be 16-byte aligned (the host
+// checks). Called by every thread of the block; the decision is uniform.
+template <typename Qd>
+__device__ __forceinline__ Qd *stage_qdata(unsigned char *tile, unsigned long long *bar,
+                                           const Qd *qd, int ne, int e0, int cnt, size_t eb,
+                                           int tid)
+{
+   const size_t b0 = (size_t)e0 * eb, b1 = (size_t)(e0 + cnt) * eb, total = (size_t)ne * eb;
+   const size_t a0 = b0 & ~size_t(15), a1 = (b1 + 15) & ~size_t(15);
+   if (a1 > total) { return nullptr; }
+   if (tid == 0) { mbar_init(bar, 1); }
+   __syncthreads();
+   if (tid == 0)
+   {
+      tma_load_1d(tile, reinterpret_cast<const unsigned char *>(qd) + a0, (unsigned)(a1 - a0), bar);
+   }
+   return reinterpret_cast<Qd *>(tile + (b0 - a0));
+}
+
 template <typename AR, bool COH = false>
 __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__restrict__ x,
                                                        const int *__restrict__ gmap,
@@ -483,19 +507,14 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
    unsigned long long *bar = nullptr;
    if (AR::kTmaQd && tma)
    {
+      const size_t eb = sizeof(Qd) * (size_t)S * Q3;
       size_t off = sizeof(V) * (2 * Q * D + (size_t)nbz * per);
       off = (off + 15) & ~size_t(15);
-      sQ = reinterpret_cast<Qd *>(smem_raw + off);
-      off += sizeof(Qd) * (size_t)nbz * S * Q3;
+      unsigned char *tile = smem_raw + off;
+      off += eb * nbz + 32;
       off = (off + 7) & ~size_t(7);
       bar = reinterpret_cast<unsigned long long *>(smem_raw + off);
-      if (tid == 0) { mbar_init(bar, 1); }
-      __syncthreads();
-      if (tid == 0)
-      {
-         const int cnt = min(nbz, ne - e0);
-         tma_load_1d(sQ, qd + (long long)e0 * S * Q3, (unsigned)(sizeof(Qd) * cnt * S * Q3), bar);
-      }
+      sQ = stage_qdata<Qd>(tile, bar, qd, ne, e0, min(nbz, ne - e0), eb, tid);
    }
    for (int i = tid; i < Q * D; i += nthr)
    {
@@ -549,19 +568,14 @@ __global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d
    unsigned long long *bar = nullptr;
    if (tma)
    {
+      const size_t eb = sizeof(Qd) * (size_t)S * Q3;
       size_t off = sizeof(V) * (2 * Q * D + (size_t)nbz * per);
       off = (off + 15) & ~size_t(15);
-      sQ = reinterpret_cast<Qd *>(smem_raw + off);
-      off += sizeof(Qd) * (size_t)nbz * S * Q3;
+      unsigned char *tile = smem_raw + off;
+      off += eb * nbz + 32;
       off = (off + 7) & ~size_t(7);
       bar = reinterpret_cast<unsigned long long *>(smem_raw + off);
-      if (tid == 0) { mbar_init(bar, 1); }
-      __syncthreads();
-      if (tid == 0)
-      {
-         const int cnt = min(nbz, ne - e0);
-         tma_load_1d(sQ, qd + (long long)e0 * S * Q3, (unsigned)(sizeof(Qd) * cnt * S * Q3), bar);
-      }
+      sQ = stage_qdata<Qd>(tile, bar, qd, ne, e0, min(nbz, ne - e0), eb, tid);
    }
    for (int i = tid; i < Q * D; i += nthr)
    {

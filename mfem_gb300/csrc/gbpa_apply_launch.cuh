@@ -50,13 +50,14 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
    const int nbz = std::max(1, std::min(elements_per_block(GBPA_DIFFUSION, prec, D, Q),
                                         max_threads_for(k) / (Q * Q)));
    size_t smem = sizeof(typename AR::V) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
-   // TMA staging of the block's qdata when the arithmetic asks for it and the
-   // copy meets the bulk-copy rules: 16-byte aligned start, size multiple of 16
+   // TMA staging of the block's qdata when the arithmetic asks for it; the
+   // kernel copies the enclosing 16-byte-aligned range, so only the array base
+   // has to be 16-byte aligned (tile + 32 bytes of rounding slack + barrier)
    const size_t qbytes = sizeof(typename AR::Qd) * (symm ? 6 : 9) * (size_t)Q * Q * Q;
-   int tma = (AR::kTmaQd && ((uintptr_t)qd % 16 == 0) && (qbytes % 16 == 0)) ? 1 : 0;
+   int tma = (AR::kTmaQd && ((uintptr_t)qd % 16 == 0)) ? 1 : 0;
    if (tma)
    {
-      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 16;
+      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 48;
       if (with <= 200 * 1024) { smem = with; }
       else { tma = 0; }
    }
@@ -94,12 +95,12 @@ int launch_diffusion_block_ar(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, 
    const int prec = sizeof(typename AR::V) == 4 ? GBPA_F32 : GBPA_F64;
    const int nbz = std::max(1, std::min(elements_per_block(GBPA_DIFFUSION, prec, D, Q), max_thr / (Q * Q)));
    size_t smem = sizeof(typename AR::V) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
-   // qdata staged once per block for all right-hand sides (TMA rules permitting)
+   // qdata staged once per block for all right-hand sides (16-byte aligned base)
    const size_t qbytes = sizeof(typename AR::Qd) * (symm ? 6 : 9) * (size_t)Q * Q * Q;
-   int tma = ((uintptr_t)qd % 16 == 0 && qbytes % 16 == 0) ? 1 : 0;
+   int tma = ((uintptr_t)qd % 16 == 0) ? 1 : 0;
    if (tma)
    {
-      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 16;
+      const size_t with = ((smem + 15) & ~size_t(15)) + nbz * qbytes + 48;
       if (with <= 200 * 1024) { smem = with; }
       else { tma = 0; }
    }

@@ -24,6 +24,7 @@
 #include "gbpa_dispatch.cuh"
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace gbpa
@@ -232,8 +233,10 @@ batched_pcg_kernel(BParams P)
          V *bufA = sm + 2 * Q * D + (part ? tz : 0) * per;
          V *bufB = bufA + (per - 2 * D * D * Q);
          const typename AR::Qd *qd;
-         if constexpr (sizeof(typename AR::Qd) == sizeof(float2)) { qd = (const typename AR::Qd *)pr.qd2; }
-         else { qd = (const typename AR::Qd *)pr.qd; }
+         // the split (hi, lo) copy for the double-float arithmetic, the FP64
+         // qdata otherwise (select by type: both element types are 8 bytes)
+         if constexpr (std::is_same<typename AR::Qd, float2>::value) { qd = pr.qd2; }
+         else { qd = pr.qd; }
          batched_element<AR>(D, Q, (long long)bt.e0 + tz, part && tz < bt.count, part, tx, ty, sB, sG,
                              bufA, bufB, qd, pr.d, pr.gmap, pr.mask, pr.yE);
       }
