@@ -317,8 +317,11 @@ int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
 /* Batching form: many independent Dirichlet problems of uneven size and
  * order, solved together. Each problem owns its maps, qdata and vectors
  * (device pointers inside the descriptor array, which is itself host
- * memory). All problems advance in the same persistent launches; a per-
- * problem converged mask stops finished problems. FP64. */
+ * memory). All problems advance in lockstep; a per-problem converged mask
+ * stops finished problems. Each problem follows CGSolver::Mult with
+ * OperatorJacobiSmoother (linalg/solvers.cpp:869-1050) on its
+ * ConstrainedOperator-wrapped PA diffusion operator; no single reference
+ * entry point solves several problems at once. FP64. */
 typedef struct gbpa_problem_desc
 {
    int ne, ndofs, d1d, q1d;
@@ -344,6 +347,24 @@ int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
                                      double abs_tol, int max_it,
                                      int *iterations, int *converged,
                                      double *final_norms, double *seconds);
+
+/* How the batched iterations are scheduled on the GPU.
+ *  GBPA_BATCH_GRAPH       each PCG iteration is a few launches that cover
+ *                         all active problems (one grouped element-apply
+ *                         launch per order, with that order's compile-time
+ *                         kernel, then the vector phases), K iterations
+ *                         captured in a CUDA graph; the work tables are
+ *                         compacted as problems converge. Orders up to
+ *                         d1d, q1d <= 10. The default.
+ *  GBPA_BATCH_PERSISTENT  one cooperative persistent launch for the whole
+ *                         solve, grid-wide barriers between the phases and
+ *                         one runtime-size element kernel (p <= 6). */
+enum gbpa_batch_schedule { GBPA_BATCH_GRAPH = 0, GBPA_BATCH_PERSISTENT = 1 };
+int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
+                              const gbpa_problem_desc *probs, int precision,
+                              int schedule, double rel_tol, double abs_tol,
+                              int max_it, int *iterations, int *converged,
+                              double *final_norms, double *seconds);
 
 /* --------------------------------------------------------------- tuning */
 /* Elements per thread block used by the apply kernels for (kind, precision,

@@ -17,6 +17,7 @@ D = ctypes.c_double
 GBPA_DIFFUSION, GBPA_MASS = 0, 1
 GBPA_F64, GBPA_F32, GBPA_F64X2 = 0, 1, 2
 GBPA_SCATTER_CSR, GBPA_SCATTER_ATOMIC = 0, 1
+GBPA_BATCH_GRAPH, GBPA_BATCH_PERSISTENT = 0, 1
 
 STATUS = {
     0: "success", -1: "invalid argument", -2: "unsupported", -3: "CUDA error",
@@ -99,6 +100,8 @@ SIGNATURES = {
                                    ctypes.POINTER(D)]),
     "gbpa_batched_pcg_solve_precision": (I, [P, I, ctypes.POINTER(ProblemDesc), I, D, D, I, P, P, P,
                                              ctypes.POINTER(D)]),
+    "gbpa_batched_pcg_solve_ex": (I, [P, I, ctypes.POINTER(ProblemDesc), I, I, D, D, I, P, P, P,
+                                      ctypes.POINTER(D)]),
     "gbpa_set_elements_per_block": (I, [I, I, I, I, I]),
     "gbpa_get_elements_per_block": (I, [I, I, I, I]),
 }

@@ -471,25 +471,27 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    }
 }
 
-template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
-__global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
-                                       const typename AR::In *__restrict__ gB,
-                                       const typename AR::In *__restrict__ gG,
-                                       const typename AR::Qd *__restrict__ qd,
-                                       const typename AR::In *__restrict__ x,
-                                       const int *__restrict__ gmap,
-                                       const unsigned char *__restrict__ mask,
-                                       typename AR::In *__restrict__ y, int accumulate,
-                                       const int *__restrict__ skip, int tma)
+// One block's share of the diffusion apply: elements [e0, e0 + cnt) of an
+// operator with ne elements (cnt <= blockDim.z), in the 2D-slab layout
+// (Q, Q, nbz). Shared by the single-operator kernel and the batched kernel
+// that maps blocks onto (problem, first element) pairs.
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD, int MAXQ>
+__device__ __forceinline__ void diffusion_apply_slab(int ne, int e0, int cnt, int symm, int d1d,
+                                                     int q1d, const typename AR::In *__restrict__ gB,
+                                                     const typename AR::In *__restrict__ gG,
+                                                     const typename AR::Qd *__restrict__ qd,
+                                                     const typename AR::In *__restrict__ x,
+                                                     const int *__restrict__ gmap,
+                                                     const unsigned char *__restrict__ mask,
+                                                     typename AR::In *__restrict__ y, int accumulate,
+                                                     int tma)
 {
    using V = typename AR::V;
    using Qd = typename AR::Qd;
-   if (skip && *skip) { return; }   // uniform per launch: solver finished
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
    const int nbz = blockDim.z;
-   const int e0 = blockIdx.x * nbz;
    const int e = e0 + tz;
 
    extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -514,7 +516,7 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
       off += eb * nbz + 32;
       off = (off + 7) & ~size_t(7);
       bar = reinterpret_cast<unsigned long long *>(smem_raw + off);
-      sQ = stage_qdata<Qd>(tile, bar, qd, ne, e0, min(nbz, ne - e0), eb, tid);
+      sQ = stage_qdata<Qd>(tile, bar, qd, ne, e0, cnt, eb, tid);
    }
    for (int i = tid; i < Q * D; i += nthr)
    {
@@ -522,10 +524,28 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
       sB[q * D + d] = AR::in(gB[i]);
       sG[q * D + d] = AR::in(gG[i]);
    }
-   diffusion_element<AR, TD, TQ, GATHER, MAXD, MAXQ>(e, e < ne, true, D, Q, tx, ty, symm, sB, sG,
+   diffusion_element<AR, TD, TQ, GATHER, MAXD, MAXQ>(e, tz < cnt, true, D, Q, tx, ty, symm, sB, sG,
                                                      bufA, bufB, qd, x, gmap, mask, y, accumulate,
                                                      1, 1, sQ ? sQ + (size_t)tz * S * Q3 : nullptr,
                                                      bar);
+}
+
+template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
+__global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
+                                       const typename AR::In *__restrict__ gB,
+                                       const typename AR::In *__restrict__ gG,
+                                       const typename AR::Qd *__restrict__ qd,
+                                       const typename AR::In *__restrict__ x,
+                                       const int *__restrict__ gmap,
+                                       const unsigned char *__restrict__ mask,
+                                       typename AR::In *__restrict__ y, int accumulate,
+                                       const int *__restrict__ skip, int tma)
+{
+   if (skip && *skip) { return; }   // uniform per launch: solver finished
+   const int e0 = blockIdx.x * blockDim.z;
+   diffusion_apply_slab<AR, TD, TQ, GATHER, MAXD, MAXQ>(ne, e0, min((int)blockDim.z, ne - e0), symm,
+                                                        d1d, q1d, gB, gG, qd, x, gmap, mask, y,
+                                                        accumulate, tma);
 }
 
 // R right-hand sides stored interleaved (x[j*R + r], E-vector out

@@ -1,26 +1,38 @@
 // Batched PCG (batching form): many independent Dirichlet Poisson problems of
-// uneven size and order solved together in ONE persistent cooperative launch.
-// Each problem follows CGSolver::Mult with OperatorJacobiSmoother
-// (linalg/solvers.cpp:869-1050, 427-452) on its ConstrainedOperator-wrapped
-// PA diffusion operator (linalg/operator.cpp:601-661,
-// fem/bilinearform_ext.cpp:487-564); a converged problem drops out of the work
-// tables while the others continue.
+// uneven size and order solved together. Each problem follows CGSolver::Mult
+// with OperatorJacobiSmoother (linalg/solvers.cpp:869-1050, 427-452) on its
+// ConstrainedOperator-wrapped PA diffusion operator
+// (linalg/operator.cpp:601-661, fem/bilinearform_ext.cpp:487-564); a converged
+// problem drops out of the work while the others continue.
 //
 // Work decomposition (built on the host once per call):
 //   element batches  (problem, first element, count): one block processes a
 //                    batch with the 2D-slab layout (Q, Q, nbz) of that
-//                    problem's order, nbz chosen per Q (tuning table)
+//                    problem's order, nbz chosen per order (tuning table)
 //   dof chunks       (problem, first dof, last dof): vector phases and the CSR
 //                    scatter; each chunk writes one partial sum
 // Per-problem dots sum their chunks' partials in chunk order, so results do
 // not depend on the grid size or on scheduling.
 //
-// The grid barrier is a generation counter with a bounded spin: a barrier that
-// does not complete within the spin budget raises GBPA_FLAG_TIMEOUT and every
-// block leaves the solve loop, so the kernel always terminates. The launch is
-// cooperative, so all blocks are co-resident and the barrier completes in
-// normal operation.
+// Two schedules run the same iteration:
+//   graph       per iteration one grouped apply launch per order (that
+//               order's compile-time kernel) and three vector-phase launches
+//               over the active problems' chunks; the block that completes a
+//               problem's partials finishes its scalars (last-block-done).
+//               K iterations are captured in a CUDA graph; the host polls the
+//               per-problem state between graph launches and rebuilds the
+//               tables (and the graph) once the active elements have shrunk
+//               enough, so converged problems stop costing blocks.
+//   persistent  one cooperative launch for the whole solve with grid-wide
+//               barriers between the phases and one runtime-size element
+//               kernel. The grid barrier is a generation counter with a
+//               bounded spin: a barrier that does not complete within the
+//               spin budget raises GBPA_FLAG_TIMEOUT and every block leaves
+//               the solve loop, so the kernel always terminates. The launch is
+//               cooperative, so all blocks are co-resident and the barrier
+//               completes in normal operation.
 #include "gbpa_apply_kernels.cuh"
+#include "gbpa_batched.cuh"
 #include "gbpa_dispatch.cuh"
 #include <algorithm>
 #include <cmath>
@@ -29,33 +41,26 @@
 
 namespace gbpa
 {
-constexpr int BATCH_THREADS = 256;
-constexpr int BATCH_MAXD = 7;    // p <= 6
+constexpr int BATCH_MAXD = 7;    // persistent schedule: p <= 6
 constexpr int BATCH_MAXQ = 8;
-constexpr int CHUNK = 2048;
-constexpr int GBPA_FLAG_TIMEOUT = 16;
 
-struct BProb
+int batched_apply_nbz_f64(int D, int Q);
+int batched_apply_nbz_x2(int D, int Q);
+int launch_batched_apply_f64(gbpa_ctx *ctx, int D, int Q, int nbz, const BBatch *batches, int nbatch,
+                             const BProb *probs, const BScal *scal);
+int launch_batched_apply_x2(gbpa_ctx *ctx, int D, int Q, int nbz, const BBatch *batches, int nbatch,
+                            const BProb *probs, const BScal *scal);
+
+int batched_apply_nbz(int precision, int D, int Q)
 {
-   int ne, ndofs, D, Q, nbz;
-   const double *B, *G, *qd, *dinv, *b;
-   const float2 *qd2;   // qdata split into (hi, lo) floats for the double-float arithmetic
-   double *x;
-   const int *gmap, *off, *ind;
-   const unsigned char *mask;
-   double *r, *d, *z, *yE;
-   int chunk0, nchunk;
-};
-// Per-problem solver scalars. They are written by one thread and read by all
-// blocks across grid barriers, so every access goes through a volatile
-// pointer (L2, never a stale L1 line).
-struct BScal
+   return precision == GBPA_F64X2 ? batched_apply_nbz_x2(D, Q) : batched_apply_nbz_f64(D, Q);
+}
+int launch_batched_apply(gbpa_ctx *ctx, int precision, int D, int Q, int nbz, const BBatch *batches,
+                         int nbatch, const BProb *probs, const BScal *scal)
 {
-   double nom, nom0, den, betanom, alpha, beta, r0;
-   int iter, done, converged, final_iter;
-};
-struct BBatch { int prob, e0, count; };
-struct BChunk { int prob, i0, i1; };
+   return precision == GBPA_F64X2 ? launch_batched_apply_x2(ctx, D, Q, nbz, batches, nbatch, probs, scal)
+                                  : launch_batched_apply_f64(ctx, D, Q, nbz, batches, nbatch, probs, scal);
+}
 
 struct BParams
 {
@@ -354,24 +359,359 @@ __global__ void batched_mask_kernel(int n, const int *ess, unsigned char *mask, 
    }
 }
 
+// ------------------------------------------------------------ graph schedule
+struct GParams
+{
+   const BProb *probs;
+   BScal *scal;
+   const BChunk *chunks;
+   double *partials;
+   unsigned int *cnt;   // per problem: chunks of the current phase published
+   double rel2, abs2;
+   int max_it;
+   int *flags;
+};
+
+// Publishes a chunk's partial (thread 0 holds the block sum) and returns, in
+// thread 0, whether this block completed its problem's set of partials. Then
+// (thread 0 only) problem_total sums them in chunk order and re-arms the
+// counter for the next phase.
+__device__ __forceinline__ bool chunk_publish(const GParams &P, const BChunk &ch, int nchunk, double s)
+{
+   bool last = false;
+   if (threadIdx.x == 0)
+   {
+      P.partials[ch.slot] = s;
+      __threadfence();
+      last = atomicAdd(P.cnt + ch.prob, 1u) == (unsigned)(nchunk - 1);
+   }
+   return last;
+}
+__device__ __forceinline__ double problem_total(const GParams &P, const BProb &pr, int prob)
+{
+   __threadfence();
+   double s = 0.0;
+   for (int c = 0; c < pr.nchunk; ++c) { s += __ldcg(P.partials + pr.chunk0 + c); }
+   P.cnt[prob] = 0;
+   return s;
+}
+
+// r = b, x = 0, z = dinv r, d = z; nom = (z, r), stopping threshold
+__global__ void __launch_bounds__(BATCH_THREADS) bg_init_kernel(GParams P)
+{
+   const BChunk ch = P.chunks[blockIdx.x];
+   const BProb &pr = P.probs[ch.prob];
+   double s = 0.0;
+   for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+   {
+      const double ri = pr.b[i];
+      pr.x[i] = 0.0;
+      pr.r[i] = ri;
+      const double zi = pr.dinv[i] * ri;
+      pr.z[i] = zi;
+      pr.d[i] = zi;
+      s += zi * ri;
+   }
+   s = bblock_sum(s);
+   if (chunk_publish(P, ch, pr.nchunk, s))
+   {
+      BScal &sc = P.scal[ch.prob];
+      const double nom = problem_total(P, pr, ch.prob);
+      sc.nom = nom; sc.nom0 = nom; sc.betanom = nom;
+      sc.iter = 1; sc.converged = 0; sc.final_iter = 0;
+      int done = 0;
+      if (!isfinite(nom)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); done = 1; }
+      else if (nom < 0.0) { done = 1; }
+      else
+      {
+         sc.r0 = fmax(nom * P.rel2, P.abs2);
+         if (nom <= sc.r0) { sc.converged = 1; done = 1; }
+      }
+      sc.done = done;
+   }
+}
+
+// z = R^T yE (z[ess] = d[ess]); den = (d, z); alpha = nom / den
+__global__ void __launch_bounds__(BATCH_THREADS) bg_scatter_den_kernel(GParams P)
+{
+   const BChunk ch = P.chunks[blockIdx.x];
+   if (P.scal[ch.prob].done) { return; }
+   const BProb &pr = P.probs[ch.prob];
+   double s = 0.0;
+   for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+   {
+      double v;
+      if (pr.mask && pr.mask[i]) { v = pr.d[i]; }
+      else
+      {
+         v = 0.0;
+         for (int j = pr.off[i]; j < pr.off[i + 1]; ++j)
+         {
+            const int sj = pr.ind[j];
+            const double a = pr.yE[sj >= 0 ? sj : -1 - sj];
+            v += sj >= 0 ? a : -a;
+         }
+      }
+      pr.z[i] = v;
+      s += pr.d[i] * v;
+   }
+   s = bblock_sum(s);
+   if (chunk_publish(P, ch, pr.nchunk, s))
+   {
+      BScal &sc = P.scal[ch.prob];
+      const double den = problem_total(P, pr, ch.prob);
+      sc.den = den;
+      if (!isfinite(den)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); sc.final_iter = sc.iter; sc.done = 1; }
+      else if (den == 0.0) { sc.final_iter = sc.iter; sc.done = 1; }
+      else { sc.alpha = sc.nom / den; }
+   }
+}
+
+// x += alpha d; r -= alpha z; z = dinv r; betanom = (r, z); convergence; beta
+__global__ void __launch_bounds__(BATCH_THREADS) bg_update_kernel(GParams P)
+{
+   const BChunk ch = P.chunks[blockIdx.x];
+   if (P.scal[ch.prob].done) { return; }
+   const BProb &pr = P.probs[ch.prob];
+   const double alpha = P.scal[ch.prob].alpha;
+   double s = 0.0;
+   for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+   {
+      pr.x[i] += alpha * pr.d[i];
+      const double ri = pr.r[i] - alpha * pr.z[i];
+      pr.r[i] = ri;
+      const double zi = pr.dinv[i] * ri;
+      pr.z[i] = zi;
+      s += ri * zi;
+   }
+   s = bblock_sum(s);
+   if (chunk_publish(P, ch, pr.nchunk, s))
+   {
+      BScal &sc = P.scal[ch.prob];
+      const double bn = problem_total(P, pr, ch.prob);
+      sc.betanom = bn;
+      int done = 0;
+      if (!isfinite(bn)) { atomicOr(P.flags, GBPA_FLAG_NOT_FINITE); sc.final_iter = sc.iter; done = 1; }
+      else if (bn < 0.0) { sc.final_iter = sc.iter; done = 1; }
+      else if (bn <= sc.r0) { sc.converged = 1; sc.final_iter = sc.iter; done = 1; }
+      else
+      {
+         const int iter = sc.iter + 1;
+         sc.iter = iter;
+         if (iter > P.max_it) { sc.final_iter = P.max_it; done = 1; }
+         else
+         {
+            sc.beta = bn / sc.nom;
+            sc.nom = bn;
+         }
+      }
+      sc.done = done;
+   }
+}
+
+// d = z + beta d
+__global__ void __launch_bounds__(BATCH_THREADS) bg_direction_kernel(GParams P)
+{
+   const BChunk ch = P.chunks[blockIdx.x];
+   if (P.scal[ch.prob].done) { return; }
+   const BProb &pr = P.probs[ch.prob];
+   const double beta = P.scal[ch.prob].beta;
+   for (int i = ch.i0 + threadIdx.x; i < ch.i1; i += blockDim.x)
+   {
+      pr.d[i] = pr.z[i] + beta * pr.d[i];
+   }
+}
+
 } // namespace gbpa
 
-using namespace gbpa;
+namespace gbpa
+{
+namespace
+{
+struct Group { int D, Q, nbz; };
 
-extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
-                                                const gbpa_problem_desc *probs, int precision,
-                                                double rel_tol, double abs_tol, int max_it,
-                                                int *iterations, int *converged,
-                                                double *final_norms, double *seconds)
+// The graph schedule's tables for the problems with active[k] set: element
+// batches grouped by order (group g owns batches [gofs[g], gofs[g+1])) and
+// the problems' dof chunks (each keeps its slot in the full chunk list).
+void graph_tables(const std::vector<BProb> &hp, const std::vector<Group> &groups,
+                  const std::vector<int> &grp_of, const std::vector<char> &active,
+                  std::vector<BBatch> &batches, std::vector<int> &gofs, std::vector<BChunk> &chunks)
+{
+   batches.clear();
+   chunks.clear();
+   gofs.assign(groups.size() + 1, 0);
+   for (size_t g = 0; g < groups.size(); ++g)
+   {
+      gofs[g] = (int)batches.size();
+      const int nbz = groups[g].nbz;
+      for (size_t k = 0; k < hp.size(); ++k)
+      {
+         if (!active[k] || grp_of[k] != (int)g) { continue; }
+         for (int e0 = 0; e0 < hp[k].ne; e0 += nbz)
+         {
+            batches.push_back({(int)k, e0, std::min(nbz, hp[k].ne - e0)});
+         }
+      }
+   }
+   gofs[groups.size()] = (int)batches.size();
+   for (size_t k = 0; k < hp.size(); ++k)
+   {
+      if (!active[k]) { continue; }
+      for (int c = 0; c < hp[k].nchunk; ++c)
+      {
+         const int i0 = c * CHUNK;
+         chunks.push_back({(int)k, i0, std::min(hp[k].ndofs, i0 + CHUNK), hp[k].chunk0 + c});
+      }
+   }
+}
+
+int check_every()
+{
+   const char *s = getenv("GBPA_PCG_CHECK_EVERY");
+   const int k = s ? atoi(s) : 10;
+   return k >= 1 && k <= 1000 ? k : 10;
+}
+
+// Runs the graph schedule from the uploaded tables to the end of the solve.
+int run_graph_schedule(gbpa_ctx *ctx, int precision, const std::vector<BProb> &hp,
+                       const std::vector<Group> &groups, const std::vector<int> &grp_of, GParams G,
+                       BProb *d_probs, BBatch *d_batch, BChunk *d_chunk, int nchunk_all, int max_it,
+                       std::vector<BScal> &hs, float *ms)
+{
+   const int nprob = (int)hp.size();
+   int rc = GBPA_SUCCESS;
+   if (!ctx->capture_stream)
+   {
+      rc = check_cuda(cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking),
+                      "cudaStreamCreate(capture)");
+      if (rc) { return rc; }
+   }
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   if (nchunk_all > 0)
+   {
+      bg_init_kernel<<<nchunk_all, BATCH_THREADS, 0, ctx->stream>>>(G);
+      rc = last_launch(ctx, "batched_init");
+   }
+   const int K = check_every();
+   cudaGraphExec_t exec = nullptr;
+   int64_t table_elems = 0;
+   int per_iter = 0;
+   long long launched = 0;
+   std::vector<BBatch> tb;
+   std::vector<BChunk> tc;
+   std::vector<int> gofs;
+   std::vector<char> active(nprob, 0);
+   while (!rc)
+   {
+      rc = check_cuda(cudaMemcpyAsync(hs.data(), G.scal, sizeof(BScal) * nprob, cudaMemcpyDeviceToHost,
+                                      ctx->stream), "cudaMemcpyAsync(state)");
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize"); }
+      if (rc) { break; }
+      int64_t act_elems = 0;
+      int nact = 0;
+      for (int k = 0; k < nprob; ++k)
+      {
+         active[k] = hs[k].done ? 0 : 1;
+         if (active[k]) { ++nact; act_elems += hp[k].ne; }
+      }
+      if (nact == 0) { break; }
+      if (launched > (long long)max_it + K) { break; }   // safety net; the device caps iterations
+      // (re)build the tables and the graph when the active elements have
+      // fallen to 60% of those the current graph launches blocks for
+      if (!exec || act_elems * 10 <= table_elems * 6)
+      {
+         graph_tables(hp, groups, grp_of, active, tb, gofs, tc);
+         if (!tb.empty())
+         {
+            rc = check_cuda(cudaMemcpyAsync(d_batch, tb.data(), sizeof(BBatch) * tb.size(),
+                                            cudaMemcpyHostToDevice, ctx->stream), "copy");
+         }
+         if (!rc && !tc.empty())
+         {
+            rc = check_cuda(cudaMemcpyAsync(d_chunk, tc.data(), sizeof(BChunk) * tc.size(),
+                                            cudaMemcpyHostToDevice, ctx->stream), "copy");
+         }
+         if (rc) { break; }
+         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+         // capture on the private stream (the context's stream may be the
+         // legacy default stream, which cannot be captured); captured
+         // launches are not counted, executed ones are (below)
+         const int64_t launches0 = ctx->launches;
+         cudaGraph_t g = nullptr;
+         cudaStream_t saved = ctx->stream;
+         rc = check_cuda(cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal),
+                         "cudaStreamBeginCapture");
+         if (rc) { break; }
+         ctx->stream = ctx->capture_stream;
+         const unsigned nc = (unsigned)tc.size();
+         per_iter = 3;
+         for (size_t gi = 0; gi < groups.size(); ++gi) { per_iter += gofs[gi + 1] > gofs[gi] ? 1 : 0; }
+         for (int it = 0; it < K && !rc; ++it)
+         {
+            for (size_t gi = 0; gi < groups.size() && !rc; ++gi)
+            {
+               const int cnt = gofs[gi + 1] - gofs[gi];
+               if (cnt == 0) { continue; }
+               rc = launch_batched_apply(ctx, precision, groups[gi].D, groups[gi].Q, groups[gi].nbz,
+                                         d_batch + gofs[gi], cnt, d_probs, G.scal);
+            }
+            if (rc) { break; }
+            bg_scatter_den_kernel<<<nc, BATCH_THREADS, 0, ctx->stream>>>(G);
+            rc = last_launch(ctx, "batched_scatter_den");
+            if (rc) { break; }
+            bg_update_kernel<<<nc, BATCH_THREADS, 0, ctx->stream>>>(G);
+            rc = last_launch(ctx, "batched_update");
+            if (rc) { break; }
+            bg_direction_kernel<<<nc, BATCH_THREADS, 0, ctx->stream>>>(G);
+            rc = last_launch(ctx, "batched_direction");
+         }
+         ctx->stream = saved;
+         ctx->launches = launches0;
+         const int rc2 = check_cuda(cudaStreamEndCapture(ctx->capture_stream, &g), "cudaStreamEndCapture");
+         if (rc || rc2)
+         {
+            if (g) { cudaGraphDestroy(g); }
+            if (!rc) { rc = rc2; }
+            break;
+         }
+         rc = check_cuda(cudaGraphInstantiate(&exec, g, 0), "cudaGraphInstantiate");
+         cudaGraphDestroy(g);
+         if (rc) { break; }
+         table_elems = act_elems;
+      }
+      rc = check_cuda(cudaGraphLaunch(exec, ctx->stream), "cudaGraphLaunch");
+      ctx->launches += (int64_t)K * per_iter;
+      launched += K;
+   }
+   cudaEventRecord(e1, ctx->stream);
+   cudaEventSynchronize(e1);
+   float t = 0.f;
+   cudaEventElapsedTime(&t, e0, e1);
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   if (exec) { cudaGraphExecDestroy(exec); }
+   if (ms) { *ms = t; }
+   return rc;
+}
+} // namespace
+
+static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *probs, int precision,
+                         int schedule, double rel_tol, double abs_tol, int max_it, int *iterations,
+                         int *converged, double *final_norms, double *seconds)
 {
    if (precision != GBPA_F64 && precision != GBPA_F64X2) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (schedule != GBPA_BATCH_GRAPH && schedule != GBPA_BATCH_PERSISTENT) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (!ctx || nprob < 0 || (nprob > 0 && !probs) || max_it < 0 || rel_tol < 0 || abs_tol < 0)
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
    if (nprob == 0) { return GBPA_SUCCESS; }
+   const bool graph = schedule == GBPA_BATCH_GRAPH;
    // ---- host tables
    std::vector<BProb> hp(nprob);
+   std::vector<Group> groups;
+   std::vector<int> grp_of(nprob, 0);
    std::vector<BBatch> batches;
    std::vector<BChunk> chunks;
    size_t ws_doubles = 0, mask_bytes = 0;
@@ -380,27 +720,53 @@ extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
    {
       const gbpa_problem_desc &d = probs[k];
       if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0) { return GBPA_ERR_INVALID_ARGUMENT; }
-      if (d.d1d < 1 || d.q1d < 1 || d.d1d > BATCH_MAXD || d.q1d > BATCH_MAXQ) { return GBPA_ERR_UNSUPPORTED; }
+      if (d.d1d < 1 || d.q1d < 1) { return GBPA_ERR_UNSUPPORTED; }
+      if (!graph && (d.d1d > BATCH_MAXD || d.q1d > BATCH_MAXQ)) { return GBPA_ERR_UNSUPPORTED; }
       if (d.ne > 0 && (!d.B || !d.G || !d.qdata || !d.gather_map || !d.offsets || !d.indices)) { return GBPA_ERR_INVALID_ARGUMENT; }
       if (d.ndofs > 0 && (!d.dinv || !d.b || !d.x)) { return GBPA_ERR_INVALID_ARGUMENT; }
       if (d.n_ess > 0 && !d.ess) { return GBPA_ERR_INVALID_ARGUMENT; }
       const int Q = d.q1d, D = d.d1d;
-      int nbz = std::min(elements_per_block(GBPA_DIFFUSION, GBPA_F64, D, Q), BATCH_THREADS / (Q * Q));
-      if (nbz < 1) { nbz = 1; }
+      int nbz = 0;
+      if (graph)
+      {
+         size_t g = 0;
+         while (g < groups.size() && !(groups[g].D == D && groups[g].Q == Q)) { ++g; }
+         if (g == groups.size())
+         {
+            const int nb = batched_apply_nbz(precision, D, Q);
+            if (nb < 1) { return GBPA_ERR_UNSUPPORTED; }
+            groups.push_back({D, Q, nb});
+         }
+         grp_of[k] = (int)g;
+         nbz = groups[g].nbz;
+      }
+      else
+      {
+         nbz = std::max(1, std::min(elements_per_block(GBPA_DIFFUSION, GBPA_F64, D, Q), BATCH_THREADS / (Q * Q)));
+         for (int e0 = 0; e0 < d.ne; e0 += nbz) { batches.push_back({k, e0, std::min(nbz, d.ne - e0)}); }
+         const size_t sm = sizeof(double) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
+         smem_max = std::max(smem_max, sm);
+      }
       BProb &p = hp[k];
       p = BProb{};
       p.ne = d.ne; p.ndofs = d.ndofs; p.D = D; p.Q = Q; p.nbz = nbz;
       p.B = d.B; p.G = d.G; p.qd = d.qdata; p.dinv = d.dinv; p.b = d.b; p.x = d.x;
       p.gmap = d.gather_map; p.off = d.offsets; p.ind = d.indices;
-      for (int e0 = 0; e0 < d.ne; e0 += nbz) { batches.push_back({k, e0, std::min(nbz, d.ne - e0)}); }
       p.chunk0 = (int)chunks.size();
-      for (int i0 = 0; i0 < d.ndofs; i0 += CHUNK) { chunks.push_back({k, i0, std::min(d.ndofs, i0 + CHUNK)}); }
+      for (int i0 = 0; i0 < d.ndofs; i0 += CHUNK)
+      {
+         chunks.push_back({k, i0, std::min(d.ndofs, i0 + CHUNK), (int)chunks.size()});
+      }
       p.nchunk = (int)chunks.size() - p.chunk0;
       ws_doubles += 3 * (size_t)d.ndofs + (size_t)d.ne * D * D * D;
       if (precision == GBPA_F64X2) { ws_doubles += (size_t)d.ne * 6 * Q * Q * Q; }   // split qdata
       if (d.n_ess > 0) { mask_bytes += (size_t)d.ndofs; }
-      const size_t sm = sizeof(double) * (2 * Q * D + (size_t)nbz * diff_smem_per_elem(D, Q));
-      smem_max = std::max(smem_max, sm);
+   }
+   std::vector<int> gofs;
+   if (graph)
+   {
+      const std::vector<char> all(nprob, 1);
+      graph_tables(hp, groups, grp_of, all, batches, gofs, chunks);
    }
    // ---- device workspace: one allocation for everything
    const size_t nb = batches.size(), nc = chunks.size();
@@ -412,6 +778,7 @@ extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
    const size_t o_chunk = take(sizeof(BChunk) * (nc ? nc : 1));
    const size_t o_part = take(sizeof(double) * (nc ? nc : 1));
    const size_t o_sync = take(sizeof(unsigned int) * 64);
+   const size_t o_cnt = take(sizeof(unsigned int) * nprob);
    const size_t o_ws = take(sizeof(double) * ws_doubles);
    const size_t o_mask = take(mask_bytes ? mask_bytes : 1);
    unsigned char *base = (unsigned char *)scratch(ctx, SLOT_BATCH, off);
@@ -419,6 +786,7 @@ extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
    double *ws = (double *)(base + o_ws);
    unsigned char *mk = base + o_mask;
    int rc = check_cuda(cudaMemsetAsync(base + o_sync, 0, sizeof(unsigned int) * 64, ctx->stream), "memset");
+   if (!rc) { rc = check_cuda(cudaMemsetAsync(base + o_cnt, 0, sizeof(unsigned int) * nprob, ctx->stream), "memset"); }
    if (!rc && mask_bytes) { rc = check_cuda(cudaMemsetAsync(mk, 0, mask_bytes, ctx->stream), "memset"); }
    if (rc) { return rc; }
    for (int k = 0; k < nprob; ++k)
@@ -447,63 +815,91 @@ extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
          mk += d.ndofs;
       }
    }
+   // initial solver state: problems without dofs are converged at iteration 0
+   // (the other entries are set by the solve's first phase)
+   std::vector<BScal> hs(nprob);
+   for (int k = 0; k < nprob; ++k)
+   {
+      hs[k] = BScal{};
+      if (hp[k].ndofs == 0) { hs[k].converged = 1; hs[k].done = 1; }
+   }
    rc = check_cuda(cudaMemcpyAsync(base + o_probs, hp.data(), sizeof(BProb) * nprob, cudaMemcpyHostToDevice, ctx->stream), "copy");
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(base + o_scal, hs.data(), sizeof(BScal) * nprob, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
    if (!rc && nb) { rc = check_cuda(cudaMemcpyAsync(base + o_batch, batches.data(), sizeof(BBatch) * nb, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
    if (!rc && nc) { rc = check_cuda(cudaMemcpyAsync(base + o_chunk, chunks.data(), sizeof(BChunk) * nc, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
    if (rc) { return rc; }
    int flags0 = 0;
-   rc = gbpa_get_error_flags(ctx, &flags0);   // syncs: host tables may go out of scope after
+   rc = gbpa_get_error_flags(ctx, &flags0);   // syncs: host tables may change after
    if (rc) { return rc; }
    if (flags0 & GBPA_FLAG_INDEX) { return GBPA_ERR_INDEX; }
 
-   BParams P;
-   P.probs = (const BProb *)(base + o_probs);
-   P.scal = (BScal *)(base + o_scal);
-   P.nprob = nprob;
-   P.batches = (const BBatch *)(base + o_batch);
-   P.nbatch = (int)nb;
-   P.chunks = (const BChunk *)(base + o_chunk);
-   P.nchunk = (int)nc;
-   P.partials = (double *)(base + o_part);
-   P.rel2 = rel_tol * rel_tol;
-   P.abs2 = abs_tol * abs_tol;
-   P.max_it = max_it;
-   unsigned int *sync = (unsigned int *)(base + o_sync);
-   P.bar_count = sync;
-   P.bar_gen = sync + 32;
-   P.flags = ctx->d_flags;
-   P.n_active = (int *)(sync + 1);
-   P.abort = (int *)(sync + 2);
-   P.spin_limit = 1LL << 26;   // ~2 s of 32 ns sleeps
-
-   const void *kfn = precision == GBPA_F64X2 ? (const void *)batched_pcg_kernel<ArX2>
-                                             : (const void *)batched_pcg_kernel<ArF64>;
-   rc = ensure_smem(kfn, smem_max);
-   if (rc) { return rc; }
-   int per_sm = 0;
-   rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BATCH_THREADS, smem_max),
-                   "occupancy");
-   if (rc) { return rc; }
-   if (per_sm < 1) { return GBPA_ERR_UNSUPPORTED; }
-   const int grid = per_sm * ctx->num_sms;
-   void *args[] = {&P};
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
-   rc = check_cuda(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(BATCH_THREADS), args, smem_max,
-                                               ctx->stream), "cudaLaunchCooperativeKernel");
-   ctx->launches++;
-   cudaEventRecord(e1, ctx->stream);
-   if (!rc) { rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize"); }
    float ms = 0.f;
-   if (!rc) { cudaEventElapsedTime(&ms, e0, e1); }
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
-   if (rc) { return rc; }
+   if (graph)
+   {
+      GParams G;
+      G.probs = (const BProb *)(base + o_probs);
+      G.scal = (BScal *)(base + o_scal);
+      G.chunks = (const BChunk *)(base + o_chunk);
+      G.partials = (double *)(base + o_part);
+      G.cnt = (unsigned int *)(base + o_cnt);
+      G.rel2 = rel_tol * rel_tol;
+      G.abs2 = abs_tol * abs_tol;
+      G.max_it = max_it;
+      G.flags = ctx->d_flags;
+      rc = run_graph_schedule(ctx, precision, hp, groups, grp_of, G, (BProb *)(base + o_probs),
+                              (BBatch *)(base + o_batch), (BChunk *)(base + o_chunk), (int)nc, max_it, hs,
+                              &ms);
+      if (rc) { return rc; }
+   }
+   else
+   {
+      BParams P;
+      P.probs = (const BProb *)(base + o_probs);
+      P.scal = (BScal *)(base + o_scal);
+      P.nprob = nprob;
+      P.batches = (const BBatch *)(base + o_batch);
+      P.nbatch = (int)nb;
+      P.chunks = (const BChunk *)(base + o_chunk);
+      P.nchunk = (int)nc;
+      P.partials = (double *)(base + o_part);
+      P.rel2 = rel_tol * rel_tol;
+      P.abs2 = abs_tol * abs_tol;
+      P.max_it = max_it;
+      unsigned int *sync = (unsigned int *)(base + o_sync);
+      P.bar_count = sync;
+      P.bar_gen = sync + 32;
+      P.flags = ctx->d_flags;
+      P.n_active = (int *)(sync + 1);
+      P.abort = (int *)(sync + 2);
+      P.spin_limit = 1LL << 26;   // ~2 s of 32 ns sleeps
+
+      const void *kfn = precision == GBPA_F64X2 ? (const void *)batched_pcg_kernel<ArX2>
+                                                : (const void *)batched_pcg_kernel<ArF64>;
+      rc = ensure_smem(kfn, smem_max);
+      if (rc) { return rc; }
+      int per_sm = 0;
+      rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, BATCH_THREADS, smem_max),
+                      "occupancy");
+      if (rc) { return rc; }
+      if (per_sm < 1) { return GBPA_ERR_UNSUPPORTED; }
+      const int grid = per_sm * ctx->num_sms;
+      void *args[] = {&P};
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0); cudaEventCreate(&e1);
+      cudaEventRecord(e0, ctx->stream);
+      rc = check_cuda(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(BATCH_THREADS), args, smem_max,
+                                                  ctx->stream), "cudaLaunchCooperativeKernel");
+      ctx->launches++;
+      cudaEventRecord(e1, ctx->stream);
+      if (!rc) { rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize"); }
+      if (!rc) { cudaEventElapsedTime(&ms, e0, e1); }
+      cudaEventDestroy(e0); cudaEventDestroy(e1);
+      if (rc) { return rc; }
+      rc = check_cuda(cudaMemcpy(hs.data(), base + o_scal, sizeof(BScal) * nprob, cudaMemcpyDeviceToHost),
+                      "copy back");
+      if (rc) { return rc; }
+   }
    if (seconds) { *seconds = ms * 1e-3; }
-   std::vector<BScal> hs(nprob);
-   rc = check_cuda(cudaMemcpy(hs.data(), base + o_scal, sizeof(BScal) * nprob, cudaMemcpyDeviceToHost),
-                   "copy back");
-   if (rc) { return rc; }
    int flags = 0;
    rc = gbpa_get_error_flags(ctx, &flags);
    if (rc) { return rc; }
@@ -517,11 +913,33 @@ extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
    if (flags & GBPA_FLAG_NOT_FINITE) { return GBPA_ERR_NOT_FINITE; }
    return GBPA_SUCCESS;
 }
+} // namespace gbpa
+
+using namespace gbpa;
+
+extern "C" int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
+                                         int precision, int schedule, double rel_tol, double abs_tol,
+                                         int max_it, int *iterations, int *converged, double *final_norms,
+                                         double *seconds)
+{
+   return batched_solve(ctx, nprob, probs, precision, schedule, rel_tol, abs_tol, max_it, iterations,
+                        converged, final_norms, seconds);
+}
+
+extern "C" int gbpa_batched_pcg_solve_precision(gbpa_ctx_t ctx, int nprob,
+                                                const gbpa_problem_desc *probs, int precision,
+                                                double rel_tol, double abs_tol, int max_it,
+                                                int *iterations, int *converged,
+                                                double *final_norms, double *seconds)
+{
+   return batched_solve(ctx, nprob, probs, precision, GBPA_BATCH_GRAPH, rel_tol, abs_tol, max_it,
+                        iterations, converged, final_norms, seconds);
+}
 
 extern "C" int gbpa_batched_pcg_solve(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
                                       double rel_tol, double abs_tol, int max_it, int *iterations,
                                       int *converged, double *final_norms, double *seconds)
 {
-   return gbpa_batched_pcg_solve_precision(ctx, nprob, probs, GBPA_F64, rel_tol, abs_tol, max_it,
-                                           iterations, converged, final_norms, seconds);
+   return batched_solve(ctx, nprob, probs, GBPA_F64, GBPA_BATCH_GRAPH, rel_tol, abs_tol, max_it,
+                        iterations, converged, final_norms, seconds);
 }

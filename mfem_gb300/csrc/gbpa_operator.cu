@@ -512,12 +512,14 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
       }
       cudaGraph_t g = nullptr;
       cudaStream_t saved = ctx->stream;
+      const int64_t launches0 = ctx->launches;   // captured launches are counted when they run
       rc = check_cuda(cudaStreamBeginCapture(ctx->capture_stream, cudaStreamCaptureModeThreadLocal),
                       "cudaStreamBeginCapture");
       if (rc) { return rc; }
       ctx->stream = ctx->capture_stream;
       for (int k = 0; k < K && !rc; ++k) { rc = pcg_iteration<T>(op, x, dinv, grid); }
       ctx->stream = saved;
+      ctx->launches = launches0;
       const int rc2 = check_cuda(cudaStreamEndCapture(ctx->capture_stream, &g), "cudaStreamEndCapture");
       if (rc || rc2)
       {
