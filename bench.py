@@ -451,7 +451,10 @@ def run_pcg_form(n, p, max_it=2000):
     del Xx2
     A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=1)
     d32 = M.dinv.float()
-    for name, outer in (("mixed_f32_in_f64", A64), ("mixed_f32_in_f64x2", Ax2)):
+    # the true residual of the defect correction uses the native FP64 operator:
+    # the double-float operator's ~1e-14 error, amplified by the condition
+    # number, stalls that residual near 2e-10 on this problem
+    for name, outer in (("mixed_f32_in_f64", A64),):
         Xm = torch.zeros_like(b)
         st = dev.lib.gbpa_pcg_solve_mixed(outer.handle, A32.handle, P(d32), P(b), P(Xm), 1e-10, 1e-5,
                                           30, max_it, ctypes.byref(info))
@@ -460,10 +463,6 @@ def run_pcg_form(n, p, max_it=2000):
                      "true_rel_residual": info.true_rel_residual,
                      "rel_l2_vs_fp64": float(torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64))}
     t64 = out["fp64_pcg"]["seconds"]
-    # the precision form proper: FP32 apply inside FP64 defect correction whose
-    # true residual uses the native FP64 operator (the double-float outer
-    # operator's ~1e-14 error, amplified by the condition number, can stall the
-    # true residual above 1e-10 on ill-conditioned problems; reported beside)
     out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
     out["speedup_mixed_vs_f64x2_pcg"] = out["f64x2_pcg"]["seconds"] / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
     return out

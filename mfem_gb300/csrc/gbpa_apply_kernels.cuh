@@ -189,6 +189,7 @@ __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__
                                                        long long slot, int xs = 1)
 {
    const int g = __ldg(gmap + slot);
+   if (g == GBPA_GATHER_SKIP) { return AR::zero(); }   // pre-masked map: constrained dof
    const int j = g >= 0 ? g : -1 - g;
    if (mask && __ldg(mask + j)) { return AR::zero(); }
    const typename AR::In *p = x + (long long)j * xs;

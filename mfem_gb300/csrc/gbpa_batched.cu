@@ -243,7 +243,7 @@ batched_pcg_kernel(BParams P)
          if constexpr (std::is_same<typename AR::Qd, float2>::value) { qd = pr.qd2; }
          else { qd = pr.qd; }
          batched_element<AR>(D, Q, (long long)bt.e0 + tz, part && tz < bt.count, part, tx, ty, sB, sG,
-                             bufA, bufB, qd, pr.d, pr.gmap, pr.mask, pr.yE);
+                             bufA, bufB, qd, pr.d, pr.gmap, nullptr, pr.yE);
       }
       if (!grid_barrier(P)) { return; }
       // ---- S: z = R^T yE (z[ess] = d[ess]); partial (d, z). yE comes from
@@ -714,13 +714,14 @@ static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *prob
    std::vector<int> grp_of(nprob, 0);
    std::vector<BBatch> batches;
    std::vector<BChunk> chunks;
-   size_t ws_doubles = 0, mask_bytes = 0;
+   size_t ws_doubles = 0, mask_bytes = 0, gm_ints = 0;
    size_t smem_max = 0;
    for (int k = 0; k < nprob; ++k)
    {
       const gbpa_problem_desc &d = probs[k];
       if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0) { return GBPA_ERR_INVALID_ARGUMENT; }
       if (d.d1d < 1 || d.q1d < 1) { return GBPA_ERR_UNSUPPORTED; }
+      if (d.n_ess > 0) { gm_ints += (size_t)d.ne * d.d1d * d.d1d * d.d1d; }
       if (!graph && (d.d1d > BATCH_MAXD || d.q1d > BATCH_MAXQ)) { return GBPA_ERR_UNSUPPORTED; }
       if (d.ne > 0 && (!d.B || !d.G || !d.qdata || !d.gather_map || !d.offsets || !d.indices)) { return GBPA_ERR_INVALID_ARGUMENT; }
       if (d.ndofs > 0 && (!d.dinv || !d.b || !d.x)) { return GBPA_ERR_INVALID_ARGUMENT; }
@@ -781,10 +782,12 @@ static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *prob
    const size_t o_cnt = take(sizeof(unsigned int) * nprob);
    const size_t o_ws = take(sizeof(double) * ws_doubles);
    const size_t o_mask = take(mask_bytes ? mask_bytes : 1);
+   const size_t o_gm = take(sizeof(int) * (gm_ints ? gm_ints : 1));
    unsigned char *base = (unsigned char *)scratch(ctx, SLOT_BATCH, off);
    if (!base) { return GBPA_ERR_OUT_OF_MEMORY; }
    double *ws = (double *)(base + o_ws);
    unsigned char *mk = base + o_mask;
+   int *gm = (int *)(base + o_gm);
    int rc = check_cuda(cudaMemsetAsync(base + o_sync, 0, sizeof(unsigned int) * 64, ctx->stream), "memset");
    if (!rc) { rc = check_cuda(cudaMemsetAsync(base + o_cnt, 0, sizeof(unsigned int) * nprob, ctx->stream), "memset"); }
    if (!rc && mask_bytes) { rc = check_cuda(cudaMemsetAsync(mk, 0, mask_bytes, ctx->stream), "memset"); }
@@ -813,6 +816,12 @@ static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *prob
          if (rc) { return rc; }
          p.mask = mk;
          mk += d.ndofs;
+         // the element gather reads the pre-masked map (no mask lookup)
+         const int64_t nE = (int64_t)d.ne * d.d1d * d.d1d * d.d1d;
+         rc = launch_masked_gather_map(ctx, nE, d.gather_map, p.mask, gm);
+         if (rc) { return rc; }
+         p.gmap = gm;
+         gm += nE;
       }
    }
    // initial solver state: problems without dofs are converged at iteration 0

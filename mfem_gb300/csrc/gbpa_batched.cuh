@@ -17,8 +17,8 @@ struct BProb
    const double *B, *G, *qd, *dinv, *b;
    const float2 *qd2;   // qdata split into (hi, lo) floats for the double-float arithmetic
    double *x;
-   const int *gmap, *off, *ind;
-   const unsigned char *mask;
+   const int *gmap, *off, *ind;          // gmap: pre-masked (GBPA_GATHER_SKIP on ess slots) when mask is set
+   const unsigned char *mask;           // ess mask (scatter), or null
    double *r, *d, *z, *yE;
    int chunk0, nchunk;
 };

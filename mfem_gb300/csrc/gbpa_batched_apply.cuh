@@ -27,7 +27,7 @@ __global__ void batched_apply_kernel(const BBatch *__restrict__ batches, const B
    if constexpr (std::is_same<typename AR::Qd, float2>::value) { qd = pr.qd2; }
    else { qd = pr.qd; }
    diffusion_apply_slab<AR, TD, TQ, true, MAXD, MAXQ>(pr.ne, bt.e0, bt.count, 1, pr.D, pr.Q, pr.B, pr.G, qd,
-                                                      pr.d, pr.gmap, pr.mask, pr.yE, 0, tma);
+                                                      pr.d, pr.gmap, nullptr, pr.yE, 0, tma);
 }
 
 // Compile-time kernels for p = 1..6 with the default rule Q = D + 1, the

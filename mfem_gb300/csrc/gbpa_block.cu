@@ -309,14 +309,14 @@ static int block_apply_evec(gbpa_operator *op, int R, const T *x, const int *ski
    {
       return launch_diffusion_block_f32(op->ctx, d.ne, R, d.symm ? 1 : 0, d.d1d, d.q1d,
                                         (const float *)d.B, (const float *)d.G,
-                                        (const float *)d.qdata, x, d.gather_map, op->mask,
+                                        (const float *)d.qdata, x, op->gather(), op->gather_mask(),
                                         (float *)op->yEb, skip);
    }
    else
    {
       return launch_diffusion_block_f64(op->ctx, d.ne, R, d.symm ? 1 : 0, d.d1d, d.q1d,
                                         (const double *)d.B, (const double *)d.G,
-                                        (const double *)d.qdata, x, d.gather_map, op->mask,
+                                        (const double *)d.qdata, x, op->gather(), op->gather_mask(),
                                         (double *)op->yEb, skip);
    }
 }

@@ -149,6 +149,27 @@ __global__ void gather_kernel(int64_t n, int nd, int vdim, int byvdim,
    }
 }
 
+__global__ void masked_gather_map_kernel(int64_t n, const int *__restrict__ gmap,
+                                         const unsigned char *__restrict__ mask, int *__restrict__ out)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int g = gmap[i];
+      const int j = g >= 0 ? g : -1 - g;
+      out[i] = mask[j] ? GBPA_GATHER_SKIP : g;
+   }
+}
+
+int launch_masked_gather_map(gbpa_ctx *ctx, int64_t n, const int *gather_map, const unsigned char *mask,
+                             int *out)
+{
+   if (n <= 0) { return GBPA_SUCCESS; }
+   masked_gather_map_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, gather_map, mask,
+                                                                                        out);
+   return last_launch(ctx, "masked_gather_map");
+}
+
 template <typename T>
 __global__ void csr_scatter_kernel(int ndofs, const int *__restrict__ offsets,
                                    const int *__restrict__ indices,

@@ -7,6 +7,11 @@
 #include <vector>
 
 #define GBPA_MAX_1D 16       // largest D1D / Q1D handled (the generic kernels)
+// Gather-map entry that reads as zero: a constrained operator's pre-masked
+// copy of the map marks its essential dofs' slots with it, so the gather
+// needs no separate mask lookup. Never a valid signed index (-1 - j with
+// j <= INT_MAX - 1, since ndofs is an int).
+#define GBPA_GATHER_SKIP (-2147483647 - 1)
 
 struct gbpa_ctx
 {
@@ -104,6 +109,10 @@ int launch_csr_scatter(gbpa_ctx *ctx, int ndofs, const int *offsets,
                        const int *indices, const T *xE, T *y,
                        const unsigned char *ess_mask, const T *xc, bool add,
                        bool abs_values);
+
+// out[i] = gather_map[i], or GBPA_GATHER_SKIP where the slot's dof is masked.
+int launch_masked_gather_map(gbpa_ctx *ctx, int64_t n, const int *gather_map,
+                             const unsigned char *mask, int *out);
 
 // nbz chosen for (kind, precision, D, Q): tuned table or default.
 int elements_per_block(int kind, int precision, int D, int Q);

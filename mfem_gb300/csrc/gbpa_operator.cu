@@ -304,6 +304,11 @@ extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *de
       int flags = 0;
       if (!rc) { rc = gbpa_get_error_flags(ctx, &flags); }
       if (!rc && (flags & GBPA_FLAG_INDEX)) { rc = GBPA_ERR_INDEX; }
+      if (!rc && nE > 0)
+      {
+         rc = check_cuda(cudaMalloc(&op->gmap_m, sizeof(int) * nE), "cudaMalloc(masked map)");
+         if (!rc) { rc = launch_masked_gather_map(ctx, nE, d.gather_map, op->mask, op->gmap_m); }
+      }
    }
    if (rc) { gbpa_operator_destroy(op); return rc; }
    *out = op;
@@ -315,7 +320,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    if (!op) { return GBPA_SUCCESS; }
    cudaStreamSynchronize(op->ctx->stream);
    if (op->graph) { cudaGraphExecDestroy(op->graph); }
-   cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->qd2);
+   cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->gmap_m); cudaFree(op->qd2);
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
    cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb);
@@ -335,19 +340,19 @@ static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
       {
          return launch_diffusion_apply_x2(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
                                           (const double *)d.B, (const double *)d.G, op->qd2, xd,
-                                          d.gather_map, op->mask, (double *)op->yE, false, skip);
+                                          op->gather(), op->gather_mask(), (double *)op->yE, false, skip);
       }
       return launch_mass_apply_x2(op->ctx, d.ne, d.d1d, d.q1d, (const double *)d.B, op->qd2, xd,
-                                  d.gather_map, op->mask, (double *)op->yE, false, skip);
+                                  op->gather(), op->gather_mask(), (double *)op->yE, false, skip);
    }
    if (d.kind == GBPA_DIFFUSION)
    {
       return launch_diffusion_apply<T>(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
                                        (const T *)d.B, (const T *)d.G, (const T *)d.qdata, x,
-                                       d.gather_map, op->mask, (T *)op->yE, false, skip);
+                                       op->gather(), op->gather_mask(), (T *)op->yE, false, skip);
    }
    return launch_mass_apply<T>(op->ctx, d.ne, d.d1d, d.q1d, (const T *)d.B,
-                               (const T *)d.qdata, x, d.gather_map, op->mask, (T *)op->yE,
+                               (const T *)d.qdata, x, op->gather(), op->gather_mask(), (T *)op->yE,
                                false, skip);
 }
 

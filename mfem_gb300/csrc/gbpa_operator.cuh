@@ -13,9 +13,15 @@ struct PcgState
 
 struct gbpa_operator
 {
+   // gather map and mask for the element kernels: the pre-masked map when
+   // the operator is constrained (no per-gather mask lookup)
+   const int *gather() const { return gmap_m ? gmap_m : d.gather_map; }
+   const unsigned char *gather_mask() const { return gmap_m ? nullptr : mask; }
+
    gbpa_ctx *ctx = nullptr;
    gbpa_operator_desc d{};
    unsigned char *mask = nullptr;   // ess mask (ndofs) or null
+   int *gmap_m = nullptr;           // with ess: gather map with the ess slots set to GBPA_GATHER_SKIP
    void *yE = nullptr;              // E-vector scratch in the operator's precision
    float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
    // PCG workspace (vectors in the operator's precision)
