@@ -105,6 +105,31 @@ def test_large_apply_matches_oracle():
     assert np.linalg.norm(y.cpu().numpy() - yo) / np.linalg.norm(yo) < 1e-12
 
 
+@pytest.mark.parametrize("p", [4, 5])
+def test_reduced_precision_constrained_apply(p):
+    """FP32 and double-float constrained L->L applies (pre-masked gather map;
+    FP32 qdata staged by bulk copies, at p=5 with odd Q where the last
+    block's aligned copy would pass the end of the array and the block reads
+    global memory) against the FP64 constrained apply."""
+    from mfem_gb300.pa import PAOperator
+    fes, integ, _ = setup(16 if p == 4 else 13, p, "kappa")
+    ess = fes.GetBoundaryTrueDofs()
+    args = (0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata)
+    op64 = PAOperator(*args, ess=ess)
+    x = torch.rand(fes.ndofs, dtype=torch.float64, device="cuda") - 0.5
+    y64 = torch.empty_like(x)
+    op64.Mult(x, y64)
+    opx = PAOperator(*args, ess=ess, precision=2)
+    yx = torch.empty_like(x)
+    opx.Mult(x, yx)
+    assert float(torch.linalg.norm(yx - y64) / torch.linalg.norm(y64)) < 1e-12
+    op32 = PAOperator(*args, ess=ess, precision=1)
+    x32 = x.float()
+    y32 = torch.empty_like(x32)
+    op32.Mult(x32, y32)
+    assert float(torch.linalg.norm(y32.double() - y64) / torch.linalg.norm(y64)) < 1e-5
+
+
 def test_under_integration_d_greater_than_q():
     """D > Q (p=4 with a 3-point rule) runs through the generic apply kernel."""
     from tests import oracle_lib
