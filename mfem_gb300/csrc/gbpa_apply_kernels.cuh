@@ -248,7 +248,47 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             for (int qz = 0; qz < QM; ++qz) { qpre[k][qz] = AR::ldq(qe + k * Q3 + Q * Q * qz); }
       }
    }
-   if (part && active)
+   if constexpr (GATHER && TD > 0 && TQ > 0)
+   {
+      // compile-time sizes: all of the thread's map entries first, then all
+      // of its dof loads, so the dependent map -> x loads overlap instead of
+      // taking one round trip per dof
+      constexpr int Q2 = TQ * TQ, NPT = (TD * TD * TD + Q2 - 1) / Q2;
+      const int ts = tx + TQ * ty;
+      const long long base = e * D3;
+      int gi[NPT];
+#pragma unroll
+      for (int k = 0; k < NPT; ++k)
+      {
+         const int i = ts + k * Q2;
+         gi[k] = (part && active && i < D3) ? __ldg(gmap + base + i) : GBPA_GATHER_SKIP;
+      }
+      V gv[NPT];
+#pragma unroll
+      for (int k = 0; k < NPT; ++k)
+      {
+         const int g = gi[k];
+         V v = AR::zero();
+         if (g != GBPA_GATHER_SKIP)
+         {
+            const int j = g >= 0 ? g : -1 - g;
+            if (!(mask && __ldg(mask + j)))
+            {
+               const typename AR::In *p = x + (long long)j * xs;
+               v = AR::in(COH ? __ldcg(p) : __ldg(p));
+               if (g < 0) { v = AR::neg(v); }
+            }
+         }
+         gv[k] = v;
+      }
+#pragma unroll
+      for (int k = 0; k < NPT; ++k)
+      {
+         const int i = ts + k * Q2;
+         if (part && active && i < D3) { bufA[i] = gv[k]; }
+      }
+   }
+   else if (part && active)
    {
       const long long base = e * D3;
       for (int i = tx + Q * ty; i < D3; i += Q * Q)
