@@ -33,6 +33,7 @@
 //               completes in normal operation.
 #include "gbpa_apply_kernels.cuh"
 #include "gbpa_batched.cuh"
+#include "gbpa_csr.cuh"
 #include "gbpa_dispatch.cuh"
 #include <algorithm>
 #include <cmath>
@@ -258,16 +259,7 @@ batched_pcg_kernel(BParams P)
          {
             double v;
             if (pr.mask && pr.mask[i]) { v = pr.d[i]; }
-            else
-            {
-               v = 0.0;
-               for (int j = pr.off[i]; j < pr.off[i + 1]; ++j)
-               {
-                  const int sj = pr.ind[j];
-                  const double a = __ldcg(pr.yE + (sj >= 0 ? sj : -1 - sj));
-                  v += sj >= 0 ? a : -a;
-               }
-            }
+            else { v = csr_row_sum<double, true>(pr.off, pr.ind, pr.yE, i); }
             pr.z[i] = v;
             s += pr.d[i] * v;
          }
@@ -442,16 +434,7 @@ __global__ void __launch_bounds__(BATCH_THREADS) bg_scatter_den_kernel(GParams P
    {
       double v;
       if (pr.mask && pr.mask[i]) { v = pr.d[i]; }
-      else
-      {
-         v = 0.0;
-         for (int j = pr.off[i]; j < pr.off[i + 1]; ++j)
-         {
-            const int sj = pr.ind[j];
-            const double a = pr.yE[sj >= 0 ? sj : -1 - sj];
-            v += sj >= 0 ? a : -a;
-         }
-      }
+      else { v = csr_row_sum<double>(pr.off, pr.ind, pr.yE, i); }
       pr.z[i] = v;
       s += pr.d[i] * v;
    }

@@ -4,6 +4,7 @@
 // one set of scalars per right-hand side) on vectors stored interleaved,
 // v[i*R + r]. A mixed-precision block solve wraps FP32 block PCG in FP64 defect
 // correction with FP64 true residuals, per right-hand side.
+#include "gbpa_csr.cuh"
 #include "gbpa_operator.cuh"
 #include <cmath>
 #include <cstdlib>
@@ -123,16 +124,7 @@ __global__ void blk_scatter_den_kernel(int ndofs, int R, const int *__restrict__
       const int i = (int)(k / R), q = (int)(k % R);
       T v;
       if (mask && mask[i]) { v = d[k]; }
-      else
-      {
-         v = T(0);
-         for (int j = offsets[i]; j < offsets[i + 1]; ++j)
-         {
-            const int sj = indices[j];
-            const T a = yE[(int64_t)(sj >= 0 ? sj : -1 - sj) * R + q];
-            v += sj >= 0 ? a : -a;
-         }
-      }
+      else { v = csr_row_sum<T>(offsets, indices, yE, i, false, R, q); }
       z[k] = v;
       s += (double)d[k] * (double)v;
    }
@@ -227,14 +219,7 @@ __global__ void blk_scatter_kernel(int ndofs, int R, const int *__restrict__ off
    {
       const int i = (int)(k / R), q = (int)(k % R);
       if (mask && mask[i]) { y[k] = xc[k]; continue; }
-      T v = T(0);
-      for (int j = offsets[i]; j < offsets[i + 1]; ++j)
-      {
-         const int sj = indices[j];
-         const T a = yE[(int64_t)(sj >= 0 ? sj : -1 - sj) * R + q];
-         v += sj >= 0 ? a : -a;
-      }
-      y[k] = v;
+      y[k] = csr_row_sum<T>(offsets, indices, yE, i, false, R, q);
    }
 }
 

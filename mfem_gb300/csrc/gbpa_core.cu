@@ -5,6 +5,7 @@
 //   dot / reduce       linalg/vector.cpp:1079-1106, general/reducers.hpp:451-594
 //   vector add         linalg/vector.cpp:414-600
 //   Jacobi setup       linalg/solvers.cpp:401-425
+#include "gbpa_csr.cuh"
 #include "gbpa_dispatch.cuh"
 #include <cstring>
 #include <mutex>
@@ -182,15 +183,7 @@ __global__ void csr_scatter_kernel(int ndofs, const int *__restrict__ offsets,
         i += gridDim.x * blockDim.x)
    {
       if (mask && mask[i]) { y[i] = xc[i]; continue; }
-      T v = 0;
-      const int j0 = offsets[i], j1 = offsets[i + 1];
-      for (int j = j0; j < j1; ++j)
-      {
-         const int s = indices[j];
-         const int k = s >= 0 ? s : -1 - s;
-         const T a = xE[k];
-         v += (s >= 0 || use_abs) ? a : -a;
-      }
+      const T v = csr_row_sum<T>(offsets, indices, xE, i, use_abs != 0);
       y[i] = add ? y[i] + v : v;
    }
 }

@@ -5,6 +5,7 @@
 //   ConstrainedOperator (DIAG_ONE)    linalg/operator.cpp:526-661
 //   CGSolver::Mult                    linalg/solvers.cpp:869-1050
 //   OperatorJacobiSmoother::Mult      linalg/solvers.cpp:427-452
+#include "gbpa_csr.cuh"
 #include "gbpa_operator.cuh"
 #include <cmath>
 #include <cstdlib>
@@ -122,16 +123,7 @@ __global__ void pcg_scatter_den_kernel(int ndofs, const int *__restrict__ offset
    {
       T v;
       if (mask && mask[i]) { v = d[i]; }
-      else
-      {
-         v = T(0);
-         for (int j = offsets[i]; j < offsets[i + 1]; ++j)
-         {
-            const int sj = indices[j];
-            const T a = yE[sj >= 0 ? sj : -1 - sj];
-            v += sj >= 0 ? a : -a;
-         }
-      }
+      else { v = csr_row_sum<T>(offsets, indices, yE, i); }
       z[i] = v;
       s += (double)d[i] * (double)v;
    }

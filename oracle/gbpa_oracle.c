@@ -784,3 +784,347 @@ done:
    free(r); free(d); free(z); free(zz); free(work);
    return final_iter;
 }
+
+/* ------------------------------------------------------------ p-multigrid */
+/* CGSolver::Mult (linalg/solvers.cpp:869-1050) with a general
+ * preconditioner (prec == NULL: plain CG, z = r), zero initial guess. */
+typedef void (*or_prec_fn)(void *ctx, const double *r, double *z);
+static int pcg_generic(const or_cop *A, or_prec_fn prec, void *pctx, const double *b,
+                       double *x, double rel_tol, double abs_tol, int max_it,
+                       double *final_norm, int *converged)
+{
+   const int n = A->ndofs;
+   double *r = (double *)malloc(sizeof(double) * n);
+   double *d = (double *)malloc(sizeof(double) * n);
+   double *z = (double *)malloc(sizeof(double) * n);
+   int i, final_iter = 0;
+   double nom, den, betanom = 0.0, alpha, beta, r0;
+   memcpy(r, b, sizeof(double) * n);
+   memset(x, 0, sizeof(double) * n);
+   if (prec) { prec(pctx, r, z); } else { memcpy(z, r, sizeof(double) * n); }
+   memcpy(d, z, sizeof(double) * n);
+   nom = dot(n, d, r);
+   *converged = 0;
+   if (nom < 0.0 || !isfinite(nom)) { *final_norm = nom; goto done; }
+   r0 = fmax(nom * rel_tol * rel_tol, abs_tol * abs_tol);
+   if (nom <= r0) { *converged = 1; *final_norm = sqrt(nom); goto done; }
+   cop_mult(A, d, z);
+   den = dot(n, z, d);
+   if (den == 0.0) { *final_norm = sqrt(nom); goto done; }
+   final_iter = max_it;
+   for (i = 1; 1;)
+   {
+      alpha = nom / den;
+      for (int k = 0; k < n; ++k) { x[k] += alpha * d[k]; }
+      for (int k = 0; k < n; ++k) { r[k] += -alpha * z[k]; }
+      if (prec) { prec(pctx, r, z); } else { memcpy(z, r, sizeof(double) * n); }
+      betanom = dot(n, r, z);
+      if (betanom < 0.0 || !isfinite(betanom)) { final_iter = i; break; }
+      if (betanom <= r0) { *converged = 1; final_iter = i; break; }
+      if (++i > max_it) { break; }
+      beta = betanom / nom;
+      for (int k = 0; k < n; ++k) { d[k] = z[k] + beta * d[k]; }
+      cop_mult(A, d, z);
+      den = dot(n, d, z);
+      if (den == 0.0) { final_iter = i; break; }
+      nom = betanom;
+   }
+   *final_norm = sqrt(betanom);
+done:
+   free(r); free(d); free(z);
+   return final_iter;
+}
+
+/* ElementRestriction::BooleanMask (fem/restriction.cpp:255-292): 1 on the
+ * first element slot of each dof's CSR row, 0 on its other slots. */
+void or_boolean_mask(int ndofs, int nslots, const int *offsets, const int *indices,
+                     double *mask)
+{
+   for (int s = 0; s < nslots; ++s) { mask[s] = 0.0; }
+   for (int i = 0; i < ndofs; ++i)
+   {
+      if (offsets[i + 1] > offsets[i])
+      {
+         const int s = indices[offsets[i]];
+         mask[s >= 0 ? s : -1 - s] = 1.0;
+      }
+   }
+}
+
+/* y(qx,qy,qz) = sum Bi(qx,dx) Bi(qy,dy) Bi(qz,dz) x(dx,dy,dz) per element
+ * (Bi: (df, dc)); transpose != 0 applies the transposed contraction
+ * (fem/transfer.cpp:2703-2934, TransferKernels::{Prolongation,Restriction}3D). */
+static void interp3d(int ne, int dc, int df, const double *Bi, const double *x, double *y,
+                     int transpose)
+{
+   const int n_in = transpose ? df : dc, n_out = transpose ? dc : df;
+   const long in3 = (long)n_in * n_in * n_in, out3 = (long)n_out * n_out * n_out;
+   double *t1 = (double *)malloc(sizeof(double) * n_out * n_in * n_in);
+   double *t2 = (double *)malloc(sizeof(double) * n_out * n_out * n_in);
+   for (int e = 0; e < ne; ++e)
+   {
+      const double *xe = x + e * in3;
+      double *ye = y + e * out3;
+      /* M(o, i) = Bi(o, i) (prolong) or Bi(i, o) (transpose) */
+#define MI(o, i) (transpose ? Bi[(i) + df * (o)] : Bi[(o) + df * (i)])
+      for (int k = 0; k < n_in; ++k)
+         for (int j = 0; j < n_in; ++j)
+            for (int o = 0; o < n_out; ++o)
+            {
+               double s = 0.0;
+               for (int i = 0; i < n_in; ++i) { s += MI(o, i) * xe[i + n_in * (j + n_in * k)]; }
+               t1[o + n_out * (j + n_in * k)] = s;
+            }
+      for (int k = 0; k < n_in; ++k)
+         for (int o2 = 0; o2 < n_out; ++o2)
+            for (int o = 0; o < n_out; ++o)
+            {
+               double s = 0.0;
+               for (int j = 0; j < n_in; ++j) { s += MI(o2, j) * t1[o + n_out * (j + n_in * k)]; }
+               t2[o + n_out * (o2 + n_out * k)] = s;
+            }
+      for (int o3 = 0; o3 < n_out; ++o3)
+         for (int o2 = 0; o2 < n_out; ++o2)
+            for (int o = 0; o < n_out; ++o)
+            {
+               double s = 0.0;
+               for (int k = 0; k < n_in; ++k) { s += MI(o3, k) * t2[o + n_out * (o2 + n_out * k)]; }
+               ye[o + n_out * (o2 + n_out * o3)] = s;
+            }
+#undef MI
+   }
+   free(t1); free(t2);
+}
+
+/* TensorProductPRefinementTransferOperator::Mult (fem/transfer.cpp:2939-2963):
+ * y_f = R_f^T (mask .* I (R_c x_c)). */
+void or_ptransfer_mult(const or_mg_level *c, const or_mg_level *f, const double *x, double *y)
+{
+   const int ne = c->ne, dc = c->d1d, df = f->d1d;
+   const long nc = (long)ne * dc * dc * dc, nf = (long)ne * df * df * df;
+   double *xe = (double *)malloc(sizeof(double) * nc);
+   double *ye = (double *)malloc(sizeof(double) * nf);
+   double *mask = (double *)malloc(sizeof(double) * nf);
+   or_restriction_mult(ne, dc * dc * dc, c->gather_map, x, xe);
+   interp3d(ne, dc, df, f->Bi, xe, ye, 0);
+   or_boolean_mask(f->ndofs, (int)nf, f->offsets, f->indices, mask);
+   for (long s = 0; s < nf; ++s) { ye[s] *= mask[s]; }
+   or_restriction_mult_transpose(df * df * df, f->ndofs, f->offsets, f->indices, ye, y, 0);
+   free(xe); free(ye); free(mask);
+}
+
+/* ::MultTranspose (fem/transfer.cpp:2965-2989): y_c = R_c^T I^T (mask .* R_f x_f). */
+void or_ptransfer_mult_transpose(const or_mg_level *c, const or_mg_level *f, const double *x,
+                                 double *y)
+{
+   const int ne = c->ne, dc = c->d1d, df = f->d1d;
+   const long nc = (long)ne * dc * dc * dc, nf = (long)ne * df * df * df;
+   double *xe = (double *)malloc(sizeof(double) * nf);
+   double *ye = (double *)malloc(sizeof(double) * nc);
+   double *mask = (double *)malloc(sizeof(double) * nf);
+   or_restriction_mult(ne, df * df * df, f->gather_map, x, xe);
+   or_boolean_mask(f->ndofs, (int)nf, f->offsets, f->indices, mask);
+   for (long s = 0; s < nf; ++s) { xe[s] *= mask[s]; }
+   interp3d(ne, dc, df, f->Bi, xe, ye, 1);
+   or_restriction_mult_transpose(dc * dc * dc, c->ndofs, c->offsets, c->indices, ye, y, 0);
+   free(xe); free(ye); free(mask);
+}
+
+/* Chebyshev smoother coefficients (linalg/solvers.cpp:552-616 states them
+ * in closed form for orders 1-5): with the interval [0.3, 1.2] * lambda,
+ * theta its centre and delta its half width, the smoother is
+ * y = p(D^-1 A) D^-1 x where 1 - t p(t) = T_k((theta - t)/delta) /
+ * T_k(theta/delta). Derived here by expanding the Chebyshev recurrence
+ * T_{m+1} = 2 s T_m - T_{m-1} at s = (theta - t)/delta as polynomials in t:
+ * c_{j-1} = -e_j / e_0 for T_k(s(t)) = sum_j e_j t^j. */
+void or_chebyshev_coeffs(int order, double lambda, double *c)
+{
+   const double up = 1.2 * lambda, lo = 0.3 * lambda;
+   const double theta = 0.5 * (up + lo), delta = 0.5 * (up - lo);
+   const double a = theta / delta, b = -1.0 / delta;
+   double Pm[16] = {0}, P[16] = {0}, Pn[16];
+   Pm[0] = 1.0;                 /* T_0 */
+   P[0] = a; P[1] = b;          /* T_1 */
+   if (order == 1) { memcpy(Pm, P, sizeof(P)); }
+   for (int m = 1; m < order; ++m)
+   {
+      for (int j = 0; j <= m + 1; ++j)
+      {
+         double v = 2.0 * a * P[j] - Pm[j];
+         if (j > 0) { v += 2.0 * b * P[j - 1]; }
+         Pn[j] = v;
+      }
+      for (int j = m + 2; j < 16; ++j) { Pn[j] = 0.0; }
+      memcpy(Pm, P, sizeof(P));
+      memcpy(P, Pn, sizeof(P));
+   }
+   const double *T = order == 1 ? Pm : P;
+   for (int j = 1; j <= order; ++j) { c[j - 1] = -T[j] / T[0]; }
+}
+
+static void level_cop(const or_mg_level *l, or_cop *A, double *work, double *zz)
+{
+   or_cop t = {l->ne, l->ndofs, 1, l->d1d, l->q1d, l->gather_map, l->offsets, l->indices,
+               l->B, l->G, l->qdata, l->ess, l->n_ess, work, zz};
+   *A = t;
+}
+static double *level_dinv(const or_mg_level *l)
+{
+   double *dinv = (double *)malloc(sizeof(double) * l->ndofs);
+   for (int i = 0; i < l->ndofs; ++i) { dinv[i] = 1.0 / l->diag[i]; }
+   for (int i = 0; i < l->n_ess; ++i) { dinv[l->ess[i]] = 1.0; }
+   return dinv;
+}
+
+/* OperatorChebyshevSmoother::Mult (linalg/solvers.cpp:619-656) */
+void or_chebyshev_mult(const or_mg_level *l, int order, const double *x, double *y)
+{
+   const int n = l->ndofs;
+   const long nE = (long)l->ne * l->d1d * l->d1d * l->d1d;
+   double coeffs[16];
+   or_chebyshev_coeffs(order, l->lambda, coeffs);
+   double *dinv = level_dinv(l);
+   double *res = (double *)malloc(sizeof(double) * n);
+   double *h = (double *)malloc(sizeof(double) * n);
+   double *work = (double *)malloc(sizeof(double) * 2 * nE);
+   double *zz = (double *)malloc(sizeof(double) * n);
+   or_cop A;
+   level_cop(l, &A, work, zz);
+   memcpy(res, x, sizeof(double) * n);
+   for (int i = 0; i < n; ++i) { y[i] = 0.0; }
+   for (int k = 0; k < order; ++k)
+   {
+      if (k > 0)
+      {
+         cop_mult(&A, res, h);
+         memcpy(res, h, sizeof(double) * n);
+      }
+      for (int i = 0; i < n; ++i) { res[i] *= dinv[i]; }
+      for (int i = 0; i < n; ++i) { y[i] += coeffs[k] * res[i]; }
+   }
+   free(dinv); free(res); free(h); free(work); free(zz);
+}
+
+/* splitmix64 at counter i: the i-th draw of the stream seeded with `seed`,
+ * as a double in [0, 1) */
+static double sm_u01(unsigned long long seed, long i)
+{
+   unsigned long long z = seed + (unsigned long long)(i + 1) * 0x9e3779b97f4a7c15ULL;
+   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+   z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+   z ^= z >> 31;
+   return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* PowerMethod::EstimateLargestEigenvalue (linalg/operator.cpp:886-942) on
+ * D^-1 A (OperatorJacobiSmoother with ess entries 1, linalg/solvers.cpp:
+ * 493-510); the start vector is the splitmix64 stream of `seed`. */
+double or_power_method(const or_mg_level *l, int steps, double tol, unsigned long long seed)
+{
+   const int n = l->ndofs;
+   const long nE = (long)l->ne * l->d1d * l->d1d * l->d1d;
+   double *dinv = level_dinv(l);
+   double *v0 = (double *)malloc(sizeof(double) * n);
+   double *v1 = (double *)malloc(sizeof(double) * n);
+   double *work = (double *)malloc(sizeof(double) * 2 * nE);
+   double *zz = (double *)malloc(sizeof(double) * n);
+   or_cop A;
+   level_cop(l, &A, work, zz);
+   for (int i = 0; i < n; ++i) { v0[i] = sm_u01(seed, i); }
+   double lam = 1.0;
+   for (int it = 0; it < steps; ++it)
+   {
+      const double nrm = sqrt(dot(n, v0, v0));
+      for (int i = 0; i < n; ++i) { v0[i] /= nrm; }
+      cop_mult(&A, v0, v1);
+      for (int i = 0; i < n; ++i) { v1[i] *= dinv[i]; }
+      const double ln = dot(n, v0, v1);
+      const double diff = fabs((ln - lam) / lam);
+      lam = ln;
+      double *t = v0; v0 = v1; v1 = t;
+      if (diff < tol) { break; }
+   }
+   free(dinv); free(v0); free(v1); free(work); free(zz);
+   return lam;
+}
+
+typedef struct
+{
+   const or_mg_level *lv;
+   int order;
+   double coarse_tol;
+   int coarse_max;
+} or_mg;
+
+/* MultigridBase::Cycle, V-cycle with one pre- and one post-smoothing step
+ * (fem/multigrid.cpp:147-239): X = right-hand side, Y = correction. */
+static void mg_cycle(const or_mg *M, int level, const double *X, double *Y)
+{
+   const or_mg_level *l = M->lv + level;
+   const int n = l->ndofs;
+   const long nE = (long)l->ne * l->d1d * l->d1d * l->d1d;
+   double *work = (double *)malloc(sizeof(double) * 2 * nE);
+   double *zz = (double *)malloc(sizeof(double) * n);
+   or_cop A;
+   level_cop(l, &A, work, zz);
+   if (level == 0)
+   {
+      double fn; int conv;
+      pcg_generic(&A, NULL, NULL, X, Y, M->coarse_tol, 0.0, M->coarse_max, &fn, &conv);
+      free(work); free(zz);
+      return;
+   }
+   const or_mg_level *c = M->lv + level - 1;
+   double *R = (double *)malloc(sizeof(double) * n);
+   double *Z = (double *)malloc(sizeof(double) * n);
+   double *Xc = (double *)malloc(sizeof(double) * c->ndofs);
+   double *Yc = (double *)malloc(sizeof(double) * c->ndofs);
+   or_chebyshev_mult(l, M->order, X, Y);                  /* pre-smooth, zero guess */
+   cop_mult(&A, Y, R);
+   for (int i = 0; i < n; ++i) { R[i] = X[i] - R[i]; }
+   or_ptransfer_mult_transpose(c, l, R, Xc);
+   for (int i = 0; i < c->ndofs; ++i) { Yc[i] = 0.0; }
+   mg_cycle(M, level - 1, Xc, Yc);
+   or_ptransfer_mult(c, l, Yc, Z);
+   for (int i = 0; i < n; ++i) { Y[i] += Z[i]; }
+   cop_mult(&A, Y, R);                                    /* post-smooth */
+   for (int i = 0; i < n; ++i) { R[i] = X[i] - R[i]; }
+   or_chebyshev_mult(l, M->order, R, Z);
+   for (int i = 0; i < n; ++i) { Y[i] += Z[i]; }
+   free(R); free(Z); free(Xc); free(Yc); free(work); free(zz);
+}
+
+void or_mg_mult(const or_mg_level *lv, int nl, int order, double coarse_tol, int coarse_max,
+                const double *x, double *y)
+{
+   or_mg M = {lv, order, coarse_tol, coarse_max};
+   for (int i = 0; i < lv[nl - 1].ndofs; ++i) { y[i] = 0.0; }
+   mg_cycle(&M, nl - 1, x, y);
+}
+
+typedef struct { or_mg M; int nl; } or_mg_ctx;
+static void mg_prec_top(void *ctx, const double *r, double *z)
+{
+   const or_mg_ctx *C = (const or_mg_ctx *)ctx;
+   for (int i = 0; i < C->M.lv[C->nl - 1].ndofs; ++i) { z[i] = 0.0; }
+   mg_cycle(&C->M, C->nl - 1, r, z);
+}
+
+/* CGSolver::Mult preconditioned by the V-cycle (the fine level's
+ * constrained operator); returns the iteration count. */
+int or_mg_pcg(const or_mg_level *lv, int nl, int order, double coarse_tol, int coarse_max,
+              const double *b, double *x, double rel_tol, double abs_tol, int max_it,
+              double *final_norm, int *converged)
+{
+   const or_mg_level *f = lv + nl - 1;
+   const long nE = (long)f->ne * f->d1d * f->d1d * f->d1d;
+   double *work = (double *)malloc(sizeof(double) * 2 * nE);
+   double *zz = (double *)malloc(sizeof(double) * f->ndofs);
+   or_cop A;
+   level_cop(f, &A, work, zz);
+   or_mg_ctx C = {{lv, order, coarse_tol, coarse_max}, nl};
+   const int it = pcg_generic(&A, mg_prec_top, &C, b, x, rel_tol, abs_tol, max_it, final_norm,
+                              converged);
+   free(work); free(zz);
+   return it;
+}

@@ -95,6 +95,44 @@ int or_pcg_diffusion(int ne, int ndofs, int symm, int d1d, int q1d,
                      double rel_tol, double abs_tol, int max_it,
                      int iterative_mode, double *final_norm, int *converged);
 
+/* ---- p-multigrid (examples/ex26.cpp structure). One level of the
+ * hierarchy: its symmetric PA diffusion operator (constrained by ess), the
+ * unconstrained diagonal and eigenvalue estimate of D^-1 A for its
+ * Chebyshev smoother, and Bi (d1d, d1d of the level below): the coarser
+ * level's Lagrange basis at this level's lexicographic nodes. */
+typedef struct or_mg_level
+{
+   int ne, ndofs, d1d, q1d;
+   const int *gather_map, *offsets, *indices;
+   const double *B, *G, *qdata;
+   const int *ess;
+   int n_ess;
+   const double *diag;
+   double lambda;
+   const double *Bi;
+} or_mg_level;
+
+/* fem/restriction.cpp:255-292 */
+void or_boolean_mask(int ndofs, int nslots, const int *offsets, const int *indices,
+                     double *mask);
+/* fem/transfer.cpp:2939-2989 (c: coarse level, f: fine level) */
+void or_ptransfer_mult(const or_mg_level *c, const or_mg_level *f, const double *x, double *y);
+void or_ptransfer_mult_transpose(const or_mg_level *c, const or_mg_level *f, const double *x,
+                                 double *y);
+/* linalg/solvers.cpp:538-616 (coefficients), 619-656 (Mult) */
+void or_chebyshev_coeffs(int order, double lambda, double *c);
+void or_chebyshev_mult(const or_mg_level *l, int order, const double *x, double *y);
+/* linalg/operator.cpp:886-942 on D^-1 A; start vector: splitmix64(seed) */
+double or_power_method(const or_mg_level *l, int steps, double tol, unsigned long long seed);
+/* fem/multigrid.cpp:106-239: y = V(1,1)-cycle(x); level 0 solved by CG to
+ * coarse_tol (at most coarse_max iterations) */
+void or_mg_mult(const or_mg_level *lv, int nl, int order, double coarse_tol, int coarse_max,
+                const double *x, double *y);
+/* CGSolver::Mult preconditioned by the V-cycle; returns iterations */
+int or_mg_pcg(const or_mg_level *lv, int nl, int order, double coarse_tol, int coarse_max,
+              const double *b, double *x, double rel_tol, double abs_tol, int max_it,
+              double *final_norm, int *converged);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int or_num_threads(void);
 

@@ -8,6 +8,7 @@
 //   AddMultPA / AssembleDiagonal fem/integ/bilininteg_{diffusion,mass}_pa.cpp
 //   BilinearForm::Mult (PA)      fem/bilinearform_ext.cpp:487-564
 //   PCG + OperatorJacobiSmoother linalg/solvers.cpp:331-452,869-1050
+//   p-multigrid (transfer, Chebyshev smoother, V-cycle): run_pmg below
 // Usage: golden_driver <outdir>   (one subdirectory per case)
 #include "mfem.hpp"
 #include "fem/integ/bilininteg_diffusion_kernels.hpp"
@@ -382,6 +383,176 @@ static void run_case(const Case &c, const std::string &root)
           p + 1, q, coeff_dim);
 }
 
+// p-multigrid case (examples/ex26.cpp's structure with a variable kappa):
+// orders 1, 2, 4 on one jittered mesh; TransferOperator between the orders
+// (TensorProductPRefinementTransferOperator, fem/transfer.cpp:2620-2990);
+// OperatorChebyshevSmoother of order 2 on levels 1, 2 (linalg/solvers.cpp:
+// 455-660, its eigenvalue estimate from PowerMethod, linalg/operator.cpp:
+// 886-942); CGSolver to 1e-2 (max 200) on level 0; Multigrid V(1,1)
+// (fem/multigrid.cpp:106-239) as the preconditioner of CGSolver to 1e-10.
+static void run_pmg(const std::string &root)
+{
+   const std::string dir = root + "/pmg4_p124";
+   mkdir(dir.c_str(), 0755);
+   const int n = 4;
+   Mesh mesh = Mesh::MakeCartesian3D(n, n, n, Element::HEXAHEDRON, 1.0, 1.0, 1.0, true);
+   jitter_vertices(mesh, n, 0.1, 1);
+   g_modes = make_modes(3);
+   FunctionCoefficient kfn(kappa_fn);
+   const int orders[3] = {1, 2, 4};
+   const int L = 3;
+   Array<int> ess_bdr(mesh.bdr_attributes.Max());
+   ess_bdr = 1;
+   std::vector<H1_FECollection *> fecs;
+   std::vector<FiniteElementSpace *> spaces;
+   std::vector<BilinearForm *> forms;
+   std::vector<Array<int>> ess(L);
+   Array<Operator *> ops, prolongs;
+   Array<Solver *> smoothers;
+   Array<bool> own_ops, own_sm, own_pr;
+   std::vector<double> lambdas;
+   for (int l = 0; l < L; l++)
+   {
+      fecs.push_back(new H1_FECollection(orders[l], 3));
+      spaces.push_back(new FiniteElementSpace(&mesh, fecs.back()));
+      FiniteElementSpace &fes = *spaces.back();
+      const std::string lv = "l" + std::to_string(l) + "_";
+      // the default rule of DiffusionIntegrator::GetRule (fem/bilininteg.cpp:
+      // 1346-1375): order 2p + 2, p + 2 points per direction
+      const int q = orders[l] + 2;
+      const IntegrationRule &ir = IntRules.Get(Geometry::CUBE, 2 * orders[l] + 2);
+      MFEM_VERIFY(ir.GetNPoints() == q * q * q, "rule size");
+      {
+         const ElementRestriction *R = dynamic_cast<const ElementRestriction*>(
+            fes.GetElementRestriction(ElementDofOrdering::LEXICOGRAPHIC));
+         save(dir, (lv + "gather_map").c_str(), R->GatherMap());
+         save(dir, (lv + "offsets").c_str(), R->Offsets());
+         save(dir, (lv + "indices").c_str(), R->Indices());
+         const DofToQuad &maps = fes.GetTypicalFE()->GetDofToQuad(ir, DofToQuad::TENSOR);
+         save(dir, (lv + "B").c_str(), maps.B);
+         save(dir, (lv + "G").c_str(), maps.G);
+         const GeometricFactors *geom = mesh.GetGeometricFactors(ir, GeometricFactors::JACOBIANS);
+         QuadratureSpace qs(mesh, ir);
+         CoefficientVector cv(qs, CoefficientStorage::COMPRESSED);
+         cv.Project(kfn);
+         Vector qd(6 * q * q * q * mesh.GetNE());
+         internal::PADiffusionSetup(3, 3, orders[l] + 1, q, 1, mesh.GetNE(), ir.GetWeights(), geom->J,
+                                    cv, qd);
+         save(dir, (lv + "qdata").c_str(), qd);
+         if (l > 0)
+         {
+            // the transfer's tables: the coarse basis at this level's nodes
+            // in lexicographic order (fem/transfer.cpp:2640-2656)
+            const TensorBasisElement *htel =
+               dynamic_cast<const TensorBasisElement*>(fes.GetTypicalFE());
+            const Array<int> &hmap = htel->GetDofMap();
+            const IntegrationRule &nodes = fes.GetTypicalFE()->GetNodes();
+            IntegrationRule lex = nodes;
+            for (int i = 0; i < nodes.GetNPoints(); ++i)
+            {
+               const int j = hmap[i] >= 0 ? hmap[i] : -1 - hmap[i];
+               lex.IntPoint(i) = nodes.IntPoint(j);
+            }
+            const DofToQuad &tm = spaces[l - 1]->GetTypicalFE()->GetDofToQuad(lex, DofToQuad::TENSOR);
+            save(dir, (lv + "Bi").c_str(), tm.B);
+         }
+      }
+      BilinearForm *a = new BilinearForm(&fes);
+      a->SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      a->AddDomainIntegrator(new DiffusionIntegrator(kfn, &ir));
+      a->Assemble();
+      forms.push_back(a);
+      fes.GetEssentialTrueDofs(ess_bdr, ess[l]);
+      OperatorPtr A;
+      a->FormSystemMatrix(ess[l], A);
+      A.SetOperatorOwner(false);
+      ops.Append(A.Ptr()); own_ops.Append(true);
+      save(dir, (lv + "ess").c_str(), ess[l]);
+      if (l == 0)
+      {
+         CGSolver *cg = new CGSolver();
+         cg->SetPrintLevel(-1);
+         cg->SetMaxIter(200);
+         cg->SetRelTol(sqrt(1e-4));
+         cg->SetAbsTol(0.0);
+         cg->SetOperator(*A.Ptr());
+         smoothers.Append(cg);
+      }
+      else
+      {
+         Vector diag(fes.GetTrueVSize());
+         a->AssembleDiagonal(diag);
+         save(dir, (lv + "diag").c_str(), diag);
+         // the smoother's own eigenvalue estimate, repeated to record it
+         OperatorJacobiSmoother invd(diag, ess[l], 1.0);
+         ProductOperator dA(&invd, A.Ptr(), false, false);
+         PowerMethod pm;
+         Vector ev(fes.GetTrueVSize());
+         const double lam = pm.EstimateLargestEigenvalue(dA, ev, 10, 1e-8, 12345);
+         lambdas.push_back(lam);
+         smoothers.Append(new OperatorChebyshevSmoother(*A.Ptr(), diag, ess[l], 2));
+         // the smoother applied with the recorded estimate to a fixed vector
+         OperatorChebyshevSmoother S(*A.Ptr(), diag, ess[l], 2, lam);
+         Vector x(fes.GetTrueVSize()), y(fes.GetTrueVSize());
+         uint64_t sd = 20 + l;
+         for (int i = 0; i < x.Size(); i++) { x(i) = 2.0 * u01(sd) - 1.0; }
+         S.Mult(x, y);
+         save(dir, (lv + "cheb_x").c_str(), x);
+         save(dir, (lv + "cheb_y").c_str(), y);
+      }
+      own_sm.Append(true);
+      if (l > 0)
+      {
+         TransferOperator *P = new TransferOperator(*spaces[l - 1], fes);
+         prolongs.Append(P); own_pr.Append(true);
+         Vector xc(spaces[l - 1]->GetTrueVSize()), yf(fes.GetTrueVSize());
+         Vector xf(fes.GetTrueVSize()), yc(spaces[l - 1]->GetTrueVSize());
+         uint64_t s1 = 30 + l, s2 = 40 + l;
+         for (int i = 0; i < xc.Size(); i++) { xc(i) = 2.0 * u01(s1) - 1.0; }
+         for (int i = 0; i < xf.Size(); i++) { xf(i) = 2.0 * u01(s2) - 1.0; }
+         P->Mult(xc, yf);
+         P->MultTranspose(xf, yc);
+         save(dir, (lv + "P_x").c_str(), xc);
+         save(dir, (lv + "P_y").c_str(), yf);
+         save(dir, (lv + "Pt_x").c_str(), xf);
+         save(dir, (lv + "Pt_y").c_str(), yc);
+      }
+   }
+   save_dbls(dir, "lambda", lambdas);
+   Multigrid mg(ops, smoothers, prolongs, own_ops, own_sm, own_pr);
+   mg.SetCycleType(Multigrid::CycleType::VCYCLE, 1, 1);
+   FiniteElementSpace &ffes = *spaces.back();
+   ConstantCoefficient one(1.0);
+   LinearForm b(&ffes);
+   b.AddDomainIntegrator(new DomainLFIntegrator(one));
+   b.Assemble();
+   GridFunction xs(&ffes); xs = 0.0;
+   OperatorPtr A; Vector X, Bv;
+   forms.back()->FormLinearSystem(ess.back(), xs, b, A, X, Bv);
+   save(dir, "B_rhs", Bv);
+   {
+      // one preconditioner application (V-cycle) to the right-hand side
+      Vector Mb(Bv.Size());
+      mg.Mult(Bv, Mb);
+      save(dir, "mg_b", Mb);
+   }
+   CGSolver cg;
+   cg.SetRelTol(1e-10); cg.SetAbsTol(0.0); cg.SetMaxIter(200); cg.SetPrintLevel(0);
+   cg.SetOperator(*A); cg.SetPreconditioner(mg);
+   X = 0.0;
+   cg.Mult(Bv, X);
+   save(dir, "X", X);
+   std::vector<double> info = {(double)cg.GetNumIterations(), cg.GetFinalNorm(), (double)cg.GetConverged()};
+   save_dbls(dir, "cg_info", info);
+   std::vector<int> meta = {mesh.GetNE(), n, orders[0], orders[1], orders[2]};
+   save_ints(dir, "meta", meta);
+   printf("pmg4_p124: MG-PCG iterations %d final norm %.6e lambda %.6f %.6f\n", cg.GetNumIterations(),
+          cg.GetFinalNorm(), lambdas[0], lambdas[1]);
+   for (auto *f : forms) { delete f; }
+   for (auto *f : spaces) { delete f; }
+   for (auto *f : fecs) { delete f; }
+}
+
 int main(int argc, char **argv)
 {
    if (argc < 2) { fprintf(stderr, "usage: %s outdir\n", argv[0]); return 1; }
@@ -404,5 +575,6 @@ int main(int argc, char **argv)
       {"cfg1_solve",      8, 3, 4, 0.0, C_ONE,    false, true},
    };
    for (const Case &c : cases) { run_case(c, root); }
+   run_pmg(root);
    return 0;
 }

@@ -36,7 +36,39 @@ _SIGS = {
     "or_pcg_diffusion": [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,
                          _P, _P, _P, _D, _D, _I, _I, _P, _P],
     "or_num_threads": [],
+    "or_boolean_mask": [_I, _I, _P, _P, _P],
+    "or_ptransfer_mult": [_P, _P, _P, _P],
+    "or_ptransfer_mult_transpose": [_P, _P, _P, _P],
+    "or_chebyshev_coeffs": [_I, _D, _P],
+    "or_chebyshev_mult": [_P, _I, _P, _P],
+    "or_power_method": [_P, _I, _D, ctypes.c_ulonglong],
+    "or_mg_mult": [_P, _I, _I, _D, _I, _P, _P],
+    "or_mg_pcg": [_P, _I, _I, _D, _I, _P, _P, _D, _D, _I, _P, _P],
 }
+_RESTYPES = {"or_pcg_diffusion": ctypes.c_int, "or_num_threads": ctypes.c_int,
+             "or_power_method": ctypes.c_double, "or_mg_pcg": ctypes.c_int}
+
+
+class MGLevel(ctypes.Structure):
+    """One level of the p-multigrid hierarchy (or_mg_level in gbpa_oracle.h).
+    The numpy arrays it points to are kept alive in `keep`."""
+    _fields_ = [("ne", _I), ("ndofs", _I), ("d1d", _I), ("q1d", _I), ("gather_map", _P),
+                ("offsets", _P), ("indices", _P), ("B", _P), ("G", _P), ("qdata", _P), ("ess", _P),
+                ("n_ess", _I), ("diag", _P), ("lambda_", _D), ("Bi", _P)]
+
+
+def mg_level(ne, ndofs, d1d, q1d, gm, off, ind, B, G, qd, ess, diag=None, lam=0.0, Bi=None):
+    arrs = dict(gm=np.ascontiguousarray(gm, np.int32), off=np.ascontiguousarray(off, np.int32),
+                ind=np.ascontiguousarray(ind, np.int32), B=np.ascontiguousarray(B, np.float64),
+                G=np.ascontiguousarray(G, np.float64), qd=np.ascontiguousarray(qd, np.float64),
+                ess=np.ascontiguousarray(ess, np.int32),
+                diag=None if diag is None else np.ascontiguousarray(diag, np.float64),
+                Bi=None if Bi is None else np.ascontiguousarray(Bi, np.float64))
+    lv = MGLevel(ne, ndofs, d1d, q1d, _ptr(arrs["gm"]), _ptr(arrs["off"]), _ptr(arrs["ind"]),
+                 _ptr(arrs["B"]), _ptr(arrs["G"]), _ptr(arrs["qd"]), _ptr(arrs["ess"]), arrs["ess"].size,
+                 _ptr(arrs["diag"]), lam, _ptr(arrs["Bi"]))
+    lv.keep = arrs
+    return lv
 
 
 def build():
@@ -156,6 +188,53 @@ class Oracle:
     def num_threads(self):
         return self.lib.or_num_threads()
 
+    # ---- p-multigrid (levels: list of MGLevel, coarsest first)
+    @staticmethod
+    def _levels(levels):
+        arr = (MGLevel * len(levels))(*levels)
+        return arr
+
+    def ptransfer_mult(self, c, f, x):
+        y = np.zeros(f.ndofs)
+        self.lib.or_ptransfer_mult(ctypes.byref(c), ctypes.byref(f), _ptr(np.ascontiguousarray(x)), _ptr(y))
+        return y
+
+    def ptransfer_mult_transpose(self, c, f, x):
+        y = np.zeros(c.ndofs)
+        self.lib.or_ptransfer_mult_transpose(ctypes.byref(c), ctypes.byref(f),
+                                             _ptr(np.ascontiguousarray(x)), _ptr(y))
+        return y
+
+    def chebyshev_coeffs(self, order, lam):
+        c = np.zeros(order)
+        self.lib.or_chebyshev_coeffs(order, lam, _ptr(c))
+        return c
+
+    def chebyshev_mult(self, lv, order, x):
+        y = np.zeros(lv.ndofs)
+        self.lib.or_chebyshev_mult(ctypes.byref(lv), order, _ptr(np.ascontiguousarray(x)), _ptr(y))
+        return y
+
+    def power_method(self, lv, steps=10, tol=1e-8, seed=12345):
+        return self.lib.or_power_method(ctypes.byref(lv), steps, tol, seed)
+
+    def mg_mult(self, levels, x, order=2, coarse_tol=1e-2, coarse_max=200):
+        arr = self._levels(levels)
+        y = np.zeros(levels[-1].ndofs)
+        self.lib.or_mg_mult(arr, len(levels), order, coarse_tol, coarse_max,
+                            _ptr(np.ascontiguousarray(x)), _ptr(y))
+        return y
+
+    def mg_pcg(self, levels, b, order=2, coarse_tol=1e-2, coarse_max=200, rel_tol=1e-10, abs_tol=0.0,
+               max_it=200):
+        arr = self._levels(levels)
+        x = np.zeros(levels[-1].ndofs)
+        fn = ctypes.c_double(0.0); conv = ctypes.c_int(0)
+        it = self.lib.or_mg_pcg(arr, len(levels), order, coarse_tol, coarse_max,
+                                _ptr(np.ascontiguousarray(b)), _ptr(x), rel_tol, abs_tol, max_it,
+                                ctypes.byref(fn), ctypes.byref(conv))
+        return x, it, fn.value, bool(conv.value)
+
 
 _cached = None
 
@@ -169,6 +248,6 @@ def load():
         for name, args in _SIGS.items():
             f = getattr(lib, name)
             f.argtypes = args
-            f.restype = ctypes.c_int if name in ("or_pcg_diffusion", "or_num_threads") else None
+            f.restype = _RESTYPES.get(name)
         _cached = Oracle(lib)
     return _cached
