@@ -366,6 +366,73 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
                               int max_it, int *iterations, int *converged,
                               double *final_norms, double *seconds);
 
+/* ---------------------------------------------------------- p-multigrid */
+/* p-multigrid preconditioning around the PA diffusion operator, the
+ * structure of the reference's examples/ex26.cpp. Levels are operators
+ * (gbpa_operator_create) with FP64 vectors: precision GBPA_F64 or
+ * GBPA_F64X2; they are borrowed, never freed by these objects. */
+
+/* p-refinement transfer between two H1 spaces on the same mesh
+ * (TensorProductPRefinementTransferOperator, fem/transfer.cpp:2620-2990;
+ * FiniteElementSpace::GetTransferOperator picks it for tensor H1 spaces of
+ * different orders, fem/transfer.cpp:2195-2216). The maps are the two
+ * spaces' lexicographic ElementRestriction maps (device memory, borrowed);
+ * Bi (d1d_f, d1d_c), host memory, column-major: the coarse Lagrange basis
+ * at the fine element's lexicographic nodes. d1d <= 10. */
+typedef struct gbpa_ptransfer *gbpa_ptransfer_t;
+int gbpa_ptransfer_create(gbpa_ctx_t ctx, int ne, int d1d_c, int ndofs_c,
+                          const int *gather_map_c, const int *offsets_c,
+                          const int *indices_c, int d1d_f, int ndofs_f,
+                          const int *gather_map_f, const int *offsets_f,
+                          const int *indices_f, const double *Bi,
+                          gbpa_ptransfer_t *out);
+int gbpa_ptransfer_destroy(gbpa_ptransfer_t T);
+/* TransferOperator::Mult: y_f = P x_c (prolongation) */
+int gbpa_ptransfer_mult(gbpa_ptransfer_t T, const double *xc, double *yf);
+/* TransferOperator::MultTranspose: y_c = P^T x_f */
+int gbpa_ptransfer_mult_transpose(gbpa_ptransfer_t T, const double *xf,
+                                  double *yc);
+
+/* OperatorChebyshevSmoother (linalg/solvers.cpp:455-660) for the
+ * constrained operator A with its unconstrained diagonal `diag` (device).
+ * max_eig > 0: the given estimate of the largest eigenvalue of D^-1 A
+ * (the constructor at solvers.cpp:455-469); max_eig <= 0: estimated by
+ * PowerMethod::EstimateLargestEigenvalue (linalg/operator.cpp:886-942) with
+ * power_iterations steps and tolerance power_tol (the reference's defaults:
+ * 10, 1e-8) from a splitmix64 start vector of `seed` (the reference draws
+ * it with the C library's rand()). order 1..8. */
+typedef struct gbpa_chebyshev *gbpa_chebyshev_t;
+int gbpa_chebyshev_create(gbpa_operator_t A, const double *diag, int order,
+                          double max_eig, int power_iterations,
+                          double power_tol, unsigned long long seed,
+                          gbpa_chebyshev_t *out);
+int gbpa_chebyshev_destroy(gbpa_chebyshev_t S);
+int gbpa_chebyshev_get_max_eig(gbpa_chebyshev_t S, double *max_eig);
+int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const double *x, double *y);
+
+/* Multigrid (fem/multigrid.cpp:106-239): V-cycle with one pre- and one
+ * post-smoothing step; level 0 (coarsest) solved by CGSolver without a
+ * preconditioner to coarse_rel_tol in at most coarse_max_it iterations
+ * (examples/ex26.cpp: 1e-2, 200). ops[0..nlevels), smoothers[1..nlevels)
+ * (smoothers[0] unused), prolongations[l] from level l to l+1. */
+typedef struct gbpa_multigrid *gbpa_multigrid_t;
+int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels,
+                          const gbpa_operator_t *ops,
+                          const gbpa_chebyshev_t *smoothers,
+                          const gbpa_ptransfer_t *prolongations,
+                          double coarse_rel_tol, int coarse_max_it,
+                          gbpa_multigrid_t *out);
+int gbpa_multigrid_destroy(gbpa_multigrid_t M);
+/* MultigridBase::Mult: y = one V-cycle applied to x (zero initial guess) */
+int gbpa_multigrid_mult(gbpa_multigrid_t M, const double *x, double *y);
+/* CGSolver::Mult (linalg/solvers.cpp:869-1050) on the finest operator A
+ * preconditioned by M, zero initial guess. info->iterations: outer CG
+ * iterations; info->inner_iterations: coarse-level CG iterations summed
+ * over all cycles; true_rel_residual is not computed (-1). */
+int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const double *b,
+                      double *x, double rel_tol, double abs_tol, int max_it,
+                      gbpa_solve_info *info);
+
 /* --------------------------------------------------------------- tuning */
 /* Elements per thread block used by the apply kernels for (kind, precision,
  * d1d, q1d); 0 = library default. The autotuner (python side) sweeps this. */

@@ -416,6 +416,12 @@ class CGSolver:
     def SetPrintLevel(self, _): pass
 
     def Mult(self, b, x):
+        if isinstance(self.prec, Multigrid):
+            st = _dev().lib.gbpa_pcg_solve_mg(self.oper.handle, self.prec.handle, _p(b), _p(x), self.rel_tol,
+                                              self.abs_tol, self.max_iter, ctypes.byref(self.info))
+            if st not in (0, -6):
+                check(st, "pcg_solve_mg")
+            return
         if self.prec is None:
             dinv = torch.ones_like(b)
         else:
@@ -429,3 +435,126 @@ class CGSolver:
     def GetNumIterations(self): return self.info.iterations
     def GetFinalNorm(self): return self.info.final_norm
     def GetConverged(self): return bool(self.info.converged)
+
+
+# ------------------------------------------------------------ p-multigrid
+class TransferOperator:
+    """fem/transfer.cpp TransferOperator between two H1 spaces of different
+    orders on the same mesh (TensorProductPRefinementTransferOperator):
+    Mult prolongs lfes -> hfes, MultTranspose restricts."""
+
+    def __init__(self, lfes, hfes):
+        dev = _dev()
+        from . import fem
+        Rl, Rh = lfes.GetElementRestriction(), hfes.GetElementRestriction()
+        dc, df = lfes.p + 1, hfes.p + 1
+        Bi, _ = fem.basis_tables(fem.gauss_lobatto(dc), fem.gauss_lobatto(df))
+        self.Bi = np.ascontiguousarray(Bi, np.float64)
+        self.lfes, self.hfes = lfes, hfes
+        h = ctypes.c_void_p()
+        check(dev.lib.gbpa_ptransfer_create(dev.ctx, lfes.ne, dc, lfes.ndofs, _p(Rl.gather_map), _p(Rl.offsets),
+                                            _p(Rl.indices), df, hfes.ndofs, _p(Rh.gather_map), _p(Rh.offsets),
+                                            _p(Rh.indices), self.Bi.ctypes.data_as(ctypes.c_void_p),
+                                            ctypes.byref(h)), "ptransfer_create")
+        self.handle = h
+
+    def Mult(self, x, y):
+        check(_dev().lib.gbpa_ptransfer_mult(self.handle, _p(x), _p(y)), "ptransfer_mult")
+
+    def MultTranspose(self, x, y):
+        check(_dev().lib.gbpa_ptransfer_mult_transpose(self.handle, _p(x), _p(y)), "ptransfer_mult_transpose")
+
+    def __del__(self):
+        try:
+            _dev().lib.gbpa_ptransfer_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class OperatorChebyshevSmoother:
+    """linalg/solvers.cpp OperatorChebyshevSmoother on a constrained
+    PAOperator. max_eig_estimate None: PowerMethod (power_iterations,
+    power_tolerance) from a splitmix64 start vector of power_seed."""
+
+    def __init__(self, oper, diag, ess_tdof_list, order, max_eig_estimate=None, power_iterations=10,
+                 power_tolerance=1e-8, power_seed=12345):
+        dev = _dev()
+        self.oper, self.diag = oper, diag
+        h = ctypes.c_void_p()
+        lam = float(max_eig_estimate) if max_eig_estimate else 0.0
+        check(dev.lib.gbpa_chebyshev_create(oper.handle, _p(diag), order, lam, power_iterations, power_tolerance,
+                                            power_seed, ctypes.byref(h)), "chebyshev_create")
+        self.handle = h
+
+    def GetMaxEigEstimate(self):
+        v = ctypes.c_double(0.0)
+        check(_dev().lib.gbpa_chebyshev_get_max_eig(self.handle, ctypes.byref(v)), "chebyshev_get_max_eig")
+        return v.value
+
+    def Mult(self, x, y):
+        check(_dev().lib.gbpa_chebyshev_mult(self.handle, _p(x), _p(y)), "chebyshev_mult")
+
+    def __del__(self):
+        try:
+            _dev().lib.gbpa_chebyshev_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class Multigrid:
+    """fem/multigrid.cpp Multigrid with a V(1,1) cycle: operators coarsest
+    first, Chebyshev smoothers on levels >= 1, prolongations between
+    consecutive levels; level 0 solved by CG to coarse_rel_tol."""
+
+    def __init__(self, operators, smoothers, prolongations, coarse_rel_tol=1e-2, coarse_max_it=200):
+        dev = _dev()
+        nl = len(operators)
+        self.operators, self.smoothers, self.prolongations = operators, smoothers, prolongations
+        ops = (ctypes.c_void_p * nl)(*[o.handle for o in operators])
+        sms = (ctypes.c_void_p * nl)(*[None] + [s.handle for s in smoothers[1:]])
+        prs = (ctypes.c_void_p * max(nl - 1, 1))(*[P.handle for P in prolongations])
+        h = ctypes.c_void_p()
+        check(dev.lib.gbpa_multigrid_create(dev.ctx, nl, ops, sms, prs, coarse_rel_tol, coarse_max_it,
+                                            ctypes.byref(h)), "multigrid_create")
+        self.handle = h
+
+    def Mult(self, x, y):
+        check(_dev().lib.gbpa_multigrid_mult(self.handle, _p(x), _p(y)), "multigrid_mult")
+
+    def __del__(self):
+        try:
+            _dev().lib.gbpa_multigrid_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class DiffusionMultigrid(Multigrid):
+    """The reference's examples/ex26.cpp DiffusionMultigrid on one mesh with
+    an order hierarchy (e.g. 1, 2, 4): a constrained PA diffusion operator
+    per order (Dirichlet on the whole boundary), order-2 Chebyshev smoothers
+    with power-method eigenvalue estimates, CG to 1e-2 on the coarsest
+    order. precision: the levels' arithmetic (GBPA_F64 or GBPA_F64X2).
+    max_eigs: optional eigenvalue estimates for levels 1.. (else estimated)."""
+
+    def __init__(self, mesh, orders, coeff="kappa", modes=None, precision=_lib.GBPA_F64, cheb_order=2,
+                 coarse_rel_tol=1e-2, coarse_max_it=200, max_eigs=None, ir_points=None):
+        dev = _dev()
+        self.spaces, self.integs, ops, smoothers, prols = [], [], [], [], []
+        self.ess = []
+        for l, p in enumerate(orders):
+            fes = FiniteElementSpace(mesh, p)
+            integ = DiffusionIntegrator(coeff, ir_points=ir_points(p) if ir_points else None)
+            integ.AssemblePA(fes, modes=modes)
+            ess = fes.GetBoundaryTrueDofs()
+            A = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=precision)
+            self.spaces.append(fes); self.integs.append(integ); self.ess.append(ess)
+            ops.append(A)
+            if l == 0:
+                smoothers.append(None)
+            else:
+                diag = torch.empty(fes.ndofs, dtype=torch.float64, device=dev.torch_device)
+                A.AssembleDiagonal(diag)
+                lam = max_eigs[l - 1] if max_eigs is not None else None
+                smoothers.append(OperatorChebyshevSmoother(A, diag, ess, cheb_order, lam))
+                prols.append(TransferOperator(self.spaces[l - 1], fes))
+        super().__init__(ops, smoothers, prols, coarse_rel_tol, coarse_max_it)
