@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--combined", action="store_true", help="run only the combined-form comparison")
     ap.add_argument("--combined-n", type=int, default=24, help="54: ~19.9 M DOFs at p=5")
     ap.add_argument("--no-reference", action="store_true", help="combined form: skip the FP64 reference solve")
+    ap.add_argument("--mg", action="store_true", help="run only the p-multigrid-preconditioned solve")
+    ap.add_argument("--mg-n", type=int, default=77)
+    ap.add_argument("--mg-jacobi", action="store_true", help="p-multigrid form: also time FP64 Jacobi-PCG")
     return ap.parse_args()
 
 
@@ -558,6 +561,74 @@ def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
             "problems_per_order": {str(q): orders.count(q) for q in range(2, 7)}}
 
 
+def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
+    """p-multigrid (next step past the Jacobi preconditioner): the precision
+    form's problem (jittered n^3 mesh, lognormal kappa, RHS ~ U[0,1], seed 4,
+    Dirichlet boundary) solved by CG preconditioned with a V(1,1) p-multigrid
+    cycle over the orders `orders` (order-2 Chebyshev smoothing with
+    power-method estimates, CG to 1e-2 on the coarsest order), the structure
+    of the reference's examples/ex26.cpp (coarse CG without preconditioner,
+    at most 200 iterations), and the same with a Jacobi-preconditioned coarse
+    CG capped at 50 iterations. Level arithmetic FP64 and double-float; the
+    true FP64 residual of each solution is reported, and, with_jacobi, the
+    plain FP64 Jacobi-PCG solve of the same system."""
+    import torch
+    from mfem_gb300 import _lib, fem
+    from mfem_gb300.pa import CGSolver, Device, DiffusionMultigrid, OperatorJacobiSmoother
+    dev = Device.get()
+    mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
+    out = {"workload": f"Dirichlet Poisson, lognormal kappa, jittered n={n}^3, p={p}, levels p={list(orders)}",
+           "rel_tol": rel_tol}
+    sols = {}
+    A64 = M64 = None
+    b = None
+    configs = [("fp64", _lib.GBPA_F64, False, 200), ("f64x2", _lib.GBPA_F64X2, False, 200),
+               ("fp64_coarse_jacobi", _lib.GBPA_F64, True, 50), ("f64x2_coarse_jacobi", _lib.GBPA_F64X2, True, 50)]
+    for name, prec, cj, cmax in configs:
+        t0 = time.perf_counter()
+        M = DiffusionMultigrid(mesh, orders, "kappa", modes=fem.kappa_modes(3), precision=prec,
+                               coarse_jacobi=cj, coarse_max_it=cmax)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        fes = M.spaces[-1]
+        if b is None:
+            b = torch.from_numpy(fem.u01_array(4, fes.ndofs)).cuda()
+            b[torch.from_numpy(M.ess[-1]).long().cuda()] = 0.0
+        x = torch.zeros_like(b)
+        cg = CGSolver(); cg.SetRelTol(rel_tol); cg.SetMaxIter(500); cg.SetOperator(M.operators[-1])
+        cg.SetPreconditioner(M)
+        cg.Mult(b, x)
+        info = cg.info
+        if prec == _lib.GBPA_F64:
+            A64, M64 = M.operators[-1], M
+        r = torch.empty_like(b)
+        A64.Mult(x, r)
+        res = float(torch.linalg.norm(b - r) / torch.linalg.norm(b))
+        out[name] = {"seconds": info.seconds, "iterations": info.iterations, "converged": info.converged,
+                     "coarse": f"CG{' + Jacobi' if cj else ''} to 1e-2, at most {cmax} iterations",
+                     "coarse_cg_iterations": info.inner_iterations, "setup_seconds": setup,
+                     "true_rel_residual": res,
+                     "max_eig": [M.smoothers[l].GetMaxEigEstimate() for l in range(1, len(orders))]}
+        sols[name] = x
+        if M is not M64:
+            del M
+    for name in sols:
+        if name != "fp64":
+            out[name]["rel_l2_vs_fp64"] = float(torch.linalg.norm(sols[name] - sols["fp64"]) /
+                                                torch.linalg.norm(sols["fp64"]))
+    if with_jacobi:
+        J = OperatorJacobiSmoother(A64, M64.ess[-1])
+        xj = torch.zeros_like(b)
+        cj = CGSolver(); cj.SetRelTol(rel_tol); cj.SetMaxIter(20000); cj.SetOperator(A64); cj.SetPreconditioner(J)
+        cj.Mult(b, xj)
+        out["jacobi_fp64"] = {"seconds": cj.info.seconds, "iterations": cj.info.iterations,
+                              "rel_l2_mg_vs_jacobi": float(torch.linalg.norm(sols["fp64"] - xj) /
+                                                           torch.linalg.norm(xj))}
+        for name in sols:
+            out[f"speedup_{name}_vs_jacobi_fp64"] = cj.info.seconds / max(out[name]["seconds"], 1e-30)
+    return out
+
+
 def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
     """Combined form: unit cube mapped by x -> x + 0.05 sin(2 pi x) sin(2 pi y)
     sin(2 pi z) per component (order-3 geometry), H1 order p, lognormal kappa,
@@ -626,6 +697,11 @@ def main():
         from mfem_gb300.pa import Device
         Device("cuda", dist_info()[2])
         print(json.dumps({"batched": run_batched_form(args.nprob)}), flush=True)
+        return 0
+    if args.mg:
+        from mfem_gb300.pa import Device
+        Device("cuda", dist_info()[2])
+        print(json.dumps({"mg": run_mg_form(args.mg_n, 4, (1, 2, 4), args.mg_jacobi)}), flush=True)
         return 0
     if args.combined:
         from mfem_gb300.pa import Device

@@ -411,17 +411,19 @@ int gbpa_chebyshev_get_max_eig(gbpa_chebyshev_t S, double *max_eig);
 int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const double *x, double *y);
 
 /* Multigrid (fem/multigrid.cpp:106-239): V-cycle with one pre- and one
- * post-smoothing step; level 0 (coarsest) solved by CGSolver without a
- * preconditioner to coarse_rel_tol in at most coarse_max_it iterations
- * (examples/ex26.cpp: 1e-2, 200). ops[0..nlevels), smoothers[1..nlevels)
- * (smoothers[0] unused), prolongations[l] from level l to l+1. */
+ * post-smoothing step; level 0 (coarsest) solved by CGSolver to
+ * coarse_rel_tol in at most coarse_max_it iterations, without a
+ * preconditioner (coarse_jacobi = 0: examples/ex26.cpp, 1e-2 and 200) or
+ * with the Jacobi smoother of the coarse operator (coarse_jacobi = 1).
+ * ops[0..nlevels), smoothers[1..nlevels) (smoothers[0] unused),
+ * prolongations[l] from level l to l+1. */
 typedef struct gbpa_multigrid *gbpa_multigrid_t;
 int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels,
                           const gbpa_operator_t *ops,
                           const gbpa_chebyshev_t *smoothers,
                           const gbpa_ptransfer_t *prolongations,
                           double coarse_rel_tol, int coarse_max_it,
-                          gbpa_multigrid_t *out);
+                          int coarse_jacobi, gbpa_multigrid_t *out);
 int gbpa_multigrid_destroy(gbpa_multigrid_t M);
 /* MultigridBase::Mult: y = one V-cycle applied to x (zero initial guess) */
 int gbpa_multigrid_mult(gbpa_multigrid_t M, const double *x, double *y);

@@ -110,7 +110,7 @@ SIGNATURES = {
     "gbpa_chebyshev_destroy": (I, [P]),
     "gbpa_chebyshev_get_max_eig": (I, [P, ctypes.POINTER(D)]),
     "gbpa_chebyshev_mult": (I, [P, P, P]),
-    "gbpa_multigrid_create": (I, [P, I, P, P, P, D, I, ctypes.POINTER(P)]),
+    "gbpa_multigrid_create": (I, [P, I, P, P, P, D, I, I, ctypes.POINTER(P)]),
     "gbpa_multigrid_destroy": (I, [P]),
     "gbpa_multigrid_mult": (I, [P, P, P]),
     "gbpa_pcg_solve_mg": (I, [P, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),

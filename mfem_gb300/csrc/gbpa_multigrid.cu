@@ -277,8 +277,8 @@ struct gbpa_multigrid
    std::vector<gbpa_ptransfer *> P;
    double coarse_tol = 1e-2;
    int coarse_max = 200;
+   double *coarse_dinv = nullptr;      // level-0 CG preconditioner: ones (plain CG) or Jacobi
    std::vector<double *> X, Y, R, Z;   // per level
-   double *ones = nullptr;             // level-0 "preconditioner" of plain CG
    double *d_dot = nullptr;
    int64_t coarse_iterations = 0;
 };
@@ -540,10 +540,11 @@ extern "C" int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const double *x, double *
 // -------------------------------------------------------------- multigrid
 extern "C" int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels, const gbpa_operator_t *ops,
                                      const gbpa_chebyshev_t *smoothers, const gbpa_ptransfer_t *prolongations,
-                                     double coarse_rel_tol, int coarse_max_it, gbpa_multigrid_t *out)
+                                     double coarse_rel_tol, int coarse_max_it, int coarse_jacobi,
+                                     gbpa_multigrid_t *out)
 {
    if (!ctx || !out || nlevels < 1 || !ops || (nlevels > 1 && (!smoothers || !prolongations)) ||
-       coarse_rel_tol < 0 || coarse_max_it < 0)
+       coarse_rel_tol < 0 || coarse_max_it < 0 || (coarse_jacobi != 0 && coarse_jacobi != 1))
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
@@ -576,8 +577,22 @@ extern "C" int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels, const gbpa_ope
       if (!rc) { rc = dev_alloc(&z, n); }
       M->X.push_back(x); M->Y.push_back(y); M->R.push_back(r); M->Z.push_back(z);
    }
-   if (!rc) { rc = dev_alloc(&M->ones, ops[0]->d.ndofs); }
-   if (!rc) { rc = fill(ctx, ops[0]->d.ndofs, 1.0, M->ones); }
+   const int64_t n0 = ops[0]->d.ndofs;
+   if (!rc) { rc = dev_alloc(&M->coarse_dinv, n0); }
+   if (!rc && !coarse_jacobi) { rc = fill(ctx, n0, 1.0, M->coarse_dinv); }
+   if (!rc && coarse_jacobi && n0 > 0)
+   {
+      // OperatorJacobiSmoother on the coarse constrained operator: its
+      // diagonal (1 on the essential dofs), inverted
+      double *diag = nullptr;
+      rc = dev_alloc(&diag, n0);
+      if (!rc) { rc = gbpa_operator_assemble_diagonal(ops[0], diag); }
+      if (!rc)
+      {
+         rc = gbpa_jacobi_setup(ctx, n0, diag, ops[0]->d.ess, ops[0]->d.n_ess, 1.0, M->coarse_dinv);
+      }
+      cudaFree(diag);
+   }
    if (!rc) { rc = dev_alloc(&M->d_dot, 1); }
    if (rc) { gbpa_multigrid_destroy(M); return rc; }
    *out = M;
@@ -592,7 +607,7 @@ extern "C" int gbpa_multigrid_destroy(gbpa_multigrid_t M)
    for (double *p : M->Y) { cudaFree(p); }
    for (double *p : M->R) { cudaFree(p); }
    for (double *p : M->Z) { cudaFree(p); }
-   cudaFree(M->ones); cudaFree(M->d_dot);
+   cudaFree(M->coarse_dinv); cudaFree(M->d_dot);
    delete M;
    return GBPA_SUCCESS;
 }
@@ -608,10 +623,10 @@ int mg_cycle(gbpa_multigrid *M, int level)
    const int64_t n = A->d.ndofs;
    if (level == 0)
    {
-      // CGSolver without preconditioner to the coarse tolerance (plain CG is
-      // Jacobi-PCG with a unit inverse diagonal)
+      // CGSolver to the coarse tolerance: without preconditioner (plain CG is
+      // Jacobi-PCG with a unit inverse diagonal) or with Jacobi
       gbpa_solve_info info;
-      int rc = gbpa_pcg_solve(A, M->ones, M->X[0], M->Y[0], M->coarse_tol, 0.0, M->coarse_max, 0, &info);
+      int rc = gbpa_pcg_solve(A, M->coarse_dinv, M->X[0], M->Y[0], M->coarse_tol, 0.0, M->coarse_max, 0, &info);
       M->coarse_iterations += info.iterations;
       return rc == GBPA_ERR_NOT_CONVERGED ? GBPA_SUCCESS : rc;
    }

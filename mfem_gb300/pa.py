@@ -506,7 +506,8 @@ class Multigrid:
     first, Chebyshev smoothers on levels >= 1, prolongations between
     consecutive levels; level 0 solved by CG to coarse_rel_tol."""
 
-    def __init__(self, operators, smoothers, prolongations, coarse_rel_tol=1e-2, coarse_max_it=200):
+    def __init__(self, operators, smoothers, prolongations, coarse_rel_tol=1e-2, coarse_max_it=200,
+                 coarse_jacobi=False):
         dev = _dev()
         nl = len(operators)
         self.operators, self.smoothers, self.prolongations = operators, smoothers, prolongations
@@ -515,7 +516,7 @@ class Multigrid:
         prs = (ctypes.c_void_p * max(nl - 1, 1))(*[P.handle for P in prolongations])
         h = ctypes.c_void_p()
         check(dev.lib.gbpa_multigrid_create(dev.ctx, nl, ops, sms, prs, coarse_rel_tol, coarse_max_it,
-                                            ctypes.byref(h)), "multigrid_create")
+                                            1 if coarse_jacobi else 0, ctypes.byref(h)), "multigrid_create")
         self.handle = h
 
     def Mult(self, x, y):
@@ -533,11 +534,12 @@ class DiffusionMultigrid(Multigrid):
     an order hierarchy (e.g. 1, 2, 4): a constrained PA diffusion operator
     per order (Dirichlet on the whole boundary), order-2 Chebyshev smoothers
     with power-method eigenvalue estimates, CG to 1e-2 on the coarsest
-    order. precision: the levels' arithmetic (GBPA_F64 or GBPA_F64X2).
-    max_eigs: optional eigenvalue estimates for levels 1.. (else estimated)."""
+    order (coarse_jacobi: Jacobi-preconditioned). precision: the levels'
+    arithmetic (GBPA_F64 or GBPA_F64X2). max_eigs: optional eigenvalue
+    estimates for levels 1.. (else estimated)."""
 
     def __init__(self, mesh, orders, coeff="kappa", modes=None, precision=_lib.GBPA_F64, cheb_order=2,
-                 coarse_rel_tol=1e-2, coarse_max_it=200, max_eigs=None, ir_points=None):
+                 coarse_rel_tol=1e-2, coarse_max_it=200, max_eigs=None, ir_points=None, coarse_jacobi=False):
         dev = _dev()
         self.spaces, self.integs, ops, smoothers, prols = [], [], [], [], []
         self.ess = []
@@ -557,4 +559,4 @@ class DiffusionMultigrid(Multigrid):
                 lam = max_eigs[l - 1] if max_eigs is not None else None
                 smoothers.append(OperatorChebyshevSmoother(A, diag, ess, cheb_order, lam))
                 prols.append(TransferOperator(self.spaces[l - 1], fes))
-        super().__init__(ops, smoothers, prols, coarse_rel_tol, coarse_max_it)
+        super().__init__(ops, smoothers, prols, coarse_rel_tol, coarse_max_it, coarse_jacobi)

@@ -64,7 +64,7 @@ class GoldenHierarchy:
         sms = (ctypes.c_void_p * 3)(*self.sm)
         prs = (ctypes.c_void_p * 2)(*self.P)
         self.mg = ctypes.c_void_p()
-        assert d.lib.gbpa_multigrid_create(d.ctx, 3, ops, sms, prs, 1e-2, 200, ctypes.byref(self.mg)) == 0
+        assert d.lib.gbpa_multigrid_create(d.ctx, 3, ops, sms, prs, 1e-2, 200, 0, ctypes.byref(self.mg)) == 0
 
     def close(self):
         lib = self.d.lib
@@ -150,27 +150,29 @@ def test_power_method_matches_oracle(g):
     H_.close()
 
 
-def pmg_problem(n, orders, precision=0):
+def pmg_problem(n, orders, precision=0, coarse_jacobi=False):
     from mfem_gb300 import fem
     from mfem_gb300.pa import DiffusionMultigrid
     from tests.gpu_util import dev
     dev()
     mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
-    M = DiffusionMultigrid(mesh, orders, "kappa", modes=fem.kappa_modes(3), precision=precision)
+    M = DiffusionMultigrid(mesh, orders, "kappa", modes=fem.kappa_modes(3), precision=precision,
+                           coarse_jacobi=coarse_jacobi)
     fes = M.spaces[-1]
     b = torch.from_numpy(fem.u01_array(4, fes.ndofs)).cuda()
     b[torch.from_numpy(M.ess[-1]).long().cuda()] = 0.0
     return M, b
 
 
-@pytest.mark.parametrize("precision", [0, 2])
-def test_mg_pcg_solves_the_jacobi_system(precision):
+@pytest.mark.parametrize("precision,coarse_jacobi", [(0, False), (2, False), (2, True)])
+def test_mg_pcg_solves_the_jacobi_system(precision, coarse_jacobi):
     """On a 10^3 mesh at p=4 (levels 1, 2, 4): the MG-preconditioned solve
-    reaches the Jacobi-PCG solution of the same constrained system (1e-9)
-    in far fewer iterations."""
+    (plain or Jacobi-preconditioned coarse CG) reaches the Jacobi-PCG
+    solution of the same constrained system (1e-9) in far fewer
+    iterations."""
     from mfem_gb300 import _lib
     from mfem_gb300.pa import CGSolver, OperatorJacobiSmoother
-    M, b = pmg_problem(10, (1, 2, 4), precision)
+    M, b = pmg_problem(10, (1, 2, 4), precision, coarse_jacobi)
     A = M.operators[-1]
     x = torch.zeros_like(b)
     cg = CGSolver(); cg.SetRelTol(1e-11); cg.SetMaxIter(500); cg.SetOperator(A); cg.SetPreconditioner(M)
