@@ -569,9 +569,10 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
     power-method estimates, CG to 1e-2 on the coarsest order), the structure
     of the reference's examples/ex26.cpp (coarse CG without preconditioner,
     at most 200 iterations), and the same with a Jacobi-preconditioned coarse
-    CG capped at 50 iterations. Level arithmetic FP64 and double-float; the
-    true FP64 residual of each solution is reported, and, with_jacobi, the
-    plain FP64 Jacobi-PCG solve of the same system."""
+    CG capped at 50 iterations. Level arithmetic FP64 and double-float, and
+    FP32 levels preconditioning the FP64 CG; the true FP64 residual of each
+    solution is reported, and, with_jacobi, the plain FP64 Jacobi-PCG solve
+    of the same system."""
     import torch
     from mfem_gb300 import _lib, fem
     from mfem_gb300.pa import CGSolver, Device, DiffusionMultigrid, OperatorJacobiSmoother
@@ -583,7 +584,8 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
     A64 = M64 = None
     b = None
     configs = [("fp64", _lib.GBPA_F64, False, 200), ("f64x2", _lib.GBPA_F64X2, False, 200),
-               ("fp64_coarse_jacobi", _lib.GBPA_F64, True, 50), ("f64x2_coarse_jacobi", _lib.GBPA_F64X2, True, 50)]
+               ("fp64_coarse_jacobi", _lib.GBPA_F64, True, 50), ("f64x2_coarse_jacobi", _lib.GBPA_F64X2, True, 50),
+               ("f32_levels_coarse_jacobi", _lib.GBPA_F32, True, 50)]
     for name, prec, cj, cmax in configs:
         t0 = time.perf_counter()
         M = DiffusionMultigrid(mesh, orders, "kappa", modes=fem.kappa_modes(3), precision=prec,
@@ -595,7 +597,9 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
             b = torch.from_numpy(fem.u01_array(4, fes.ndofs)).cuda()
             b[torch.from_numpy(M.ess[-1]).long().cuda()] = 0.0
         x = torch.zeros_like(b)
-        cg = CGSolver(); cg.SetRelTol(rel_tol); cg.SetMaxIter(500); cg.SetOperator(M.operators[-1])
+        cg = CGSolver(); cg.SetRelTol(rel_tol); cg.SetMaxIter(500)
+        # FP32 levels precondition the FP64 iteration on the FP64 operator
+        cg.SetOperator(M.operators[-1] if prec != _lib.GBPA_F32 else A64)
         cg.SetPreconditioner(M)
         cg.Mult(b, x)
         info = cg.info

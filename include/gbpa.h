@@ -369,8 +369,10 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
 /* ---------------------------------------------------------- p-multigrid */
 /* p-multigrid preconditioning around the PA diffusion operator, the
  * structure of the reference's examples/ex26.cpp. Levels are operators
- * (gbpa_operator_create) with FP64 vectors: precision GBPA_F64 or
- * GBPA_F64X2; they are borrowed, never freed by these objects. */
+ * (gbpa_operator_create), borrowed, never freed by these objects: all with
+ * FP64 vectors (precision GBPA_F64 or GBPA_F64X2) or all GBPA_F32 (float
+ * vectors; the V-cycle then runs in FP32 as a preconditioner of the FP64
+ * CG). Vector arguments are in the levels' type. */
 
 /* p-refinement transfer between two H1 spaces on the same mesh
  * (TensorProductPRefinementTransferOperator, fem/transfer.cpp:2620-2990;
@@ -378,20 +380,21 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
  * different orders, fem/transfer.cpp:2195-2216). The maps are the two
  * spaces' lexicographic ElementRestriction maps (device memory, borrowed);
  * Bi (d1d_f, d1d_c), host memory, column-major: the coarse Lagrange basis
- * at the fine element's lexicographic nodes. d1d <= 10. */
+ * at the fine element's lexicographic nodes. d1d <= 10. precision:
+ * GBPA_F64 (double vectors) or GBPA_F32 (float vectors). */
 typedef struct gbpa_ptransfer *gbpa_ptransfer_t;
 int gbpa_ptransfer_create(gbpa_ctx_t ctx, int ne, int d1d_c, int ndofs_c,
                           const int *gather_map_c, const int *offsets_c,
                           const int *indices_c, int d1d_f, int ndofs_f,
                           const int *gather_map_f, const int *offsets_f,
                           const int *indices_f, const double *Bi,
-                          gbpa_ptransfer_t *out);
+                          int precision, gbpa_ptransfer_t *out);
 int gbpa_ptransfer_destroy(gbpa_ptransfer_t T);
 /* TransferOperator::Mult: y_f = P x_c (prolongation) */
-int gbpa_ptransfer_mult(gbpa_ptransfer_t T, const double *xc, double *yf);
+int gbpa_ptransfer_mult(gbpa_ptransfer_t T, const void *xc, void *yf);
 /* TransferOperator::MultTranspose: y_c = P^T x_f */
-int gbpa_ptransfer_mult_transpose(gbpa_ptransfer_t T, const double *xf,
-                                  double *yc);
+int gbpa_ptransfer_mult_transpose(gbpa_ptransfer_t T, const void *xf,
+                                  void *yc);
 
 /* OperatorChebyshevSmoother (linalg/solvers.cpp:455-660) for the
  * constrained operator A with its unconstrained diagonal `diag` (device).
@@ -408,27 +411,32 @@ int gbpa_chebyshev_create(gbpa_operator_t A, const double *diag, int order,
                           gbpa_chebyshev_t *out);
 int gbpa_chebyshev_destroy(gbpa_chebyshev_t S);
 int gbpa_chebyshev_get_max_eig(gbpa_chebyshev_t S, double *max_eig);
-int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const double *x, double *y);
+int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const void *x, void *y);
 
 /* Multigrid (fem/multigrid.cpp:106-239): V-cycle with one pre- and one
  * post-smoothing step; level 0 (coarsest) solved by CGSolver to
  * coarse_rel_tol in at most coarse_max_it iterations, without a
  * preconditioner (coarse_jacobi = 0: examples/ex26.cpp, 1e-2 and 200) or
- * with the Jacobi smoother of the coarse operator (coarse_jacobi = 1).
- * ops[0..nlevels), smoothers[1..nlevels) (smoothers[0] unused),
- * prolongations[l] from level l to l+1. */
+ * with the Jacobi smoother of the coarse operator (coarse_jacobi = 1; its
+ * diagonal coarse_diag, FP64 device memory, or NULL to assemble it from
+ * the coarse operator, which needs FP64 data). ops[0..nlevels),
+ * smoothers[1..nlevels) (smoothers[0] unused), prolongations[l] from level
+ * l to l+1. */
 typedef struct gbpa_multigrid *gbpa_multigrid_t;
 int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels,
                           const gbpa_operator_t *ops,
                           const gbpa_chebyshev_t *smoothers,
                           const gbpa_ptransfer_t *prolongations,
                           double coarse_rel_tol, int coarse_max_it,
-                          int coarse_jacobi, gbpa_multigrid_t *out);
+                          int coarse_jacobi, const double *coarse_diag,
+                          gbpa_multigrid_t *out);
 int gbpa_multigrid_destroy(gbpa_multigrid_t M);
 /* MultigridBase::Mult: y = one V-cycle applied to x (zero initial guess) */
-int gbpa_multigrid_mult(gbpa_multigrid_t M, const double *x, double *y);
-/* CGSolver::Mult (linalg/solvers.cpp:869-1050) on the finest operator A
- * preconditioned by M, zero initial guess. info->iterations: outer CG
+int gbpa_multigrid_mult(gbpa_multigrid_t M, const void *x, void *y);
+/* CGSolver::Mult (linalg/solvers.cpp:869-1050) on A (FP64 vectors, the
+ * finest level's size) preconditioned by M, zero initial guess; with FP32
+ * levels the residual is narrowed into the cycle and the correction widened
+ * back. info->iterations: outer CG
  * iterations; info->inner_iterations: coarse-level CG iterations summed
  * over all cycles; true_rel_residual is not computed (-1). */
 int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const double *b,

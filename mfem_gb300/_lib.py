@@ -102,7 +102,7 @@ SIGNATURES = {
                                              ctypes.POINTER(D)]),
     "gbpa_batched_pcg_solve_ex": (I, [P, I, ctypes.POINTER(ProblemDesc), I, I, D, D, I, P, P, P,
                                       ctypes.POINTER(D)]),
-    "gbpa_ptransfer_create": (I, [P, I, I, I, P, P, P, I, I, P, P, P, P, ctypes.POINTER(P)]),
+    "gbpa_ptransfer_create": (I, [P, I, I, I, P, P, P, I, I, P, P, P, P, I, ctypes.POINTER(P)]),
     "gbpa_ptransfer_destroy": (I, [P]),
     "gbpa_ptransfer_mult": (I, [P, P, P]),
     "gbpa_ptransfer_mult_transpose": (I, [P, P, P]),
@@ -110,7 +110,7 @@ SIGNATURES = {
     "gbpa_chebyshev_destroy": (I, [P]),
     "gbpa_chebyshev_get_max_eig": (I, [P, ctypes.POINTER(D)]),
     "gbpa_chebyshev_mult": (I, [P, P, P]),
-    "gbpa_multigrid_create": (I, [P, I, P, P, P, D, I, I, ctypes.POINTER(P)]),
+    "gbpa_multigrid_create": (I, [P, I, P, P, P, D, I, I, P, ctypes.POINTER(P)]),
     "gbpa_multigrid_destroy": (I, [P]),
     "gbpa_multigrid_mult": (I, [P, P, P]),
     "gbpa_pcg_solve_mg": (I, [P, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),

@@ -12,7 +12,8 @@
 //                level 0 solved by CG to a relative tolerance
 //   outer solve  CGSolver::Mult (linalg/solvers.cpp:869-1050) preconditioned
 //                by the V-cycle
-// Levels are FP64-vector operators (GBPA_F64 or GBPA_F64X2 arithmetic).
+// Levels are operators with FP64 vectors (GBPA_F64, GBPA_F64X2) or all with
+// FP32 vectors (GBPA_F32: the V-cycle then preconditions the FP64 CG in FP32).
 //
 // GPU layout. The prolongation writes every fine dof exactly once, from its
 // mask-owning element slot (no scatter, no atomics); the restriction writes
@@ -47,19 +48,21 @@ __global__ void mg_owner_kernel(int ndofs, const int *__restrict__ offsets, cons
 
 // Prolongation: one element per z-slice of the block, threads (qx, qy).
 // Bi (df, dc) column-major: Bi[q + df * d].
-__global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restrict__ Bi,
+template <typename T>
+__global__ void mg_prolong_kernel(int ne, int dc, int df, const T *__restrict__ Bi,
                                   const int *__restrict__ gm_c, const int *__restrict__ gm_f,
-                                  const unsigned char *__restrict__ own, const double *__restrict__ xc,
-                                  double *__restrict__ yf)
+                                  const unsigned char *__restrict__ own, const T *__restrict__ xc,
+                                  T *__restrict__ yf)
 {
-   extern __shared__ double sm[];
+   extern __shared__ __align__(16) unsigned char sm_raw[];
+   T *sm = reinterpret_cast<T *>(sm_raw);
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
    const int e = blockIdx.x * blockDim.z + tz;
    const int dc3 = dc * dc * dc, nthr = df * df * blockDim.z, tid = tx + df * (ty + df * tz);
-   double *sB = sm;                                     // [df][dc]
+   T *sB = sm;                                          // [df][dc]
    const int per = dc3 + dc * dc * df + dc * df * df;   // X | T1 | T2
-   double *X = sm + df * dc + tz * per;
-   double *T1 = X + dc3, *T2 = T1 + dc * dc * df;
+   T *X = sm + df * dc + tz * per;
+   T *T1 = X + dc3, *T2 = T1 + dc * dc * df;
    for (int i = tid; i < df * dc; i += nthr) { sB[i] = Bi[i]; }
    const bool active = e < ne;
    if (active)
@@ -67,7 +70,7 @@ __global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restri
       for (int i = tx + df * ty; i < dc3; i += df * df)
       {
          const int g = gm_c[(long long)e * dc3 + i];
-         const double v = xc[g >= 0 ? g : -1 - g];
+         const T v = xc[g >= 0 ? g : -1 - g];
          X[i] = g >= 0 ? v : -v;
       }
    }
@@ -77,7 +80,7 @@ __global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restri
    {
       for (int dz = 0; dz < dc; ++dz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int dx = 0; dx < dc; ++dx) { s += sB[tx + df * dx] * X[dx + dc * (ty + dc * dz)]; }
          T1[tx + df * (ty + dc * dz)] = s;
       }
@@ -88,7 +91,7 @@ __global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restri
    {
       for (int dz = 0; dz < dc; ++dz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int dy = 0; dy < dc; ++dy) { s += sB[ty + df * dy] * T1[tx + df * (dy + dc * dz)]; }
          T2[tx + df * (ty + df * dz)] = s;
       }
@@ -101,7 +104,7 @@ __global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restri
       const int df3 = df * df * df;
       for (int qz = 0; qz < df; ++qz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int dz = 0; dz < dc; ++dz) { s += sB[qz + df * dz] * T2[tx + df * (ty + df * dz)]; }
          const long long slot = (long long)e * df3 + tx + df * (ty + df * qz);
          if (own[slot])
@@ -115,19 +118,21 @@ __global__ void mg_prolong_kernel(int ne, int dc, int df, const double *__restri
 
 // Restriction (the transpose) into a coarse E-vector: X = mask .* R_f x_f,
 // then the transposed contractions; threads (qx, qy) of the fine slab.
-__global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restrict__ Bi,
+template <typename T>
+__global__ void mg_restrict_kernel(int ne, int dc, int df, const T *__restrict__ Bi,
                                    const int *__restrict__ gm_f, const unsigned char *__restrict__ own,
-                                   const double *__restrict__ xf, double *__restrict__ yEc)
+                                   const T *__restrict__ xf, T *__restrict__ yEc)
 {
-   extern __shared__ double sm[];
+   extern __shared__ __align__(16) unsigned char sm_raw[];
+   T *sm = reinterpret_cast<T *>(sm_raw);
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
    const int e = blockIdx.x * blockDim.z + tz;
    const int df3 = df * df * df, dc3 = dc * dc * dc, nthr = df * df * blockDim.z;
    const int tid = tx + df * (ty + df * tz);
-   double *sB = sm;
+   T *sB = sm;
    const int per = df3 + df * df * dc + df * dc * dc;   // X | T1 | T2
-   double *X = sm + df * dc + tz * per;
-   double *T1 = X + df3, *T2 = T1 + df * df * dc;
+   T *X = sm + df * dc + tz * per;
+   T *T1 = X + df3, *T2 = T1 + df * df * dc;
    for (int i = tid; i < df * dc; i += nthr) { sB[i] = Bi[i]; }
    const bool active = e < ne;
    if (active)
@@ -135,11 +140,11 @@ __global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restr
       for (int i = tx + df * ty; i < df3; i += df * df)
       {
          const long long slot = (long long)e * df3 + i;
-         double v = 0.0;
+         T v = T(0);
          if (own[slot])
          {
             const int g = gm_f[slot];
-            const double a = xf[g >= 0 ? g : -1 - g];
+            const T a = xf[g >= 0 ? g : -1 - g];
             v = g >= 0 ? a : -a;
          }
          X[i] = v;
@@ -151,7 +156,7 @@ __global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restr
    {
       for (int qz = 0; qz < df; ++qz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int qx = 0; qx < df; ++qx) { s += sB[qx + df * tx] * X[qx + df * (ty + df * qz)]; }
          T1[tx + dc * (ty + df * qz)] = s;
       }
@@ -162,7 +167,7 @@ __global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restr
    {
       for (int qz = 0; qz < df; ++qz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int qy = 0; qy < df; ++qy) { s += sB[qy + df * ty] * T1[tx + dc * (qy + df * qz)]; }
          T2[tx + dc * (ty + dc * qz)] = s;
       }
@@ -173,7 +178,7 @@ __global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restr
    {
       for (int dz = 0; dz < dc; ++dz)
       {
-         double s = 0.0;
+         T s = T(0);
          for (int qz = 0; qz < df; ++qz) { s += sB[qz + df * dz] * T2[tx + dc * (ty + dc * qz)]; }
          yEc[(long long)e * dc3 + tx + dc * (ty + dc * dz)] = s;
       }
@@ -181,18 +186,20 @@ __global__ void mg_restrict_kernel(int ne, int dc, int df, const double *__restr
 }
 
 // ---- vector kernels of the smoother, the cycle and the outer CG
-__global__ void mg_scale_kernel(int64_t n, const double *__restrict__ d, const double *__restrict__ x,
-                                double *__restrict__ r, double *__restrict__ y, double c, int first)
+template <typename T>
+__global__ void mg_scale_kernel(int64_t n, const T *__restrict__ d, const T *__restrict__ x,
+                                T *__restrict__ r, T *__restrict__ y, T c, int first)
 {
    // r = d .* x; y = c r (first) or y += c r
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
    {
-      const double v = d[i] * x[i];
+      const T v = d[i] * x[i];
       r[i] = v;
       y[i] = first ? c * v : y[i] + c * v;
    }
 }
-__global__ void mg_mul_kernel(int64_t n, const double *__restrict__ d, double *__restrict__ y)
+template <typename T>
+__global__ void mg_mul_kernel(int64_t n, const T *__restrict__ d, T *__restrict__ y)
 {
    // y .*= d
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -200,7 +207,8 @@ __global__ void mg_mul_kernel(int64_t n, const double *__restrict__ d, double *_
       y[i] *= d[i];
    }
 }
-__global__ void mg_axpby_kernel(int64_t n, double a, const double *x, double b, double *y)
+template <typename T>
+__global__ void mg_axpby_kernel(int64_t n, T a, const T *x, T b, T *y)
 {
    // y = a x + b y (x may alias y)
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -208,7 +216,8 @@ __global__ void mg_axpby_kernel(int64_t n, double a, const double *x, double b, 
       y[i] = a * x[i] + b * y[i];
    }
 }
-__global__ void mg_fill_kernel(int64_t n, double v, double *__restrict__ y)
+template <typename T>
+__global__ void mg_fill_kernel(int64_t n, T v, T *__restrict__ y)
 {
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
    {
@@ -216,7 +225,8 @@ __global__ void mg_fill_kernel(int64_t n, double v, double *__restrict__ y)
    }
 }
 // splitmix64 at counter i of the stream seeded with `seed`, in [0, 1)
-__global__ void mg_random_kernel(int64_t n, unsigned long long seed, double *__restrict__ y)
+template <typename T>
+__global__ void mg_random_kernel(int64_t n, unsigned long long seed, T *__restrict__ y)
 {
    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
    {
@@ -224,17 +234,35 @@ __global__ void mg_random_kernel(int64_t n, unsigned long long seed, double *__r
       z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
       z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
       z ^= z >> 31;
-      y[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+      y[i] = (T)((double)(z >> 11) * (1.0 / 9007199254740992.0));
    }
 }
-__global__ void mg_dinv_kernel(int n, const double *__restrict__ diag, double *__restrict__ dinv)
+template <typename T>
+__global__ void mg_dinv_kernel(int n, const double *__restrict__ diag, T *__restrict__ dinv)
 {
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
    {
-      dinv[i] = 1.0 / diag[i];
+      dinv[i] = (T)(1.0 / diag[i]);
    }
 }
-__global__ void mg_set_ess_kernel(int n_ess, const int *__restrict__ ess, double v, double *__restrict__ y)
+template <typename T>
+__global__ void mg_convert_kernel(int64_t n, const double *__restrict__ x, T *__restrict__ y)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+   {
+      y[i] = (T)x[i];
+   }
+}
+template <typename T>
+__global__ void mg_widen_kernel(int64_t n, const T *__restrict__ x, double *__restrict__ y)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+   {
+      y[i] = (double)x[i];
+   }
+}
+template <typename T>
+__global__ void mg_set_ess_kernel(int n_ess, const int *__restrict__ ess, T v, T *__restrict__ y)
 {
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_ess; i += gridDim.x * blockDim.x)
    {
@@ -253,46 +281,45 @@ struct gbpa_ptransfer
 {
    gbpa_ctx *ctx = nullptr;
    int ne = 0, dc = 0, df = 0, ndofs_c = 0, ndofs_f = 0;
+   bool f32 = false;                // vectors in float (GBPA_F32) or double
    const int *gm_c = nullptr, *off_c = nullptr, *ind_c = nullptr, *gm_f = nullptr;
-   double *Bi = nullptr;            // device copy (df, dc)
+   void *Bi = nullptr;              // device copy (df, dc) in the vector type
    unsigned char *own = nullptr;    // fine slot owners
-   double *yEc = nullptr;           // coarse E-vector scratch
+   void *yEc = nullptr;             // coarse E-vector scratch
 };
 
 struct gbpa_chebyshev
 {
    gbpa_operator *A = nullptr;
+   bool f32 = false;
    int order = 0;
    double lambda = 0.0;
    double coeffs[16] = {0};
-   double *dinv = nullptr, *res = nullptr, *h = nullptr;
+   void *dinv = nullptr, *res = nullptr, *h = nullptr;
 };
 
 struct gbpa_multigrid
 {
    gbpa_ctx *ctx = nullptr;
    int nl = 0;
+   bool f32 = false;
    std::vector<gbpa_operator *> ops;
    std::vector<gbpa_chebyshev *> sm;
    std::vector<gbpa_ptransfer *> P;
    double coarse_tol = 1e-2;
    int coarse_max = 200;
-   double *coarse_dinv = nullptr;      // level-0 CG preconditioner: ones (plain CG) or Jacobi
-   std::vector<double *> X, Y, R, Z;   // per level
+   void *coarse_dinv = nullptr;        // level-0 CG preconditioner: ones (plain CG) or Jacobi
+   std::vector<void *> X, Y, R, Z;     // per level, in the levels' vector type
    double *d_dot = nullptr;
    int64_t coarse_iterations = 0;
 };
 
 namespace
 {
-int ptransfer_smem(int dc, int df, int nbz, bool prolong, size_t *bytes)
-{
-   const int per = prolong ? dc * dc * dc + dc * dc * df + dc * df * df
-                           : df * df * df + df * df * dc + df * dc * dc;
-   *bytes = sizeof(double) * ((size_t)df * dc + (size_t)nbz * per);
-   return GBPA_SUCCESS;
-}
+bool fp32_vectors(const gbpa_operator *A) { return A->d.precision == GBPA_F32; }
+size_t vbytes(bool f32) { return f32 ? sizeof(float) : sizeof(double); }
 int transfer_nbz(int df) { return std::max(1, 128 / (df * df)); }
+int dev_alloc(void **p, size_t bytes) { return check_cuda(cudaMalloc(p, bytes > 0 ? bytes : 16), "cudaMalloc"); }
 
 // Chebyshev coefficients: 1 - t p(t) = T_k((theta - t)/delta) / T_k(theta/delta)
 // on [0.3, 1.2] * lambda (linalg/solvers.cpp:552-616 lists the closed forms
@@ -318,44 +345,227 @@ void chebyshev_coeffs(int order, double lambda, double *c)
       std::copy(P, P + 16, Pm);
       std::copy(Pn, Pn + 16, P);
    }
-   const double *T = P;
-   for (int j = 1; j <= order; ++j) { c[j - 1] = -T[j] / T[0]; }
+   for (int j = 1; j <= order; ++j) { c[j - 1] = -P[j] / P[0]; }
 }
 
-int host_dot(gbpa_ctx *ctx, int64_t n, const double *x, const double *y, double *d_out, double *out)
+template <typename T>
+int host_dot(gbpa_ctx *ctx, int64_t n, const T *x, const T *y, double *d_out, double *out)
 {
-   int rc = launch_dot<double>(ctx, n, x, y, d_out);
+   int rc = launch_dot<T>(ctx, n, x, y, d_out);
    if (!rc) { rc = check_cuda(cudaMemcpyAsync(ctx->h_pinned, d_out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"); }
    if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
    if (!rc) { *out = ctx->h_pinned[0]; }
    return rc;
 }
-
-int axpby(gbpa_ctx *ctx, int64_t n, double a, const double *x, double b, double *y)
-{
-   mg_axpby_kernel<<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, a, x, b, y);
-   return last_launch(ctx, "mg_axpby");
-}
-int fill(gbpa_ctx *ctx, int64_t n, double v, double *y)
+template <typename T>
+int axpby(gbpa_ctx *ctx, int64_t n, double a, const T *x, double b, T *y)
 {
    if (n <= 0) { return GBPA_SUCCESS; }
-   mg_fill_kernel<<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, v, y);
+   mg_axpby_kernel<T><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, (T)a, x, (T)b, y);
+   return last_launch(ctx, "mg_axpby");
+}
+template <typename T>
+int fill(gbpa_ctx *ctx, int64_t n, double v, T *y)
+{
+   if (n <= 0) { return GBPA_SUCCESS; }
+   mg_fill_kernel<T><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, (T)v, y);
    return last_launch(ctx, "mg_fill");
 }
-int dev_alloc(double **p, int64_t n)
+
+// ---- transfer
+template <typename T>
+int ptransfer_mult(gbpa_ptransfer *Tr, const T *xc, T *yf)
 {
-   return check_cuda(cudaMalloc(p, sizeof(double) * (n > 0 ? n : 1)), "cudaMalloc");
+   const int nbz = transfer_nbz(Tr->df);
+   int ne = Tr->ne, dc = Tr->dc, df = Tr->df;
+   const size_t smem = sizeof(T) * ((size_t)df * dc + (size_t)nbz * (dc * dc * dc + dc * dc * df + dc * df * df));
+   const T *Bi = (const T *)Tr->Bi;
+   const int *gc = Tr->gm_c, *gf = Tr->gm_f;
+   const unsigned char *own = Tr->own;
+   void *args[] = {&ne, &dc, &df, (void *)&Bi, (void *)&gc, (void *)&gf, (void *)&own, (void *)&xc, &yf};
+   return launch_generic(Tr->ctx, (const void *)mg_prolong_kernel<T>, dim3((ne + nbz - 1) / nbz), dim3(df, df, nbz),
+                         args, smem, "mg_prolong");
 }
-bool fp64_vectors(const gbpa_operator *A) { return A->d.precision == GBPA_F64 || A->d.precision == GBPA_F64X2; }
+template <typename T>
+int ptransfer_mult_transpose(gbpa_ptransfer *Tr, const T *xf, T *yc)
+{
+   if (Tr->ne == 0) { return fill<T>(Tr->ctx, Tr->ndofs_c, 0.0, yc); }
+   const int nbz = transfer_nbz(Tr->df);
+   int ne = Tr->ne, dc = Tr->dc, df = Tr->df;
+   const size_t smem = sizeof(T) * ((size_t)df * dc + (size_t)nbz * (df * df * df + df * df * dc + df * dc * dc));
+   const T *Bi = (const T *)Tr->Bi;
+   const int *gf = Tr->gm_f;
+   const unsigned char *own = Tr->own;
+   T *yEc = (T *)Tr->yEc;
+   void *args[] = {&ne, &dc, &df, (void *)&Bi, (void *)&gf, (void *)&own, (void *)&xf, &yEc};
+   int rc = launch_generic(Tr->ctx, (const void *)mg_restrict_kernel<T>, dim3((ne + nbz - 1) / nbz),
+                           dim3(df, df, nbz), args, smem, "mg_restrict");
+   if (rc) { return rc; }
+   return launch_csr_scatter<T>(Tr->ctx, Tr->ndofs_c, Tr->off_c, Tr->ind_c, yEc, yc, nullptr, nullptr, false, false);
+}
+
+// ---- Chebyshev: OperatorChebyshevSmoother::Mult (linalg/solvers.cpp:619-656):
+// res = x; y = 0; for k: (k > 0: res = A res) res .*= dinv; y += c_k res
+template <typename T>
+int chebyshev_mult(gbpa_chebyshev *S, const T *x, T *y)
+{
+   gbpa_ctx *ctx = S->A->ctx;
+   const int64_t n = S->A->d.ndofs;
+   if (n == 0) { return GBPA_SUCCESS; }
+   T *dinv = (T *)S->dinv, *res = (T *)S->res, *h = (T *)S->h;
+   int rc = GBPA_SUCCESS;
+   for (int k = 0; k < S->order && !rc; ++k)
+   {
+      const T *src = x;
+      if (k > 0)
+      {
+         rc = gbpa_operator_mult(S->A, res, h);
+         src = h;
+      }
+      if (rc) { break; }
+      mg_scale_kernel<T><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, dinv, src, res, y, (T)S->coeffs[k], k == 0);
+      rc = last_launch(ctx, "mg_scale");
+   }
+   return rc;
+}
+
+// PowerMethod::EstimateLargestEigenvalue (linalg/operator.cpp:886-942) on
+// D^-1 A: v0 random, normalised each step, lambda = (v0, D^-1 A v0)
+template <typename T>
+int power_method(gbpa_chebyshev *S, int steps, double tol, unsigned long long seed, double *out)
+{
+   gbpa_operator *A = S->A;
+   gbpa_ctx *ctx = A->ctx;
+   const int64_t n = A->d.ndofs;
+   T *v0 = (T *)S->res, *v1 = (T *)S->h;
+   double *d_s = nullptr;
+   int rc = dev_alloc((void **)&d_s, sizeof(double));
+   if (!rc && n > 0)
+   {
+      mg_random_kernel<T><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, seed, v0);
+      rc = last_launch(ctx, "mg_random");
+   }
+   double lam = 1.0;
+   for (int it = 0; it < steps && !rc; ++it)
+   {
+      double nrm2 = 0.0, ln = 0.0;
+      rc = host_dot<T>(ctx, n, v0, v0, d_s, &nrm2);
+      if (!rc) { rc = axpby<T>(ctx, n, 0.0, v0, 1.0 / std::sqrt(nrm2), v0); }
+      if (!rc) { rc = gbpa_operator_mult(A, v0, v1); }
+      if (!rc)
+      {
+         mg_mul_kernel<T><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, (const T *)S->dinv, v1);
+         rc = last_launch(ctx, "mg_mul");
+      }
+      if (!rc) { rc = host_dot<T>(ctx, n, v0, v1, d_s, &ln); }
+      if (rc) { break; }
+      const double diff = std::fabs((ln - lam) / lam);
+      lam = ln;
+      std::swap(v0, v1);
+      if (diff < tol) { break; }
+   }
+   cudaFree(d_s);
+   *out = lam;
+   return rc;
+}
+
+template <typename T>
+int coarse_solve(gbpa_multigrid *M, gbpa_solve_info *info);
+template <>
+int coarse_solve<double>(gbpa_multigrid *M, gbpa_solve_info *info)
+{
+   return gbpa_pcg_solve(M->ops[0], (const double *)M->coarse_dinv, (const double *)M->X[0], (double *)M->Y[0],
+                         M->coarse_tol, 0.0, M->coarse_max, 0, info);
+}
+template <>
+int coarse_solve<float>(gbpa_multigrid *M, gbpa_solve_info *info)
+{
+   return pcg_solve_f32(M->ops[0], (const float *)M->coarse_dinv, (const float *)M->X[0], (float *)M->Y[0],
+                        M->coarse_tol, 0.0, M->coarse_max, info);
+}
+
+// MultigridBase::Cycle (fem/multigrid.cpp:179-239), V(1,1); X[level] holds
+// the right-hand side, Y[level] receives the correction.
+template <typename T>
+int mg_cycle(gbpa_multigrid *M, int level)
+{
+   gbpa_ctx *ctx = M->ctx;
+   gbpa_operator *A = M->ops[level];
+   const int64_t n = A->d.ndofs;
+   T *X = (T *)M->X[level], *Y = (T *)M->Y[level], *R = (T *)M->R[level], *Z = (T *)M->Z[level];
+   if (level == 0)
+   {
+      // CGSolver to the coarse tolerance: without preconditioner (plain CG is
+      // Jacobi-PCG with a unit inverse diagonal) or with Jacobi
+      gbpa_solve_info info;
+      const int rc = coarse_solve<T>(M, &info);
+      M->coarse_iterations += info.iterations;
+      return rc == GBPA_ERR_NOT_CONVERGED ? GBPA_SUCCESS : rc;
+   }
+   gbpa_operator *Ac = M->ops[level - 1];
+   T *Xc = (T *)M->X[level - 1], *Yc = (T *)M->Y[level - 1];
+   // pre-smooth from a zero guess: Y = S X
+   int rc = chebyshev_mult<T>(M->sm[level], X, Y);
+   // residual R = X - A Y, restricted to the coarse right-hand side
+   if (!rc) { rc = gbpa_operator_mult(A, Y, R); }
+   if (!rc) { rc = axpby<T>(ctx, n, 1.0, X, -1.0, R); }
+   if (!rc) { rc = ptransfer_mult_transpose<T>(M->P[level - 1], R, Xc); }
+   if (!rc) { rc = fill<T>(ctx, Ac->d.ndofs, 0.0, Yc); }
+   if (!rc) { rc = mg_cycle<T>(M, level - 1); }
+   // prolongate and add
+   if (!rc) { rc = ptransfer_mult<T>(M->P[level - 1], Yc, Z); }
+   if (!rc) { rc = axpby<T>(ctx, n, 1.0, Z, 1.0, Y); }
+   // post-smooth: Y += S (X - A Y)
+   if (!rc) { rc = gbpa_operator_mult(A, Y, R); }
+   if (!rc) { rc = axpby<T>(ctx, n, 1.0, X, -1.0, R); }
+   if (!rc) { rc = chebyshev_mult<T>(M->sm[level], R, Z); }
+   if (!rc) { rc = axpby<T>(ctx, n, 1.0, Z, 1.0, Y); }
+   return rc;
+}
+
+// y = V-cycle(x) with x, y in the levels' vector type
+template <typename T>
+int mg_mult(gbpa_multigrid *M, const T *x, T *y)
+{
+   const int top = M->nl - 1;
+   const int64_t n = M->ops[top]->d.ndofs;
+   int rc = check_cuda(cudaMemcpyAsync(M->X[top], x, sizeof(T) * n, cudaMemcpyDeviceToDevice, M->ctx->stream), "copy");
+   if (!rc) { rc = fill<T>(M->ctx, n, 0.0, (T *)M->Y[top]); }
+   if (!rc) { rc = mg_cycle<T>(M, top); }
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(y, M->Y[top], sizeof(T) * n, cudaMemcpyDeviceToDevice, M->ctx->stream), "copy"); }
+   return rc;
+}
+
+// z = V-cycle(r) for FP64 vectors r, z whatever the levels' type (FP32
+// levels: r narrowed into the top level's right-hand side, the correction
+// widened back)
+int mg_precondition(gbpa_multigrid *M, const double *r, double *z)
+{
+   if (!M->f32) { return mg_mult<double>(M, r, z); }
+   const int top = M->nl - 1;
+   const int64_t n = M->ops[top]->d.ndofs;
+   gbpa_ctx *ctx = M->ctx;
+   mg_convert_kernel<float><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, r, (float *)M->X[top]);
+   int rc = last_launch(ctx, "mg_convert");
+   if (!rc) { rc = fill<float>(ctx, n, 0.0, (float *)M->Y[top]); }
+   if (!rc) { rc = mg_cycle<float>(M, top); }
+   if (!rc)
+   {
+      mg_widen_kernel<float><<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, (const float *)M->Y[top], z);
+      rc = last_launch(ctx, "mg_widen");
+   }
+   return rc;
+}
 } // namespace
 
 // ------------------------------------------------------------ p-transfer
 extern "C" int gbpa_ptransfer_create(gbpa_ctx_t ctx, int ne, int d1d_c, int ndofs_c, const int *gather_map_c,
                                      const int *offsets_c, const int *indices_c, int d1d_f, int ndofs_f,
                                      const int *gather_map_f, const int *offsets_f, const int *indices_f,
-                                     const double *Bi, gbpa_ptransfer_t *out)
+                                     const double *Bi, int precision, gbpa_ptransfer_t *out)
 {
    if (!ctx || !out || ne < 0 || ndofs_c < 0 || ndofs_f < 0 || d1d_c < 1 || d1d_f < 1) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (precision != GBPA_F64 && precision != GBPA_F32) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (d1d_c > MG_MAX_1D || d1d_f > MG_MAX_1D) { return GBPA_ERR_UNSUPPORTED; }
    if (ne > 0 && (!gather_map_c || !offsets_c || !indices_c || !gather_map_f || !offsets_f || !indices_f || !Bi))
    {
@@ -364,19 +574,23 @@ extern "C" int gbpa_ptransfer_create(gbpa_ctx_t ctx, int ne, int d1d_c, int ndof
    gbpa_ptransfer *T = new (std::nothrow) gbpa_ptransfer;
    if (!T) { return GBPA_ERR_OUT_OF_MEMORY; }
    T->ctx = ctx; T->ne = ne; T->dc = d1d_c; T->df = d1d_f; T->ndofs_c = ndofs_c; T->ndofs_f = ndofs_f;
+   T->f32 = precision == GBPA_F32;
    T->gm_c = gather_map_c; T->off_c = offsets_c; T->ind_c = indices_c; T->gm_f = gather_map_f;
    const int64_t nf = (int64_t)ne * d1d_f * d1d_f * d1d_f, nc = (int64_t)ne * d1d_c * d1d_c * d1d_c;
-   int rc = dev_alloc(&T->Bi, (int64_t)d1d_f * d1d_c);
-   if (!rc) { rc = check_cuda(cudaMemcpyAsync(T->Bi, Bi, sizeof(double) * d1d_f * d1d_c, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
-   if (!rc) { rc = check_cuda(cudaMalloc(&T->own, nf > 0 ? nf : 1), "cudaMalloc"); }
+   const int nb = d1d_f * d1d_c;
+   std::vector<float> b32(Bi ? nb : 0);
+   for (int i = 0; Bi && i < nb; ++i) { b32[i] = (float)Bi[i]; }
+   const void *src = T->f32 ? (const void *)b32.data() : (const void *)Bi;
+   int rc = dev_alloc(&T->Bi, vbytes(T->f32) * nb);
+   if (!rc && Bi) { rc = check_cuda(cudaMemcpy(T->Bi, src, vbytes(T->f32) * nb, cudaMemcpyHostToDevice), "copy"); }
+   if (!rc) { rc = dev_alloc((void **)&T->own, nf); }
    if (!rc) { rc = check_cuda(cudaMemsetAsync(T->own, 0, nf > 0 ? nf : 1, ctx->stream), "memset"); }
-   if (!rc) { rc = dev_alloc(&T->yEc, nc); }
+   if (!rc) { rc = dev_alloc(&T->yEc, vbytes(T->f32) * nc); }
    if (!rc && ndofs_f > 0)
    {
       mg_owner_kernel<<<grid_for(ndofs_f, 256), 256, 0, ctx->stream>>>(ndofs_f, offsets_f, indices_f, T->own);
       rc = last_launch(ctx, "mg_owner");
    }
-   if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }   // Bi is host memory
    if (rc) { gbpa_ptransfer_destroy(T); return rc; }
    *out = T;
    return GBPA_SUCCESS;
@@ -391,40 +605,19 @@ extern "C" int gbpa_ptransfer_destroy(gbpa_ptransfer_t T)
    return GBPA_SUCCESS;
 }
 
-extern "C" int gbpa_ptransfer_mult(gbpa_ptransfer_t T, const double *xc, double *yf)
+extern "C" int gbpa_ptransfer_mult(gbpa_ptransfer_t T, const void *xc, void *yf)
 {
    if (!T || (T->ne > 0 && (!xc || !yf))) { return GBPA_ERR_INVALID_ARGUMENT; }
    if (T->ne == 0) { return GBPA_SUCCESS; }
-   const int nbz = transfer_nbz(T->df);
-   size_t smem = 0;
-   ptransfer_smem(T->dc, T->df, nbz, true, &smem);
-   int ne = T->ne, dc = T->dc, df = T->df;
-   const double *Bi = T->Bi;
-   const int *gc = T->gm_c, *gf = T->gm_f;
-   const unsigned char *own = T->own;
-   void *args[] = {&ne, &dc, &df, (void *)&Bi, (void *)&gc, (void *)&gf, (void *)&own, (void *)&xc, &yf};
-   return launch_generic(T->ctx, (const void *)mg_prolong_kernel, dim3((ne + nbz - 1) / nbz), dim3(df, df, nbz),
-                         args, smem, "mg_prolong");
+   return T->f32 ? ptransfer_mult<float>(T, (const float *)xc, (float *)yf)
+                 : ptransfer_mult<double>(T, (const double *)xc, (double *)yf);
 }
 
-extern "C" int gbpa_ptransfer_mult_transpose(gbpa_ptransfer_t T, const double *xf, double *yc)
+extern "C" int gbpa_ptransfer_mult_transpose(gbpa_ptransfer_t T, const void *xf, void *yc)
 {
    if (!T || (T->ne > 0 && (!xf || !yc))) { return GBPA_ERR_INVALID_ARGUMENT; }
-   if (T->ne == 0) { return fill(T->ctx, T->ndofs_c, 0.0, yc); }
-   const int nbz = transfer_nbz(T->df);
-   size_t smem = 0;
-   ptransfer_smem(T->dc, T->df, nbz, false, &smem);
-   int ne = T->ne, dc = T->dc, df = T->df;
-   const double *Bi = T->Bi;
-   const int *gf = T->gm_f;
-   const unsigned char *own = T->own;
-   double *yEc = T->yEc;
-   void *args[] = {&ne, &dc, &df, (void *)&Bi, (void *)&gf, (void *)&own, (void *)&xf, &yEc};
-   int rc = launch_generic(T->ctx, (const void *)mg_restrict_kernel, dim3((ne + nbz - 1) / nbz), dim3(df, df, nbz),
-                           args, smem, "mg_restrict");
-   if (rc) { return rc; }
-   return launch_csr_scatter<double>(T->ctx, T->ndofs_c, T->off_c, T->ind_c, T->yEc, yc, nullptr, nullptr, false,
-                                     false);
+   return T->f32 ? ptransfer_mult_transpose<float>(T, (const float *)xf, (float *)yc)
+                 : ptransfer_mult_transpose<double>(T, (const double *)xf, (double *)yc);
 }
 
 // --------------------------------------------------------------- Chebyshev
@@ -436,58 +629,32 @@ extern "C" int gbpa_chebyshev_create(gbpa_operator_t A, const double *diag, int 
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
-   if (!fp64_vectors(A)) { return GBPA_ERR_UNSUPPORTED; }
    gbpa_ctx *ctx = A->ctx;
    const int n = A->d.ndofs;
    gbpa_chebyshev *S = new (std::nothrow) gbpa_chebyshev;
    if (!S) { return GBPA_ERR_OUT_OF_MEMORY; }
-   S->A = A; S->order = order;
-   int rc = dev_alloc(&S->dinv, n);
-   if (!rc) { rc = dev_alloc(&S->res, n); }
-   if (!rc) { rc = dev_alloc(&S->h, n); }
+   S->A = A; S->order = order; S->f32 = fp32_vectors(A);
+   const size_t vb = vbytes(S->f32) * (size_t)n;
+   int rc = dev_alloc(&S->dinv, vb);
+   if (!rc) { rc = dev_alloc(&S->res, vb); }
+   if (!rc) { rc = dev_alloc(&S->h, vb); }
    // dinv = 1/diag, 1 on the essential dofs (linalg/solvers.cpp:540-550)
    if (!rc && n > 0)
    {
-      mg_dinv_kernel<<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, diag, S->dinv);
+      if (S->f32) { mg_dinv_kernel<float><<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, diag, (float *)S->dinv); }
+      else { mg_dinv_kernel<double><<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, diag, (double *)S->dinv); }
       rc = last_launch(ctx, "mg_dinv");
    }
    if (!rc && A->d.n_ess > 0)
    {
-      mg_set_ess_kernel<<<grid_for(A->d.n_ess, 256), 256, 0, ctx->stream>>>(A->d.n_ess, A->d.ess, 1.0, S->dinv);
+      if (S->f32) { mg_set_ess_kernel<float><<<grid_for(A->d.n_ess, 256), 256, 0, ctx->stream>>>(A->d.n_ess, A->d.ess, 1.0f, (float *)S->dinv); }
+      else { mg_set_ess_kernel<double><<<grid_for(A->d.n_ess, 256), 256, 0, ctx->stream>>>(A->d.n_ess, A->d.ess, 1.0, (double *)S->dinv); }
       rc = last_launch(ctx, "mg_set_ess");
    }
    if (!rc && max_eig <= 0.0)
    {
-      // PowerMethod on D^-1 A (linalg/operator.cpp:886-942): v0 random,
-      // normalised each step, lambda = (v0, D^-1 A v0)
-      double *v0 = S->res, *v1 = S->h, *d_s = nullptr;
-      rc = dev_alloc(&d_s, 1);
-      if (!rc && n > 0)
-      {
-         mg_random_kernel<<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, seed, v0);
-         rc = last_launch(ctx, "mg_random");
-      }
-      double lam = 1.0;
-      for (int it = 0; it < power_iterations && !rc; ++it)
-      {
-         double nrm2 = 0.0, ln = 0.0;
-         rc = host_dot(ctx, n, v0, v0, d_s, &nrm2);
-         if (!rc) { rc = axpby(ctx, n, 0.0, v0, 1.0 / std::sqrt(nrm2), v0); }
-         if (!rc) { rc = gbpa_operator_mult(A, v0, v1); }
-         if (!rc)
-         {
-            mg_mul_kernel<<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, S->dinv, v1);
-            rc = last_launch(ctx, "mg_mul");
-         }
-         if (!rc) { rc = host_dot(ctx, n, v0, v1, d_s, &ln); }
-         if (rc) { break; }
-         const double diff = std::fabs((ln - lam) / lam);
-         lam = ln;
-         std::swap(v0, v1);
-         if (diff < power_tol) { break; }
-      }
-      cudaFree(d_s);
-      max_eig = lam;
+      rc = S->f32 ? power_method<float>(S, power_iterations, power_tol, seed, &max_eig)
+                  : power_method<double>(S, power_iterations, power_tol, seed, &max_eig);
    }
    if (rc) { gbpa_chebyshev_destroy(S); return rc; }
    if (!(max_eig > 0.0) || !std::isfinite(max_eig)) { gbpa_chebyshev_destroy(S); return GBPA_ERR_NOT_FINITE; }
@@ -513,87 +680,96 @@ extern "C" int gbpa_chebyshev_get_max_eig(gbpa_chebyshev_t S, double *max_eig)
    return GBPA_SUCCESS;
 }
 
-// OperatorChebyshevSmoother::Mult (linalg/solvers.cpp:619-656):
-// res = x; y = 0; for k: (k > 0: res = A res) res .*= dinv; y += c_k res
-extern "C" int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const double *x, double *y)
+extern "C" int gbpa_chebyshev_mult(gbpa_chebyshev_t S, const void *x, void *y)
 {
    if (!S || (S->A->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
-   gbpa_ctx *ctx = S->A->ctx;
-   const int64_t n = S->A->d.ndofs;
-   if (n == 0) { return GBPA_SUCCESS; }
-   int rc = GBPA_SUCCESS;
-   for (int k = 0; k < S->order && !rc; ++k)
-   {
-      const double *src = x;
-      if (k > 0)
-      {
-         rc = gbpa_operator_mult(S->A, S->res, S->h);
-         src = S->h;
-      }
-      if (rc) { break; }
-      mg_scale_kernel<<<vgrid(ctx, n), 256, 0, ctx->stream>>>(n, S->dinv, src, S->res, y, S->coeffs[k], k == 0);
-      rc = last_launch(ctx, "mg_scale");
-   }
-   return rc;
+   return S->f32 ? chebyshev_mult<float>(S, (const float *)x, (float *)y)
+                 : chebyshev_mult<double>(S, (const double *)x, (double *)y);
 }
 
 // -------------------------------------------------------------- multigrid
 extern "C" int gbpa_multigrid_create(gbpa_ctx_t ctx, int nlevels, const gbpa_operator_t *ops,
                                      const gbpa_chebyshev_t *smoothers, const gbpa_ptransfer_t *prolongations,
                                      double coarse_rel_tol, int coarse_max_it, int coarse_jacobi,
-                                     gbpa_multigrid_t *out)
+                                     const double *coarse_diag, gbpa_multigrid_t *out)
 {
    if (!ctx || !out || nlevels < 1 || !ops || (nlevels > 1 && (!smoothers || !prolongations)) ||
-       coarse_rel_tol < 0 || coarse_max_it < 0 || (coarse_jacobi != 0 && coarse_jacobi != 1))
+       coarse_rel_tol < 0 || coarse_max_it < 0 || (coarse_jacobi != 0 && coarse_jacobi != 1) || !ops[0])
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
+   const bool f32 = fp32_vectors(ops[0]);
    for (int l = 0; l < nlevels; ++l)
    {
-      if (!ops[l] || ops[l]->ctx != ctx) { return GBPA_ERR_INVALID_ARGUMENT; }
-      if (!fp64_vectors(ops[l])) { return GBPA_ERR_UNSUPPORTED; }
+      if (!ops[l] || ops[l]->ctx != ctx || fp32_vectors(ops[l]) != f32) { return GBPA_ERR_INVALID_ARGUMENT; }
+      if (ops[l]->d.kind != GBPA_DIFFUSION) { return GBPA_ERR_UNSUPPORTED; }
       if (l > 0)
       {
          const gbpa_ptransfer *P = prolongations[l - 1];
-         if (!smoothers[l] || smoothers[l]->A != ops[l] || !P) { return GBPA_ERR_INVALID_ARGUMENT; }
+         if (!smoothers[l] || smoothers[l]->A != ops[l] || !P || P->f32 != f32) { return GBPA_ERR_INVALID_ARGUMENT; }
          if (P->ndofs_c != ops[l - 1]->d.ndofs || P->ndofs_f != ops[l]->d.ndofs) { return GBPA_ERR_INVALID_ARGUMENT; }
       }
    }
+   // the Jacobi coarse CG needs the coarse diagonal: given, or assembled by
+   // an operator with FP64 data
+   if (coarse_jacobi && !coarse_diag && f32) { return GBPA_ERR_INVALID_ARGUMENT; }
    gbpa_multigrid *M = new (std::nothrow) gbpa_multigrid;
    if (!M) { return GBPA_ERR_OUT_OF_MEMORY; }
-   M->ctx = ctx; M->nl = nlevels;
+   M->ctx = ctx; M->nl = nlevels; M->f32 = f32;
    M->coarse_tol = coarse_rel_tol; M->coarse_max = coarse_max_it;
    int rc = GBPA_SUCCESS;
    for (int l = 0; l < nlevels && !rc; ++l)
    {
-      const int64_t n = ops[l]->d.ndofs;
+      const size_t vb = vbytes(f32) * (size_t)ops[l]->d.ndofs;
       M->ops.push_back(ops[l]);
       M->sm.push_back(l > 0 ? smoothers[l] : nullptr);
       if (l > 0) { M->P.push_back(prolongations[l - 1]); }
-      double *x = nullptr, *y = nullptr, *r = nullptr, *z = nullptr;
-      rc = dev_alloc(&x, n);
-      if (!rc) { rc = dev_alloc(&y, n); }
-      if (!rc) { rc = dev_alloc(&r, n); }
-      if (!rc) { rc = dev_alloc(&z, n); }
+      void *x = nullptr, *y = nullptr, *r = nullptr, *z = nullptr;
+      rc = dev_alloc(&x, vb);
+      if (!rc) { rc = dev_alloc(&y, vb); }
+      if (!rc) { rc = dev_alloc(&r, vb); }
+      if (!rc) { rc = dev_alloc(&z, vb); }
       M->X.push_back(x); M->Y.push_back(y); M->R.push_back(r); M->Z.push_back(z);
    }
    const int64_t n0 = ops[0]->d.ndofs;
-   if (!rc) { rc = dev_alloc(&M->coarse_dinv, n0); }
-   if (!rc && !coarse_jacobi) { rc = fill(ctx, n0, 1.0, M->coarse_dinv); }
+   if (!rc) { rc = dev_alloc(&M->coarse_dinv, vbytes(f32) * n0); }
+   if (!rc && !coarse_jacobi)
+   {
+      rc = f32 ? fill<float>(ctx, n0, 1.0, (float *)M->coarse_dinv) : fill<double>(ctx, n0, 1.0, (double *)M->coarse_dinv);
+   }
    if (!rc && coarse_jacobi && n0 > 0)
    {
       // OperatorJacobiSmoother on the coarse constrained operator: its
       // diagonal (1 on the essential dofs), inverted
-      double *diag = nullptr;
-      rc = dev_alloc(&diag, n0);
-      if (!rc) { rc = gbpa_operator_assemble_diagonal(ops[0], diag); }
+      double *diag = nullptr, *dinv64 = nullptr;
+      rc = dev_alloc((void **)&dinv64, sizeof(double) * n0);
+      if (!rc && !coarse_diag)
+      {
+         rc = dev_alloc((void **)&diag, sizeof(double) * n0);
+         if (!rc) { rc = gbpa_operator_assemble_diagonal(ops[0], diag); }
+      }
       if (!rc)
       {
-         rc = gbpa_jacobi_setup(ctx, n0, diag, ops[0]->d.ess, ops[0]->d.n_ess, 1.0, M->coarse_dinv);
+         rc = gbpa_jacobi_setup(ctx, n0, coarse_diag ? coarse_diag : diag, ops[0]->d.ess, ops[0]->d.n_ess, 1.0,
+                                dinv64);
       }
-      cudaFree(diag);
+      if (!rc)
+      {
+         if (f32)
+         {
+            mg_convert_kernel<float><<<vgrid(ctx, n0), 256, 0, ctx->stream>>>(n0, dinv64, (float *)M->coarse_dinv);
+            rc = last_launch(ctx, "mg_convert");
+         }
+         else
+         {
+            rc = check_cuda(cudaMemcpyAsync(M->coarse_dinv, dinv64, sizeof(double) * n0, cudaMemcpyDeviceToDevice,
+                                            ctx->stream), "copy");
+         }
+      }
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+      cudaFree(diag); cudaFree(dinv64);
    }
-   if (!rc) { rc = dev_alloc(&M->d_dot, 1); }
+   if (!rc) { rc = dev_alloc((void **)&M->d_dot, sizeof(double)); }
    if (rc) { gbpa_multigrid_destroy(M); return rc; }
    *out = M;
    return GBPA_SUCCESS;
@@ -603,83 +779,41 @@ extern "C" int gbpa_multigrid_destroy(gbpa_multigrid_t M)
 {
    if (!M) { return GBPA_SUCCESS; }
    cudaStreamSynchronize(M->ctx->stream);
-   for (double *p : M->X) { cudaFree(p); }
-   for (double *p : M->Y) { cudaFree(p); }
-   for (double *p : M->R) { cudaFree(p); }
-   for (double *p : M->Z) { cudaFree(p); }
+   for (void *p : M->X) { cudaFree(p); }
+   for (void *p : M->Y) { cudaFree(p); }
+   for (void *p : M->R) { cudaFree(p); }
+   for (void *p : M->Z) { cudaFree(p); }
    cudaFree(M->coarse_dinv); cudaFree(M->d_dot);
    delete M;
    return GBPA_SUCCESS;
 }
 
-namespace
+extern "C" int gbpa_multigrid_mult(gbpa_multigrid_t M, const void *x, void *y)
 {
-// MultigridBase::Cycle (fem/multigrid.cpp:179-239), V(1,1); X[level] holds
-// the right-hand side, Y[level] receives the correction.
-int mg_cycle(gbpa_multigrid *M, int level)
-{
-   gbpa_ctx *ctx = M->ctx;
-   gbpa_operator *A = M->ops[level];
-   const int64_t n = A->d.ndofs;
-   if (level == 0)
-   {
-      // CGSolver to the coarse tolerance: without preconditioner (plain CG is
-      // Jacobi-PCG with a unit inverse diagonal) or with Jacobi
-      gbpa_solve_info info;
-      int rc = gbpa_pcg_solve(A, M->coarse_dinv, M->X[0], M->Y[0], M->coarse_tol, 0.0, M->coarse_max, 0, &info);
-      M->coarse_iterations += info.iterations;
-      return rc == GBPA_ERR_NOT_CONVERGED ? GBPA_SUCCESS : rc;
-   }
-   gbpa_operator *Ac = M->ops[level - 1];
-   // pre-smooth from a zero guess: Y = S X
-   int rc = gbpa_chebyshev_mult(M->sm[level], M->X[level], M->Y[level]);
-   // residual R = X - A Y, restricted to the coarse right-hand side
-   if (!rc) { rc = gbpa_operator_mult(A, M->Y[level], M->R[level]); }
-   if (!rc) { rc = axpby(ctx, n, 1.0, M->X[level], -1.0, M->R[level]); }
-   if (!rc) { rc = gbpa_ptransfer_mult_transpose(M->P[level - 1], M->R[level], M->X[level - 1]); }
-   if (!rc) { rc = fill(ctx, Ac->d.ndofs, 0.0, M->Y[level - 1]); }
-   if (!rc) { rc = mg_cycle(M, level - 1); }
-   // prolongate and add
-   if (!rc) { rc = gbpa_ptransfer_mult(M->P[level - 1], M->Y[level - 1], M->Z[level]); }
-   if (!rc) { rc = axpby(ctx, n, 1.0, M->Z[level], 1.0, M->Y[level]); }
-   // post-smooth: Y += S (X - A Y)
-   if (!rc) { rc = gbpa_operator_mult(A, M->Y[level], M->R[level]); }
-   if (!rc) { rc = axpby(ctx, n, 1.0, M->X[level], -1.0, M->R[level]); }
-   if (!rc) { rc = gbpa_chebyshev_mult(M->sm[level], M->R[level], M->Z[level]); }
-   if (!rc) { rc = axpby(ctx, n, 1.0, M->Z[level], 1.0, M->Y[level]); }
-   return rc;
-}
-} // namespace
-
-extern "C" int gbpa_multigrid_mult(gbpa_multigrid_t M, const double *x, double *y)
-{
-   const int top = M ? M->nl - 1 : 0;
-   if (!M || (M->ops[top]->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
-   const int64_t n = M->ops[top]->d.ndofs;
-   int rc = check_cuda(cudaMemcpyAsync(M->X[top], x, sizeof(double) * n, cudaMemcpyDeviceToDevice, M->ctx->stream),
-                       "copy");
-   if (!rc) { rc = fill(M->ctx, n, 0.0, M->Y[top]); }
-   if (!rc) { rc = mg_cycle(M, top); }
-   if (!rc) { rc = check_cuda(cudaMemcpyAsync(y, M->Y[top], sizeof(double) * n, cudaMemcpyDeviceToDevice, M->ctx->stream), "copy"); }
-   return rc;
+   if (!M || (M->ops[M->nl - 1]->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (M->ops[M->nl - 1]->d.ndofs == 0) { return GBPA_SUCCESS; }
+   return M->f32 ? mg_mult<float>(M, (const float *)x, (float *)y)
+                 : mg_mult<double>(M, (const double *)x, (double *)y);
 }
 
 // CGSolver::Mult (linalg/solvers.cpp:869-1050) preconditioned by the V-cycle,
-// zero initial guess; the stopping rule (B r, r) <= max(rel^2 (B r0, r0), abs^2)
+// zero initial guess; the stopping rule (B r, r) <= max(rel^2 (B r0, r0), abs^2).
+// A has FP64 vectors; the multigrid levels may run in FP32 (the V-cycle is
+// then an FP32 preconditioner of the FP64 iteration).
 extern "C" int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const double *b, double *x, double rel_tol,
                                  double abs_tol, int max_it, gbpa_solve_info *info)
 {
-   if (!A || !M || M->ops[M->nl - 1] != A || (A->d.ndofs > 0 && (!b || !x)) || max_it < 0 || rel_tol < 0 ||
-       abs_tol < 0)
+   if (!A || !M || fp32_vectors(A) || A->ctx != M->ctx || M->ops[M->nl - 1]->d.ndofs != A->d.ndofs ||
+       (A->d.ndofs > 0 && (!b || !x)) || max_it < 0 || rel_tol < 0 || abs_tol < 0)
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
    gbpa_ctx *ctx = A->ctx;
    const int64_t n = A->d.ndofs;
    double *r = nullptr, *d = nullptr, *z = nullptr;
-   int rc = dev_alloc(&r, n);
-   if (!rc) { rc = dev_alloc(&d, n); }
-   if (!rc) { rc = dev_alloc(&z, n); }
+   int rc = dev_alloc((void **)&r, sizeof(double) * n);
+   if (!rc) { rc = dev_alloc((void **)&d, sizeof(double) * n); }
+   if (!rc) { rc = dev_alloc((void **)&z, sizeof(double) * n); }
    cudaEvent_t e0, e1;
    cudaEventCreate(&e0); cudaEventCreate(&e1);
    cudaEventRecord(e0, ctx->stream);
@@ -687,10 +821,10 @@ extern "C" int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const do
    int final_iter = 0, converged = 0, status = GBPA_SUCCESS;
    double nom = 0.0, nom0 = 0.0, den = 0.0, betanom = 0.0;
    if (!rc) { rc = check_cuda(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream), "copy"); }
-   if (!rc) { rc = fill(ctx, n, 0.0, x); }
-   if (!rc) { rc = gbpa_multigrid_mult(M, r, z); }
+   if (!rc) { rc = fill<double>(ctx, n, 0.0, x); }
+   if (!rc) { rc = mg_precondition(M, r, z); }
    if (!rc) { rc = check_cuda(cudaMemcpyAsync(d, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream), "copy"); }
-   if (!rc) { rc = host_dot(ctx, n, d, r, M->d_dot, &nom); }
+   if (!rc) { rc = host_dot<double>(ctx, n, d, r, M->d_dot, &nom); }
    nom0 = nom;
    if (!rc)
    {
@@ -702,24 +836,24 @@ extern "C" int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const do
       else
       {
          rc = gbpa_operator_mult(A, d, z);
-         if (!rc) { rc = host_dot(ctx, n, z, d, M->d_dot, &den); }
+         if (!rc) { rc = host_dot<double>(ctx, n, z, d, M->d_dot, &den); }
          final_iter = den == 0.0 ? 0 : max_it;
          for (int i = 1; !rc && den != 0.0;)
          {
             const double alpha = nom / den;
-            rc = axpby(ctx, n, alpha, d, 1.0, x);
-            if (!rc) { rc = axpby(ctx, n, -alpha, z, 1.0, r); }
-            if (!rc) { rc = gbpa_multigrid_mult(M, r, z); }
-            if (!rc) { rc = host_dot(ctx, n, r, z, M->d_dot, &betanom); }
+            rc = axpby<double>(ctx, n, alpha, d, 1.0, x);
+            if (!rc) { rc = axpby<double>(ctx, n, -alpha, z, 1.0, r); }
+            if (!rc) { rc = mg_precondition(M, r, z); }
+            if (!rc) { rc = host_dot<double>(ctx, n, r, z, M->d_dot, &betanom); }
             if (rc) { break; }
             if (!std::isfinite(betanom)) { status = GBPA_ERR_NOT_FINITE; final_iter = i; break; }
             if (betanom < 0.0) { final_iter = i; break; }
             if (betanom <= r0) { converged = 1; final_iter = i; break; }
             if (++i > max_it) { break; }
             const double beta = betanom / nom;
-            rc = axpby(ctx, n, 1.0, z, beta, d);
+            rc = axpby<double>(ctx, n, 1.0, z, beta, d);
             if (!rc) { rc = gbpa_operator_mult(A, d, z); }
-            if (!rc) { rc = host_dot(ctx, n, d, z, M->d_dot, &den); }
+            if (!rc) { rc = host_dot<double>(ctx, n, d, z, M->d_dot, &den); }
             if (!rc && den == 0.0) { final_iter = i; }
             nom = betanom;
          }

@@ -613,6 +613,16 @@ extern "C" int gbpa_pcg_solve(gbpa_operator_t A, const double *dinv, const doubl
    return true_residual(A, b, x, &inf->true_rel_residual);
 }
 
+// FP32 Jacobi-PCG on an FP32 operator (zero initial guess), for callers
+// inside the library (the multigrid coarse solve in FP32).
+int gbpa::pcg_solve_f32(gbpa_operator *A, const float *dinv, const float *b, float *x, double rel_tol,
+                        double abs_tol, int max_it, gbpa_solve_info *info)
+{
+   memset(info, 0, sizeof(*info));
+   if (A->d.ndofs == 0) { info->converged = 1; return GBPA_SUCCESS; }
+   return pcg_run<float>(A, dinv, b, x, rel_tol, abs_tol, max_it, 0, info, nullptr);
+}
+
 extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, const float *dinv32,
                                     const double *b, double *x, double outer_rel_tol,
                                     double inner_rel_tol, int max_outer, int max_inner,

@@ -38,3 +38,9 @@ struct gbpa_operator
    int yEb_nrhs = 0;
 };
 
+namespace gbpa
+{
+// FP32 Jacobi-PCG (CGSolver semantics, zero initial guess) on an FP32 operator.
+int pcg_solve_f32(gbpa_operator *A, const float *dinv, const float *b, float *x, double rel_tol,
+                  double abs_tol, int max_it, gbpa_solve_info *info);
+} // namespace gbpa

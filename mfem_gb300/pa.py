@@ -443,7 +443,7 @@ class TransferOperator:
     orders on the same mesh (TensorProductPRefinementTransferOperator):
     Mult prolongs lfes -> hfes, MultTranspose restricts."""
 
-    def __init__(self, lfes, hfes):
+    def __init__(self, lfes, hfes, precision=_lib.GBPA_F64):
         dev = _dev()
         from . import fem
         Rl, Rh = lfes.GetElementRestriction(), hfes.GetElementRestriction()
@@ -455,6 +455,7 @@ class TransferOperator:
         check(dev.lib.gbpa_ptransfer_create(dev.ctx, lfes.ne, dc, lfes.ndofs, _p(Rl.gather_map), _p(Rl.offsets),
                                             _p(Rl.indices), df, hfes.ndofs, _p(Rh.gather_map), _p(Rh.offsets),
                                             _p(Rh.indices), self.Bi.ctypes.data_as(ctypes.c_void_p),
+                                            _lib.GBPA_F32 if precision == _lib.GBPA_F32 else _lib.GBPA_F64,
                                             ctypes.byref(h)), "ptransfer_create")
         self.handle = h
 
@@ -507,7 +508,7 @@ class Multigrid:
     consecutive levels; level 0 solved by CG to coarse_rel_tol."""
 
     def __init__(self, operators, smoothers, prolongations, coarse_rel_tol=1e-2, coarse_max_it=200,
-                 coarse_jacobi=False):
+                 coarse_jacobi=False, coarse_diag=None):
         dev = _dev()
         nl = len(operators)
         self.operators, self.smoothers, self.prolongations = operators, smoothers, prolongations
@@ -516,7 +517,8 @@ class Multigrid:
         prs = (ctypes.c_void_p * max(nl - 1, 1))(*[P.handle for P in prolongations])
         h = ctypes.c_void_p()
         check(dev.lib.gbpa_multigrid_create(dev.ctx, nl, ops, sms, prs, coarse_rel_tol, coarse_max_it,
-                                            1 if coarse_jacobi else 0, ctypes.byref(h)), "multigrid_create")
+                                            1 if coarse_jacobi else 0, _p(coarse_diag), ctypes.byref(h)),
+              "multigrid_create")
         self.handle = h
 
     def Mult(self, x, y):
@@ -535,14 +537,16 @@ class DiffusionMultigrid(Multigrid):
     per order (Dirichlet on the whole boundary), order-2 Chebyshev smoothers
     with power-method eigenvalue estimates, CG to 1e-2 on the coarsest
     order (coarse_jacobi: Jacobi-preconditioned). precision: the levels'
-    arithmetic (GBPA_F64 or GBPA_F64X2). max_eigs: optional eigenvalue
-    estimates for levels 1.. (else estimated)."""
+    arithmetic (GBPA_F64, GBPA_F64X2, or GBPA_F32 for an FP32 V-cycle that
+    preconditions the FP64 CG). max_eigs: optional eigenvalue estimates for
+    levels 1.. (else estimated)."""
 
     def __init__(self, mesh, orders, coeff="kappa", modes=None, precision=_lib.GBPA_F64, cheb_order=2,
                  coarse_rel_tol=1e-2, coarse_max_it=200, max_eigs=None, ir_points=None, coarse_jacobi=False):
         dev = _dev()
         self.spaces, self.integs, ops, smoothers, prols = [], [], [], [], []
         self.ess = []
+        coarse_diag = None
         for l, p in enumerate(orders):
             fes = FiniteElementSpace(mesh, p)
             integ = DiffusionIntegrator(coeff, ir_points=ir_points(p) if ir_points else None)
@@ -551,12 +555,19 @@ class DiffusionMultigrid(Multigrid):
             A = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=precision)
             self.spaces.append(fes); self.integs.append(integ); self.ess.append(ess)
             ops.append(A)
+            # the diagonal comes from the FP64 data (an FP32 operator cannot assemble it)
+            A64 = A if precision != _lib.GBPA_F32 else PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G,
+                                                                   integ.qdata, ess=ess)
+            diag = torch.empty(fes.ndofs, dtype=torch.float64, device=dev.torch_device)
+            A64.AssembleDiagonal(diag)
+            del A64
             if l == 0:
                 smoothers.append(None)
+                coarse_diag = diag
             else:
-                diag = torch.empty(fes.ndofs, dtype=torch.float64, device=dev.torch_device)
-                A.AssembleDiagonal(diag)
                 lam = max_eigs[l - 1] if max_eigs is not None else None
                 smoothers.append(OperatorChebyshevSmoother(A, diag, ess, cheb_order, lam))
-                prols.append(TransferOperator(self.spaces[l - 1], fes))
-        super().__init__(ops, smoothers, prols, coarse_rel_tol, coarse_max_it, coarse_jacobi)
+                prols.append(TransferOperator(self.spaces[l - 1], fes, precision))
+        self.coarse_diag = coarse_diag
+        super().__init__(ops, smoothers, prols, coarse_rel_tol, coarse_max_it, coarse_jacobi,
+                         coarse_diag if coarse_jacobi else None)

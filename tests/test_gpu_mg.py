@@ -57,14 +57,15 @@ class GoldenHierarchy:
                     d.ctx, ne, ORDERS[l - 1] + 1, Rc.ndofs, ctypes.c_void_p(Rc.gather_map.data_ptr()),
                     ctypes.c_void_p(Rc.offsets.data_ptr()), ctypes.c_void_p(Rc.indices.data_ptr()), p + 1,
                     ndofs, ctypes.c_void_p(R.gather_map.data_ptr()), ctypes.c_void_p(R.offsets.data_ptr()),
-                    ctypes.c_void_p(R.indices.data_ptr()), Bi.ctypes.data_as(ctypes.c_void_p),
+                    ctypes.c_void_p(R.indices.data_ptr()), Bi.ctypes.data_as(ctypes.c_void_p), 0,
                     ctypes.byref(hp)) == 0
                 self.P.append(hp)
         ops = (ctypes.c_void_p * 3)(*[o.handle for o in self.ops])
         sms = (ctypes.c_void_p * 3)(*self.sm)
         prs = (ctypes.c_void_p * 2)(*self.P)
         self.mg = ctypes.c_void_p()
-        assert d.lib.gbpa_multigrid_create(d.ctx, 3, ops, sms, prs, 1e-2, 200, 0, ctypes.byref(self.mg)) == 0
+        assert d.lib.gbpa_multigrid_create(d.ctx, 3, ops, sms, prs, 1e-2, 200, 0, None,
+                                           ctypes.byref(self.mg)) == 0
 
     def close(self):
         lib = self.d.lib
@@ -164,16 +165,19 @@ def pmg_problem(n, orders, precision=0, coarse_jacobi=False):
     return M, b
 
 
-@pytest.mark.parametrize("precision,coarse_jacobi", [(0, False), (2, False), (2, True)])
+@pytest.mark.parametrize("precision,coarse_jacobi", [(0, False), (2, False), (2, True), (1, False), (1, True)])
 def test_mg_pcg_solves_the_jacobi_system(precision, coarse_jacobi):
     """On a 10^3 mesh at p=4 (levels 1, 2, 4): the MG-preconditioned solve
-    (plain or Jacobi-preconditioned coarse CG) reaches the Jacobi-PCG
-    solution of the same constrained system (1e-9) in far fewer
-    iterations."""
+    (FP64, double-float or FP32 levels; plain or Jacobi-preconditioned
+    coarse CG) reaches the FP64 Jacobi-PCG solution of the same constrained
+    system (1e-9) in far fewer iterations."""
     from mfem_gb300 import _lib
     from mfem_gb300.pa import CGSolver, OperatorJacobiSmoother
+    from mfem_gb300.pa import PAOperator
     M, b = pmg_problem(10, (1, 2, 4), precision, coarse_jacobi)
-    A = M.operators[-1]
+    fes, integ = M.spaces[-1], M.integs[-1]
+    A = M.operators[-1] if precision != 1 else PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
+                                                          ess=M.ess[-1])
     x = torch.zeros_like(b)
     cg = CGSolver(); cg.SetRelTol(1e-11); cg.SetMaxIter(500); cg.SetOperator(A); cg.SetPreconditioner(M)
     cg.Mult(b, x)
