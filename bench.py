@@ -329,6 +329,7 @@ def run_gpu(args):
         extras = run_extras(args, fes, integ, op, x, y)
         if not args.no_pcg:
             extras["pcg"] = run_pcg_form(args.pcg_n, args.p, args.pcg_max_it)
+            extras["mg"] = run_mg_form(args.pcg_n, args.p, (1, 2, 4))
 
     line = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,

@@ -366,6 +366,21 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
                               int max_it, int *iterations, int *converged,
                               double *final_norms, double *seconds);
 
+/* ---------------------------------------------------------- linear form */
+/* DomainLFIntegrator::AssembleDevice + LinearFormExtension::Assemble
+ * (fem/integ/lininteg_domain.cpp:22-59, DLFEvalAssemble3D in
+ * fem/integ/lininteg_domain_kernels.hpp:164-..., fem/linearform_ext.cpp:
+ * 20-68): b = R^T (B^T x B^T x B^T)(W f detJ) for one DomainLFIntegrator
+ * over all elements, b overwritten. B (Q, D) and W (Q^3) at the linear
+ * form's rule (the reference's default: order 2p, Q = p + 1), detJ (Q^3,
+ * NE) at that rule, f: coeff_size 1 (constant) or Q^3 NE values (the
+ * CoefficientVector at the rule's physical points). offsets/indices: the
+ * lexicographic restriction's CSR maps. */
+int gbpa_domain_lf3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
+                     const double *B, const double *W, const double *detJ,
+                     const double *coeff, int64_t coeff_size, int ndofs,
+                     const int *offsets, const int *indices, double *b);
+
 /* ---------------------------------------------------------- p-multigrid */
 /* p-multigrid preconditioning around the PA diffusion operator, the
  * structure of the reference's examples/ex26.cpp. Levels are operators

@@ -152,3 +152,93 @@ extern "C" int gbpa_mass_diagonal3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d,
    if (!dq_ok(d1d, q1d)) { return GBPA_ERR_UNSUPPORTED; }
    return launch_mass_diagonal(ctx, ne, d1d, q1d, B, D, y);
 }
+
+// ------------------------------------------------------------ linear form
+namespace gbpa
+{
+// DLFEvalAssemble3D (fem/integ/lininteg_domain_kernels.hpp:164-...): one
+// element per block of M x M threads (M = max(D, Q)); the quadrature values
+// v = W f detJ in shared memory, then the transposed contractions x, y, z.
+__global__ void domain_lf_kernel(int ne, int D, int Q, const double *__restrict__ B, const double *__restrict__ W,
+                                 const double *__restrict__ detJ, const double *__restrict__ f, int64_t c_size,
+                                 double *__restrict__ yE)
+{
+   extern __shared__ double sm[];
+   const int e = blockIdx.x;
+   const int tx = threadIdx.x, ty = threadIdx.y, M = blockDim.x;
+   const int Q3 = Q * Q * Q, D3 = D * D * D;
+   double *sB = sm;                  // [Q][D] as B(q, d) = B[q + Q d]
+   double *v = sB + Q * D;           // [Q^3]
+   double *t1 = v + Q3;              // [Q][Q][D]
+   double *t2 = t1 + Q * Q * D;      // [Q][D][D]
+   for (int i = tx + M * ty; i < Q * D; i += M * M) { sB[i] = B[i]; }
+   if (tx < Q && ty < Q)
+   {
+      for (int qz = 0; qz < Q; ++qz)
+      {
+         const int q = tx + Q * (ty + Q * qz);
+         const long long k = (long long)e * Q3 + q;
+         v[q] = W[q] * (c_size == 1 ? f[0] : f[k]) * detJ[k];
+      }
+   }
+   __syncthreads();
+   if (tx < D && ty < Q)   // x: thread (dx, qy)
+   {
+      for (int qz = 0; qz < Q; ++qz)
+      {
+         double s = 0.0;
+         for (int qx = 0; qx < Q; ++qx) { s += sB[qx + Q * tx] * v[qx + Q * (ty + Q * qz)]; }
+         t1[tx + D * (ty + Q * qz)] = s;
+      }
+   }
+   __syncthreads();
+   if (tx < D && ty < D)   // y: thread (dx, dy)
+   {
+      for (int qz = 0; qz < Q; ++qz)
+      {
+         double s = 0.0;
+         for (int qy = 0; qy < Q; ++qy) { s += sB[qy + Q * ty] * t1[tx + D * (qy + Q * qz)]; }
+         t2[tx + D * (ty + D * qz)] = s;
+      }
+   }
+   __syncthreads();
+   if (tx < D && ty < D)   // z
+   {
+      for (int dz = 0; dz < D; ++dz)
+      {
+         double s = 0.0;
+         for (int qz = 0; qz < Q; ++qz) { s += sB[qz + Q * dz] * t2[tx + D * (ty + D * qz)]; }
+         yE[(long long)e * D3 + tx + D * (ty + D * dz)] = s;
+      }
+   }
+}
+} // namespace gbpa
+
+// DomainLFIntegrator::AssembleDevice + LinearFormExtension::Assemble
+// (fem/integ/lininteg_domain.cpp:22-59, fem/linearform_ext.cpp:20-68)
+extern "C" int gbpa_domain_lf3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d, const double *B, const double *W,
+                                const double *detJ, const double *coeff, int64_t coeff_size, int ndofs,
+                                const int *offsets, const int *indices, double *b)
+{
+   if (!ctx || ne < 0 || ndofs < 0 || (ne > 0 && (!B || !W || !detJ || !coeff || !offsets || !indices)) ||
+       (ndofs > 0 && !b))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   if (!dq_ok(d1d, q1d)) { return GBPA_ERR_UNSUPPORTED; }
+   if (coeff_size != 1 && coeff_size != (int64_t)ne * q1d * q1d * q1d) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (ndofs == 0) { return GBPA_SUCCESS; }
+   const int64_t nE = (int64_t)ne * d1d * d1d * d1d;
+   double *yE = (double *)scratch(ctx, SLOT_EVEC_A, sizeof(double) * (nE > 0 ? nE : 1));
+   if (!yE) { return GBPA_ERR_OUT_OF_MEMORY; }
+   if (ne > 0)
+   {
+      int D = d1d, Q = q1d, M = d1d > q1d ? d1d : q1d;
+      const size_t smem = sizeof(double) * ((size_t)Q * D + (size_t)Q * Q * Q + (size_t)Q * Q * D + (size_t)Q * D * D);
+      void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&W, (void *)&detJ, (void *)&coeff, &coeff_size, &yE};
+      const int rc = launch_generic(ctx, (const void *)domain_lf_kernel, dim3(ne), dim3(M, M), args, smem,
+                                    "domain_lf");
+      if (rc) { return rc; }
+   }
+   return launch_csr_scatter<double>(ctx, ndofs, offsets, indices, yE, b, nullptr, nullptr, false, false);
+}

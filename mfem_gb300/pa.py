@@ -284,6 +284,46 @@ class MassIntegrator(_PAIntegrator):
                                            _p(self.qdata), _p(y)), "mass_diagonal3d")
 
 
+class DomainLFIntegrator(_PAIntegrator):
+    """fem/lininteg.hpp DomainLFIntegrator(f): b_i = (f, phi_i), assembled on
+    the device. Default rule: order 2p (p + 1 Gauss points per direction)."""
+
+    def quad_points(self, p):
+        return self.ir_points if self.ir_points else p + 1
+
+
+class LinearForm:
+    """fem/linearform.cpp LinearForm with device assembly (UseFastAssembly,
+    LinearFormExtension::Assemble): the sum of its domain integrators."""
+
+    def __init__(self, fes):
+        self.fes = fes
+        self.integs = []
+        self.b = None
+
+    def AddDomainIntegrator(self, lfi):
+        self.integs.append(lfi)
+
+    def Assemble(self, modes=None):
+        dev = _dev()
+        fes = self.fes
+        R = fes.GetElementRestriction()
+        self.b = torch.zeros(fes.ndofs, dtype=torch.float64, device=dev.torch_device)
+        part = torch.empty_like(self.b)
+        for lfi in self.integs:
+            t = Tables(fes.p, lfi.quad_points(fes.p))
+            geom = _geometry(fes, t, modes)
+            detJ = torch.empty(t.Q ** 3 * fes.ne, dtype=torch.float64, device=dev.torch_device)
+            check(dev.lib.gbpa_geom_determinants3d(dev.ctx, fes.ne, geom["dg"], t.Q, _p(geom["Bg"]), _p(geom["Gg"]),
+                                                   _p(geom["X"]), _p(detJ)), "geom_determinants3d")
+            C, _ = lfi._coefficient(fes, t, geom)
+            B, W = to_dev(t.B), to_dev(t.W)
+            check(dev.lib.gbpa_domain_lf3d(dev.ctx, fes.ne, t.D, t.Q, _p(B), _p(W), _p(detJ), _p(C), C.numel(),
+                                           fes.ndofs, _p(R.offsets), _p(R.indices), _p(part)), "domain_lf3d")
+            self.b += part
+        return self.b
+
+
 class PAOperator:
     """The library's fused L-vector operator (restriction + integrator +
     transpose, optionally constrained): one gbpa_operator."""

@@ -1128,3 +1128,57 @@ int or_mg_pcg(const or_mg_level *lv, int nl, int order, double coarse_tol, int c
    free(work); free(zz);
    return it;
 }
+
+/* ------------------------------------------------------------ linear form */
+/* DomainLFIntegrator::AssembleDevice + LinearFormExtension::Assemble
+ * (fem/integ/lininteg_domain.cpp:22-59, DLFEvalAssemble3D in
+ * fem/integ/lininteg_domain_kernels.hpp:164-..., fem/linearform_ext.cpp:20-68):
+ * y_e(dx,dy,dz) = sum_q B(qx,dx) B(qy,dy) B(qz,dz) W(q) f(q,e) detJ(q,e),
+ * b = R^T y. f has c_size 1 (constant) or Q^3 NE values. */
+void or_domain_lf3d(int ne, int d1d, int q1d, const double *B, const double *W,
+                    const double *detJ, const double *f, long c_size, int ndofs,
+                    const int *offsets, const int *indices, double *b)
+{
+   const int D = d1d, Q = q1d, D3 = D * D * D, Q3 = Q * Q * Q;
+   double *yE = (double *)malloc(sizeof(double) * (size_t)ne * D3);
+#pragma omp parallel for
+   for (int e = 0; e < ne; ++e)
+   {
+      double *t1 = (double *)malloc(sizeof(double) * D * Q * Q);
+      double *t2 = (double *)malloc(sizeof(double) * D * D * Q);
+      double v[4096];
+      for (int q = 0; q < Q3; ++q)
+      {
+         const double fv = c_size == 1 ? f[0] : f[q + (long)Q3 * e];
+         v[q] = W[q] * fv * detJ[q + (long)Q3 * e];
+      }
+      /* contract x, then y, then z */
+      for (int qz = 0; qz < Q; ++qz)
+         for (int qy = 0; qy < Q; ++qy)
+            for (int dx = 0; dx < D; ++dx)
+            {
+               double s = 0.0;
+               for (int qx = 0; qx < Q; ++qx) { s += B[qx + Q * dx] * v[qx + Q * (qy + Q * qz)]; }
+               t1[dx + D * (qy + Q * qz)] = s;
+            }
+      for (int qz = 0; qz < Q; ++qz)
+         for (int dy = 0; dy < D; ++dy)
+            for (int dx = 0; dx < D; ++dx)
+            {
+               double s = 0.0;
+               for (int qy = 0; qy < Q; ++qy) { s += B[qy + Q * dy] * t1[dx + D * (qy + Q * qz)]; }
+               t2[dx + D * (dy + D * qz)] = s;
+            }
+      for (int dz = 0; dz < D; ++dz)
+         for (int dy = 0; dy < D; ++dy)
+            for (int dx = 0; dx < D; ++dx)
+            {
+               double s = 0.0;
+               for (int qz = 0; qz < Q; ++qz) { s += B[qz + Q * dz] * t2[dx + D * (dy + D * qz)]; }
+               yE[(long)e * D3 + dx + D * (dy + D * dz)] = s;
+            }
+      free(t1); free(t2);
+   }
+   or_restriction_mult_transpose(D3, ndofs, offsets, indices, yE, b, 0);
+   free(yE);
+}

@@ -133,6 +133,13 @@ int or_mg_pcg(const or_mg_level *lv, int nl, int order, double coarse_tol, int c
               const double *b, double *x, double rel_tol, double abs_tol, int max_it,
               double *final_norm, int *converged);
 
+/* DomainLFIntegrator device assembly (fem/integ/lininteg_domain.cpp:22-59,
+ * fem/linearform_ext.cpp:20-68): b = R^T (B^T x B^T x B^T)(W f detJ).
+ * Q^3 <= 4096. */
+void or_domain_lf3d(int ne, int d1d, int q1d, const double *B, const double *W,
+                    const double *detJ, const double *f, long c_size, int ndofs,
+                    const int *offsets, const int *indices, double *b);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int or_num_threads(void);
 

@@ -8,6 +8,7 @@
 //   AddMultPA / AssembleDiagonal fem/integ/bilininteg_{diffusion,mass}_pa.cpp
 //   BilinearForm::Mult (PA)      fem/bilinearform_ext.cpp:487-564
 //   PCG + OperatorJacobiSmoother linalg/solvers.cpp:331-452,869-1050
+//   DomainLFIntegrator (device)  fem/linearform_ext.cpp:20-68
 //   p-multigrid (transfer, Chebyshev smoother, V-cycle): run_pmg below
 // Usage: golden_driver <outdir>   (one subdirectory per case)
 #include "mfem.hpp"
@@ -346,6 +347,35 @@ static void run_case(const Case &c, const std::string &root)
       Vector xE(R->Height()), yE(R->Height());
       R->Mult(x, xE); yE = 0.0;
       mint->AddMultPA(xE, yE); save(dir, "yE_mass", yE);
+   }
+
+   if (!c.solve)
+   {
+      // DomainLFIntegrator(kappa) through the device-style assembly
+      // (LinearForm::UseFastAssembly -> LinearFormExtension::Assemble,
+      // fem/linearform_ext.cpp:20-68, DLFEvalAssemble3D,
+      // fem/integ/lininteg_domain_kernels.hpp:164-...) with its default rule
+      // of order 2p (p + 1 Gauss points), and the inputs at that rule
+      const IntegrationRule &lir = IntRules.Get(Geometry::CUBE, 2 * p);
+      const int lq = p + 1;
+      MFEM_VERIFY(lir.GetNPoints() == lq * lq * lq, "lf rule size");
+      LinearForm lf(&fes);
+      lf.AddDomainIntegrator(new DomainLFIntegrator(kfn));
+      lf.UseFastAssembly(true);
+      lf.Assemble();
+      save(dir, "lf_fn", lf);
+      LinearForm lf2(&fes);
+      lf2.AddDomainIntegrator(new DomainLFIntegrator(kfn));
+      lf2.Assemble();
+      save(dir, "lf_fn_host", lf2);
+      const DofToQuad &lmaps = el.GetDofToQuad(lir, DofToQuad::TENSOR);
+      save(dir, "lf_B", lmaps.B);
+      save(dir, "lf_W", lir.GetWeights());
+      const GeometricFactors *lgeom = mesh.GetGeometricFactors(lir, GeometricFactors::DETERMINANTS);
+      save(dir, "lf_detJ", lgeom->detJ);
+      QuadratureSpace lqs(mesh, lir);
+      CoefficientVector lcv(kfn, lqs, CoefficientStorage::COMPRESSED);
+      save(dir, "lf_coeff", lcv);
    }
 
    if (c.solve)

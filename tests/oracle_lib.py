@@ -44,6 +44,7 @@ _SIGS = {
     "or_power_method": [_P, _I, _D, ctypes.c_ulonglong],
     "or_mg_mult": [_P, _I, _I, _D, _I, _P, _P],
     "or_mg_pcg": [_P, _I, _I, _D, _I, _P, _P, _D, _D, _I, _P, _P],
+    "or_domain_lf3d": [_I, _I, _I, _P, _P, _P, _P, _L, _I, _P, _P, _P],
 }
 _RESTYPES = {"or_pcg_diffusion": ctypes.c_int, "or_num_threads": ctypes.c_int,
              "or_power_method": ctypes.c_double, "or_mg_pcg": ctypes.c_int}
@@ -187,6 +188,15 @@ class Oracle:
 
     def num_threads(self):
         return self.lib.or_num_threads()
+
+    def domain_lf3d(self, ne, d1d, q1d, B, W, detJ, f, ndofs, off, ind):
+        b = np.zeros(ndofs)
+        f = np.ascontiguousarray(f, np.float64)
+        self.lib.or_domain_lf3d(ne, d1d, q1d, _ptr(np.ascontiguousarray(B)), _ptr(np.ascontiguousarray(W)),
+                                _ptr(np.ascontiguousarray(detJ)), _ptr(f), f.size, ndofs,
+                                _ptr(np.ascontiguousarray(off, np.int32)), _ptr(np.ascontiguousarray(ind, np.int32)),
+                                _ptr(b))
+        return b
 
     # ---- p-multigrid (levels: list of MGLevel, coarsest first)
     @staticmethod

@@ -136,3 +136,21 @@ def test_cfg1_pcg_solution(oracle):
     assert conv and bool(ref_conv)
     assert abs(it - int(ref_it)) <= 1
     assert relerr(X, g["X"]) < 1e-10
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c != "cfg1_solve"])
+def test_domain_linear_form(oracle, case):
+    """DomainLFIntegrator(kappa) assembled through the reference's device
+    path (LinearForm::UseFastAssembly) at its default rule (p + 1 Gauss
+    points): the oracle's restatement from the rule's inputs, and the basis
+    table against the oracle's own."""
+    g = load_golden(case)
+    ne, ndofs, D, Q, _ = meta(g)
+    lq = D     # p + 1 points
+    x, _ = oracle.gauss_legendre(lq)
+    B, _ = oracle.basis_tables(oracle.gauss_lobatto(D), x)
+    assert np.abs(B.ravel(order="F") - g["lf_B"]).max() < 1e-14
+    b = oracle.domain_lf3d(ne, D, lq, g["lf_B"], g["lf_W"], g["lf_detJ"], g["lf_coeff"], ndofs,
+                           g["offsets"], g["indices"])
+    ref = g["lf_fn"]
+    assert np.linalg.norm(b - ref) / np.linalg.norm(ref) < 1e-14
