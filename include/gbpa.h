@@ -366,6 +366,26 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
                               int max_it, int *iterations, int *converged,
                               double *final_norms, double *seconds);
 
+/* ------------------------------------------------------ vector diffusion */
+/* VectorDiffusionIntegrator::AssemblePA, 3D, scalar or vector coefficient
+ * (fem/integ/bilininteg_vecdiffusion_pa.cpp:68-276): for each component c of
+ * a vdim-component H1 space, the symmetric diffusion qdata scaled by the
+ * coefficient component (coeff_vdim 1: the same scalar for every
+ * component; coeff_vdim = vdim: C_c). C laid out (coeff_vdim, Q^3, NE),
+ * c_size coeff_vdim (constant) or coeff_vdim Q^3 NE. D: (Q^3, 6, vdim, NE),
+ * which fits in the reference's pa_data (Q^3 9 vdim NE). Matrix
+ * coefficients (component coupling) are not supported. */
+int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim,
+                                  int coeff_vdim, const double *W,
+                                  const double *J, const double *C,
+                                  int64_t c_size, double *D);
+/* VectorDiffusionIntegrator::AddMultPA, 3D (kernel
+ * fem/integ/bilininteg_vecdiffusion_pa.hpp:96-163): y_E += A_e x_E on the
+ * (D^3, vdim, NE) E-vectors of the vector space's element restriction. */
+int gbpa_vector_diffusion_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int d1d,
+                                  int q1d, const double *B, const double *G,
+                                  const double *D, const double *x, double *y);
+
 /* ---------------------------------------------------------- linear form */
 /* DomainLFIntegrator::AssembleDevice + LinearFormExtension::Assemble
  * (fem/integ/lininteg_domain.cpp:22-59, DLFEvalAssemble3D in

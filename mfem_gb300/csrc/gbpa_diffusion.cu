@@ -205,3 +205,15 @@ extern "C" int gbpa_diffusion_diagonal3d(gbpa_ctx_t ctx, int ne, int symm,
    if (!dq_ok(d1d, q1d)) { return GBPA_ERR_UNSUPPORTED; }
    return launch_diffusion_diagonal(ctx, ne, symm ? 1 : 0, d1d, q1d, B, G, D, y);
 }
+
+// VectorDiffusionIntegrator::AddMultPA, 3D, scalar or vector coefficient
+// (fem/integ/bilininteg_vecdiffusion_pa.cpp:282-330, kernel
+// fem/integ/bilininteg_vecdiffusion_pa.hpp:96-163): the scalar symmetric
+// apply on the vdim NE pseudo-elements of the (D^3, vdim, NE) E-vectors
+extern "C" int gbpa_vector_diffusion_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int d1d, int q1d,
+                                             const double *B, const double *G, const double *D,
+                                             const double *x, double *y)
+{
+   if (!ctx || ne < 0 || vdim < 1 || vdim > 3) { return GBPA_ERR_INVALID_ARGUMENT; }
+   return gbpa_diffusion_apply3d(ctx, ne * vdim, 1, d1d, q1d, B, G, nullptr, nullptr, D, x, y);
+}

@@ -190,6 +190,41 @@ __global__ void diffusion_setup_kernel(int ne, int Q3, int coeff_dim,
    }
 }
 
+// VectorDiffusionIntegrator::AssemblePA, 3D (fem/integ/bilininteg_vecdiffusion_pa.cpp:
+// 213-276), scalar or vector coefficient: per component c the symmetric
+// (W/detJ) adj(J) adj(J)^T scaled by C_k (k = c for a vector coefficient,
+// 0 for a scalar one; C laid out (coeff_vdim, Q^3, NE)). Layout
+// (Q^3, 6, vdim, NE): component c of element e is the scalar diffusion
+// qdata of the pseudo-element c + vdim e, so the scalar apply runs on
+// vdim NE pseudo-elements of the (D^3, vdim, NE) E-vector.
+__global__ void vector_diffusion_setup_kernel(int ne, int Q3, int vdim, int coeff_vdim,
+                                              const double *__restrict__ W,
+                                              const double *__restrict__ Jg,
+                                              const double *__restrict__ C, int const_c,
+                                              double *__restrict__ D)
+{
+   const int64_t n = (int64_t)ne * Q3;
+   const double one = 1.0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int q = (int)(i % Q3);
+      const int64_t e = i / Q3;
+      double J[3][3];
+      for (int c = 0; c < 3; ++c)
+         for (int d = 0; d < 3; ++d) { J[c][d] = Jg[q + (int64_t)Q3 * (c + 3 * (d + 3 * e))]; }
+      double d0[6];
+      diffusion_point(J, W[q], 1, &one, 1, d0, 1);
+      for (int c = 0; c < vdim; ++c)
+      {
+         const int k = coeff_vdim == 1 ? 0 : c;
+         const double ck = const_c ? C[k] : C[k + (int64_t)coeff_vdim * i];
+         double *out = D + q + (int64_t)Q3 * 6 * (c + (int64_t)vdim * e);
+         for (int s = 0; s < 6; ++s) { out[(int64_t)s * Q3] = d0[s] * ck; }
+      }
+   }
+}
+
 __global__ void diffusion_setup_nodes_kernel(int ne, int dg, int Q, int coeff_dim,
                                              const double *__restrict__ W,
                                              const double *__restrict__ Bg,
@@ -319,4 +354,22 @@ extern "C" int gbpa_mass_setup3d(gbpa_ctx_t ctx, int ne, int nq, const double *W
                                                                 c_size == 1 ? 1 : 0,
                                                                 by_val ? 1 : 0, D);
    return last_launch(ctx, "mass_setup");
+}
+
+extern "C" int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim, int coeff_vdim,
+                                             const double *W, const double *J, const double *C, int64_t c_size,
+                                             double *D)
+{
+   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const int Q3 = q1d * q1d * q1d;
+   if (c_size != coeff_vdim && c_size != (int64_t)coeff_vdim * ne * Q3) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (ne == 0) { return GBPA_SUCCESS; }
+   if (!W || !J || !C || !D) { return GBPA_ERR_INVALID_ARGUMENT; }
+   const int64_t n = (int64_t)ne * Q3;
+   vector_diffusion_setup_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, vdim, coeff_vdim, W, J, C,
+                                                                            c_size == coeff_vdim ? 1 : 0, D);
+   return last_launch(ctx, "vector_diffusion_setup");
 }

@@ -9,6 +9,7 @@
 //   BilinearForm::Mult (PA)      fem/bilinearform_ext.cpp:487-564
 //   PCG + OperatorJacobiSmoother linalg/solvers.cpp:331-452,869-1050
 //   DomainLFIntegrator (device)  fem/linearform_ext.cpp:20-68
+//   VectorDiffusionIntegrator PA fem/integ/bilininteg_vecdiffusion_pa.cpp
 //   p-multigrid (transfer, Chebyshev smoother, V-cycle): run_pmg below
 // Usage: golden_driver <outdir>   (one subdirectory per case)
 #include "mfem.hpp"
@@ -347,6 +348,36 @@ static void run_case(const Case &c, const std::string &root)
       Vector xE(R->Height()), yE(R->Height());
       R->Mult(x, xE); yE = 0.0;
       mint->AddMultPA(xE, yE); save(dir, "yE_mass", yE);
+   }
+
+   if (!c.solve && (c.coeff == C_FN || c.coeff == C_VEC))
+   {
+      // VectorDiffusionIntegrator PA on the vdim = 3 space (byNODES) with the
+      // case's scalar or vector coefficient and rule
+      // (fem/integ/bilininteg_vecdiffusion_pa.cpp:68-276, apply
+      // fem/integ/bilininteg_vecdiffusion_pa.hpp:96-163)
+      FiniteElementSpace vfes(&mesh, &fec, 3);
+      VectorDiffusionIntegrator *vdi = c.coeff == C_FN ? new VectorDiffusionIntegrator(kfn, &ir)
+                                                        : new VectorDiffusionIntegrator(kvec);
+      if (c.coeff == C_VEC) { vdi->SetIntRule(&ir); }
+      const Operator *vR = vfes.GetElementRestriction(ElementDofOrdering::LEXICOGRAPHIC);
+      Vector vx(vfes.GetVSize());
+      uint64_t sv = 5;
+      for (int i = 0; i < vx.Size(); i++) { vx(i) = 2.0 * u01(sv) - 1.0; }
+      BilinearForm va(&vfes);
+      va.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      va.AddDomainIntegrator(vdi);
+      va.Assemble();
+      Vector vy(vfes.GetVSize());
+      va.Mult(vx, vy);
+      Vector vxE(vR->Height()), vyE(vR->Height());
+      vR->Mult(vx, vxE);
+      vyE = 0.0;
+      vdi->AddMultPA(vxE, vyE);
+      save(dir, "vec_x", vx);
+      save(dir, "vec_y", vy);
+      save(dir, "vec_xE", vxE);
+      save(dir, "vec_yE", vyE);
    }
 
    if (!c.solve)
