@@ -386,6 +386,18 @@ int gbpa_vector_diffusion_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int d1d,
                                   int q1d, const double *B, const double *G,
                                   const double *D, const double *x, double *y);
 
+/* VectorMassIntegrator::AssemblePA / AddMultPA, 3D, scalar or vector
+ * coefficient (fem/integ/bilininteg_vecmass_pa.cpp:21-210): D (Q^3,
+ * coeff_vdim, NE) = C_k W detJ, the reference's own layout; the apply runs
+ * the scalar mass operator per component on the (D^3, vdim, NE) E-vectors.
+ * Matrix coefficients are not supported. */
+int gbpa_vector_mass_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim,
+                             int coeff_vdim, const double *W, const double *J,
+                             const double *C, int64_t c_size, double *D);
+int gbpa_vector_mass_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int coeff_vdim,
+                             int d1d, int q1d, const double *B,
+                             const double *D, const double *x, double *y);
+
 /* ---------------------------------------------------------- linear form */
 /* DomainLFIntegrator::AssembleDevice + LinearFormExtension::Assemble
  * (fem/integ/lininteg_domain.cpp:22-59, DLFEvalAssemble3D in

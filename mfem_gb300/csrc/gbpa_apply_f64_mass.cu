@@ -13,3 +13,12 @@ int launch_mass_apply<double>(gbpa_ctx *ctx, int ne, int D, int Q, const double 
                                 accumulate, skip);
 }
 } // namespace gbpa
+
+namespace gbpa
+{
+int launch_mass_apply_qdiv(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const double *qd,
+                           const double *x, double *y, int qdiv)
+{
+   return launch_mass_ar<ArF64>(ctx, GBPA_F64, ne, D, Q, B, qd, x, nullptr, nullptr, y, true, nullptr, qdiv);
+}
+} // namespace gbpa

@@ -661,8 +661,10 @@ __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
                                   const int *__restrict__ gmap,
                                   const unsigned char *__restrict__ mask,
                                   typename AR::In *__restrict__ y, int accumulate,
-                                  const int *__restrict__ skip)
+                                  const int *__restrict__ skip, int qdiv)
 {
+   // qdiv > 1: element e reads the qdata of element e / qdiv (the components
+   // of a vector space sharing one scalar coefficient's qdata)
    using V = typename AR::V;
    if (skip && *skip) { return; }
    constexpr int DM = TD ? TD : MAXD;
@@ -727,7 +729,7 @@ __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
    V o[DM];
 #pragma unroll
    for (int dz = 0; dz < DM; ++dz) { o[dz] = AR::zero(); }
-   const typename AR::Qd *qe = qd + (long long)e * Q3 + tx + Q * ty;
+   const typename AR::Qd *qe = qd + (long long)(e / qdiv) * Q3 + tx + Q * ty;
 #pragma unroll
    for (int qz = 0; qz < QM; ++qz)
    {

@@ -115,7 +115,7 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
                    const typename AR::In *B, const typename AR::Qd *qd,
                    const typename AR::In *x, const int *gather_map,
                    const unsigned char *ess_mask, typename AR::In *y,
-                   bool accumulate, const int *skip)
+                   bool accumulate, const int *skip, int qdiv = 1)
 {
    if (ne == 0) { return GBPA_SUCCESS; }
    if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
@@ -128,7 +128,7 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
    const size_t smem = sizeof(typename AR::V) * (Q * D + (size_t)nbz * mass_smem_per_elem(D, Q));
    int acc = accumulate ? 1 : 0;
    void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&qd, (void *)&x,
-                   (void *)&gather_map, (void *)&ess_mask, &y, &acc, (void *)&skip};
+                   (void *)&gather_map, (void *)&ess_mask, &y, &acc, (void *)&skip, &qdiv};
    return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),
                          args, smem, "mass_apply");
 }

@@ -96,6 +96,10 @@ int launch_mass_apply_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, c
                          const double *x, const int *gather_map, const unsigned char *ess_mask,
                          double *y, bool accumulate, const int *skip = nullptr);
 int launch_split_x2(gbpa_ctx *ctx, int64_t n, const double *a, float2 *b);
+// FP64 E-vector mass apply (y += A_e x) where element e reads the qdata of
+// element e / qdiv.
+int launch_mass_apply_qdiv(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const double *qd,
+                           const double *x, double *y, int qdiv);
 int launch_diffusion_diagonal(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
                               const double *B, const double *G,
                               const double *qd, double *y);

@@ -242,3 +242,20 @@ extern "C" int gbpa_domain_lf3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d, const 
    }
    return launch_csr_scatter<double>(ctx, ndofs, offsets, indices, yE, b, nullptr, nullptr, false, false);
 }
+
+// VectorMassIntegrator::AddMultPA, 3D, scalar or vector coefficient
+// (fem/integ/bilininteg_vecmass_pa.cpp:166-210, kernel
+// fem/integ/bilininteg_vecmass_pa.hpp:100-...): the scalar mass apply on the
+// vdim NE pseudo-elements of the (D^3, vdim, NE) E-vectors; pseudo-element
+// c + vdim e reads qdata (c, e) (vector coefficient) or e (scalar one)
+extern "C" int gbpa_vector_mass_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int coeff_vdim, int d1d, int q1d,
+                                        const double *B, const double *D, const double *x, double *y)
+{
+   if (!ctx || ne < 0 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim) ||
+       (ne > 0 && (!B || !D || !x || !y)))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   if (!dq_ok(d1d, q1d)) { return GBPA_ERR_UNSUPPORTED; }
+   return launch_mass_apply_qdiv(ctx, ne * vdim, d1d, q1d, B, D, x, y, coeff_vdim == 1 ? vdim : 1);
+}

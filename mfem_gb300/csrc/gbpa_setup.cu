@@ -225,6 +225,31 @@ __global__ void vector_diffusion_setup_kernel(int ne, int Q3, int vdim, int coef
    }
 }
 
+// VectorMassIntegrator::AssemblePA, 3D (fem/integ/bilininteg_vecmass_pa.cpp:
+// 119-160), scalar or vector coefficient: D(q, k, e) = C(k, q, e) W(q) detJ,
+// layout (Q^3, coeff_vdim, NE).
+__global__ void vector_mass_setup_kernel(int ne, int Q3, int coeff_vdim, const double *__restrict__ W,
+                                         const double *__restrict__ Jg, const double *__restrict__ C,
+                                         int const_c, double *__restrict__ D)
+{
+   const int64_t n = (int64_t)ne * Q3;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int q = (int)(i % Q3);
+      const int64_t e = i / Q3;
+      double J[3][3];
+      for (int c = 0; c < 3; ++c)
+         for (int d = 0; d < 3; ++d) { J[c][d] = Jg[q + (int64_t)Q3 * (c + 3 * (d + 3 * e))]; }
+      const double w_det = W[q] * det3(J);
+      for (int k = 0; k < coeff_vdim; ++k)
+      {
+         const double ck = const_c ? C[k] : C[k + (int64_t)coeff_vdim * i];
+         D[q + (int64_t)Q3 * (k + (int64_t)coeff_vdim * e)] = ck * w_det;
+      }
+   }
+}
+
 __global__ void diffusion_setup_nodes_kernel(int ne, int dg, int Q, int coeff_dim,
                                              const double *__restrict__ W,
                                              const double *__restrict__ Bg,
@@ -372,4 +397,21 @@ extern "C" int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, in
    vector_diffusion_setup_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, vdim, coeff_vdim, W, J, C,
                                                                             c_size == coeff_vdim ? 1 : 0, D);
    return last_launch(ctx, "vector_diffusion_setup");
+}
+
+extern "C" int gbpa_vector_mass_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim, int coeff_vdim, const double *W,
+                                        const double *J, const double *C, int64_t c_size, double *D)
+{
+   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const int Q3 = q1d * q1d * q1d;
+   if (c_size != coeff_vdim && c_size != (int64_t)coeff_vdim * ne * Q3) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (ne == 0) { return GBPA_SUCCESS; }
+   if (!W || !J || !C || !D) { return GBPA_ERR_INVALID_ARGUMENT; }
+   const int64_t n = (int64_t)ne * Q3;
+   vector_mass_setup_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, coeff_vdim, W, J, C,
+                                                                       c_size == coeff_vdim ? 1 : 0, D);
+   return last_launch(ctx, "vector_mass_setup");
 }

@@ -378,6 +378,32 @@ static void run_case(const Case &c, const std::string &root)
       save(dir, "vec_y", vy);
       save(dir, "vec_xE", vxE);
       save(dir, "vec_yE", vyE);
+      // VectorMassIntegrator PA with the same coefficient and the case's rule
+      // (fem/integ/bilininteg_vecmass_pa.cpp:21-210)
+      VectorMassIntegrator *vmi = c.coeff == C_FN ? new VectorMassIntegrator(kfn, &ir)
+                                                   : new VectorMassIntegrator(kvec);
+      if (c.coeff == C_VEC) { vmi->SetIntRule(&ir); }
+      BilinearForm vm(&vfes);
+      vm.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      vm.AddDomainIntegrator(vmi);
+      vm.Assemble();
+      Vector vmy(vfes.GetVSize());
+      vm.Mult(vx, vmy);
+      Vector vmyE(vR->Height());
+      vmyE = 0.0;
+      vmi->AddMultPA(vxE, vmyE);
+      save(dir, "vmass_y", vmy);
+      save(dir, "vmass_yE", vmyE);
+      if (c.coeff == C_FN)
+      {
+         CoefficientVector vc(kfn, qs, CoefficientStorage::FULL);
+         save(dir, "vmass_coeff", vc);
+      }
+      else
+      {
+         CoefficientVector vc(kvec, qs, CoefficientStorage::FULL);
+         save(dir, "vmass_coeff", vc);
+      }
    }
 
    if (!c.solve)

@@ -34,3 +34,21 @@ def test_vector_diffusion_matches_reference(case):
     y = zeros(3 * ndofs)
     call("gbpa_restriction_mult_transpose", ne, D3, 3, 0, ndofs, p(off), p(ind), p(yE), p(y), 0)
     assert relerr(H(y), g["vec_y"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_vector_mass_matches_reference(case):
+    from tests.gpu_util import T, H, p, call, zeros, relerr
+    g = load_golden(case)
+    ne, ndofs, D, Q, cdim = (int(v) for v in g["meta"][:5])
+    Q3, D3 = Q ** 3, D ** 3
+    qd = zeros(Q3 * cdim * ne)
+    C = T(g["vmass_coeff"])
+    call("gbpa_vector_mass_setup3d", ne, Q, 3, cdim, p(T(g["W"])), p(T(g["J"])), p(C), C.numel(), p(qd))
+    yE = zeros(ne * 3 * D3)
+    call("gbpa_vector_mass_apply3d", ne, 3, cdim, D, Q, p(T(g["B"])), p(qd), p(T(g["vec_xE"])), p(yE))
+    assert relerr(H(yE), g["vmass_yE"]) < 1e-12
+    y = zeros(3 * ndofs)
+    call("gbpa_restriction_mult_transpose", ne, D3, 3, 0, ndofs, p(T(g["offsets"])), p(T(g["indices"])), p(yE),
+         p(y), 0)
+    assert relerr(H(y), g["vmass_y"]) < 1e-12

@@ -175,3 +175,21 @@ def test_vector_diffusion_componentwise(oracle, case):
                                                xE[:, i, :].copy()).reshape(ne, D3)
     ref = g["vec_yE"].reshape(ne, 3, D3)
     assert np.linalg.norm(yE - ref) / np.linalg.norm(ref) < 1e-13
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.endswith("_fn") or c.endswith("_vec")])
+def test_vector_mass_componentwise(oracle, case):
+    """VectorMassIntegrator PA (vdim 3, scalar or vector coefficient) is the
+    scalar mass operator per component with that component's coefficient."""
+    g = load_golden(case)
+    ne, ndofs, D, Q, cdim = meta(g)
+    Q3, D3 = Q ** 3, D ** 3
+    C = g["vmass_coeff"]
+    xE = g["vec_xE"].reshape(ne, 3, D3)
+    yE = np.zeros_like(xE)
+    for i in range(3):
+        Ci = C if cdim == 1 else C.reshape(-1, 3)[:, i].copy()
+        Di = oracle.mass_setup3d(ne, Q3, g["W"], g["detJ"], Ci)
+        yE[:, i, :] = oracle.mass_apply3d(ne, D, Q, g["B"], Di, xE[:, i, :].copy()).reshape(ne, D3)
+    ref = g["vmass_yE"].reshape(ne, 3, D3)
+    assert np.linalg.norm(yE - ref) / np.linalg.norm(ref) < 1e-13
