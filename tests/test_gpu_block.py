@@ -40,7 +40,8 @@ def test_block_mult_equals_single(R, prec):
     op = A if prec == 0 else A32
     dt = torch.float64 if prec == 0 else torch.float32
     n = fes.ndofs
-    X = (torch.rand(n, R, dtype=torch.float64, device="cuda") - 0.5).to(dt).contiguous()
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    X = (torch.rand(n, R, dtype=torch.float64, device="cuda", generator=gen) - 0.5).to(dt).contiguous()
     Y = torch.empty_like(X)
     assert d.lib.gbpa_operator_mult_block(op.handle, R, P(X), P(Y)) == 0
     for r in range(R):
@@ -58,7 +59,8 @@ def test_block_pcg_matches_single_solves():
     d = dev()
     fes, integ, A, A32, M, e = problem(4, 4)
     n, R = fes.ndofs, 4
-    B = torch.rand(n, R, dtype=torch.float64, device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    B = torch.rand(n, R, dtype=torch.float64, device="cuda", generator=gen)
     B[torch.from_numpy(e).long().cuda()] = 0.0
     B = B.contiguous()
     X = torch.zeros_like(B)
@@ -80,7 +82,8 @@ def test_block_mixed_reaches_fp64_solution(curved):
     d = dev()
     fes, integ, A, A32, M, e = problem(4, 5 if curved else 3, curved=curved)
     n, R = fes.ndofs, 8
-    B = (torch.rand(n, R, dtype=torch.float64, device="cuda") * 2 - 1)
+    gen = torch.Generator(device="cuda").manual_seed(13)
+    B = (torch.rand(n, R, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1)
     B[torch.from_numpy(e).long().cuda()] = 0.0
     B = B.contiguous()
     X = torch.zeros_like(B)
