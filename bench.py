@@ -586,8 +586,18 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
     b = None
     configs = [("fp64", _lib.GBPA_F64, False, 200), ("f64x2", _lib.GBPA_F64X2, False, 200),
                ("fp64_coarse_jacobi", _lib.GBPA_F64, True, 50), ("f64x2_coarse_jacobi", _lib.GBPA_F64X2, True, 50),
-               ("f32_levels_coarse_jacobi", _lib.GBPA_F32, True, 50)]
+               ("f32_levels_coarse_jacobi", _lib.GBPA_F32, True, 50),
+               ("f32_levels_x2_outer", _lib.GBPA_F32, True, 50)]
+    Ax2_outer = None
     for name, prec, cj, cmax in configs:
+        if name == "f32_levels_x2_outer":
+            # the outer CG on the double-float fine operator (FP64-accurate, 3x
+            # the native FP64 apply rate)
+            fes4 = M64.spaces[-1]
+            it4 = M64.integs[-1]
+            from mfem_gb300.pa import PAOperator
+            Ax2_outer = PAOperator(0, fes4, it4.D, it4.Q, it4.B, it4.G, it4.qdata, ess=M64.ess[-1],
+                                   precision=_lib.GBPA_F64X2)
         t0 = time.perf_counter()
         M = DiffusionMultigrid(mesh, orders, "kappa", modes=fem.kappa_modes(3), precision=prec,
                                coarse_jacobi=cj, coarse_max_it=cmax)
@@ -599,8 +609,9 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
             b[torch.from_numpy(M.ess[-1]).long().cuda()] = 0.0
         x = torch.zeros_like(b)
         cg = CGSolver(); cg.SetRelTol(rel_tol); cg.SetMaxIter(500)
-        # FP32 levels precondition the FP64 iteration on the FP64 operator
-        cg.SetOperator(M.operators[-1] if prec != _lib.GBPA_F32 else A64)
+        # FP32 levels precondition the FP64 iteration on the FP64 (or the
+        # double-float) operator
+        cg.SetOperator(M.operators[-1] if prec != _lib.GBPA_F32 else (Ax2_outer if Ax2_outer else A64))
         cg.SetPreconditioner(M)
         cg.Mult(b, x)
         info = cg.info

@@ -34,7 +34,6 @@ struct f2
 
 struct ArF64
 {
-   static constexpr bool kPrefetch = false;
    using V = double; using In = double; using Qd = double;
    static __device__ __forceinline__ V zero() { return 0.0; }
    static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fma(a, b, acc); }
@@ -49,11 +48,6 @@ struct ArF64
 
 struct ArF32
 {
-   // Register prefetch of the qdata column (6 Q values per thread, loaded
-   // before the x/y contractions) measured slower on GB300 at p=4 (1.59 vs
-   // 1.49 ms per 29.5 M-DOF apply: the extra registers cost occupancy), so it
-   // is off; the code path stays for other orders and tuning.
-   static constexpr bool kPrefetch = false;
    using V = float; using In = float; using Qd = float;
    static __device__ __forceinline__ V zero() { return 0.f; }
    static __device__ __forceinline__ void mac(V &acc, V a, V b) { acc = fmaf(a, b, acc); }
@@ -69,7 +63,6 @@ struct ArF32
 
 struct ArX2
 {
-   static constexpr bool kPrefetch = false;
    using V = f2; using In = double; using Qd = float2;
    static __device__ __forceinline__ V zero() { return {0.f, 0.f}; }
    // acc += a * b. The rounded product p = a.h*b.h and its exact error
@@ -234,20 +227,6 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
    constexpr int DM = TD ? TD : MAXD;
    constexpr int QM = TQ ? TQ : MAXQ;
    const int D3 = D * D * D, Q3 = Q * Q * Q;
-   // register prefetch of this thread's symmetric qdata column (kPrefetch)
-   constexpr bool PF = AR::kPrefetch && TQ > 0;
-   V qpre[PF ? 6 : 1][PF ? QM : 1];
-   if constexpr (PF)
-   {
-      if (part && active && symm)
-      {
-         const typename AR::Qd *qe = qd + e * 6 * Q3 + tx + Q * ty;
-#pragma unroll
-         for (int k = 0; k < 6; ++k)
-#pragma unroll
-            for (int qz = 0; qz < QM; ++qz) { qpre[k][qz] = AR::ldq(qe + k * Q3 + Q * Q * qz); }
-      }
-   }
    if constexpr (GATHER && TD > 0 && TQ > 0)
    {
       // compile-time sizes: all of the thread's map entries first, then all
@@ -390,17 +369,8 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
             const typename AR::Qd *qp = qe + Q * Q * qz;
             if (symm)
             {
-               V O11, O12, O13, O22, O23, O33;
-               if constexpr (PF)
-               {
-                  O11 = qpre[0][qz]; O12 = qpre[1][qz]; O13 = qpre[2][qz];
-                  O22 = qpre[3][qz]; O23 = qpre[4][qz]; O33 = qpre[5][qz];
-               }
-               else
-               {
-                  O11 = LQ(qp); O12 = LQ(qp + Q3); O13 = LQ(qp + 2 * Q3);
-                  O22 = LQ(qp + 3 * Q3); O23 = LQ(qp + 4 * Q3); O33 = LQ(qp + 5 * Q3);
-               }
+               const V O11 = LQ(qp), O12 = LQ(qp + Q3), O13 = LQ(qp + 2 * Q3);
+               const V O22 = LQ(qp + 3 * Q3), O23 = LQ(qp + 4 * Q3), O33 = LQ(qp + 5 * Q3);
                AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
                AR::mac(oy, O12, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
                AR::mac(oz, O13, gx); AR::mac(oz, O23, gy); AR::mac(oz, O33, gz);
