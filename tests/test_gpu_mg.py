@@ -223,3 +223,58 @@ def test_mg_against_oracle_on_own_hierarchy():
     assert convo and info.converged == 1
     assert abs(info.iterations - ito) <= 1
     assert rel(H(x), xo) < 1e-10
+
+
+def test_mg_order_8_hierarchy():
+    """Orders 1, 2, 4, 8 (the ex26 doubling to p = 8) on a 4^3 mesh: the
+    MG-preconditioned solve reaches the Jacobi-PCG solution."""
+    from mfem_gb300.pa import CGSolver, OperatorJacobiSmoother
+    M, b = pmg_problem(4, (1, 2, 4, 8), 2)
+    A = M.operators[-1]
+    x = torch.zeros_like(b)
+    cg = CGSolver(); cg.SetRelTol(1e-11); cg.SetMaxIter(500); cg.SetOperator(A); cg.SetPreconditioner(M)
+    cg.Mult(b, x)
+    assert cg.GetConverged()
+    J = OperatorJacobiSmoother(A, M.ess[-1])
+    xj = torch.zeros_like(b)
+    cj = CGSolver(); cj.SetRelTol(1e-11); cj.SetMaxIter(5000); cj.SetOperator(A); cj.SetPreconditioner(J)
+    cj.Mult(b, xj)
+    assert cj.GetConverged() and cg.GetNumIterations() * 3 < cj.GetNumIterations()
+    assert float(torch.linalg.norm(x - xj) / torch.linalg.norm(xj)) < 1e-9
+
+
+def test_mg_invalid_arguments_rejected():
+    """Mismatched levels and unsupported combinations return
+    GBPA_ERR_INVALID_ARGUMENT / GBPA_ERR_UNSUPPORTED without touching the GPU
+    state; the context stays usable."""
+    from mfem_gb300 import _lib
+    from mfem_gb300.pa import PAOperator
+    from tests.gpu_util import dev
+    d = dev()
+    M, b = pmg_problem(3, (1, 2))
+    ops, P, S = M.operators, M.prolongations, M.smoothers
+    h = ctypes.c_void_p()
+    arr = lambda *hs: (ctypes.c_void_p * len(hs))(*hs)
+    # smoother of the wrong level
+    assert d.lib.gbpa_multigrid_create(d.ctx, 2, arr(ops[0].handle, ops[1].handle), arr(None, None),
+                                       arr(P[0].handle), 1e-2, 200, 0, None, ctypes.byref(h)) == -1
+    # levels swapped (sizes do not match the transfer)
+    assert d.lib.gbpa_multigrid_create(d.ctx, 2, arr(ops[1].handle, ops[0].handle), arr(None, S[1].handle),
+                                       arr(P[0].handle), 1e-2, 200, 0, None, ctypes.byref(h)) == -1
+    # an FP32 coarse level with a Jacobi coarse solve needs the coarse diagonal
+    fes, integ = M.spaces[0], M.integs[0]
+    A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=M.ess[0], precision=1)
+    assert d.lib.gbpa_multigrid_create(d.ctx, 1, arr(A32.handle), None, None, 1e-2, 50, 1, None,
+                                       ctypes.byref(h)) == -1
+    # the outer CG needs FP64 vectors
+    x = torch.zeros_like(b)
+    info = _lib.SolveInfo()
+    assert d.lib.gbpa_pcg_solve_mg(A32.handle, M.handle, ctypes.c_void_p(b.data_ptr()),
+                                   ctypes.c_void_p(x.data_ptr()), 1e-10, 0.0, 10, ctypes.byref(info)) == -1
+    # transfer orders beyond p = 9
+    assert d.lib.gbpa_ptransfer_create(d.ctx, 1, 2, 8, None, None, None, 11, 1331, None, None, None, None, 0,
+                                       ctypes.byref(h)) == -2
+    # the hierarchy still works
+    y = torch.empty_like(b)
+    M.Mult(b, y)
+    assert torch.isfinite(y).all()
