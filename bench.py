@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--combined-n", type=int, default=24, help="54: ~19.9 M DOFs at p=5")
     ap.add_argument("--no-reference", action="store_true", help="combined form: skip the FP64 reference solve")
     ap.add_argument("--mg", action="store_true", help="run only the p-multigrid-preconditioned solve")
+    ap.add_argument("--sweep", action="store_true", help="run only the p = 1..8 apply sweep")
+    ap.add_argument("--sweep-dofs", type=float, default=8e6)
     ap.add_argument("--mg-n", type=int, default=77)
     ap.add_argument("--mg-jacobi", action="store_true", help="p-multigrid form: also time FP64 Jacobi-PCG")
     return ap.parse_args()
@@ -562,6 +564,55 @@ def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
             "problems_per_order": {str(q): orders.count(q) for q in range(2, 7)}}
 
 
+def run_sweep_form(target_dofs=8e6, reps=20, orders=range(1, 9)):
+    """The operator-apply sweep: orders p = 1..8 on the jittered hex mesh with
+    n = round(target_dofs^(1/3) / p) elements per side, q = p + 2, x ~
+    U[-1, 1]; diffusion and mass L->L applies in FP64, double-float and FP32,
+    `reps` applies timed with CUDA events after 3 warm-up applies (inputs larger
+    than L2). GDOF/s and the algorithmic-bytes HBM
+    fraction for each; the double-float and FP32 results' relative L2 error
+    against FP64."""
+    import torch
+    from mfem_gb300 import fem
+    from mfem_gb300.pa import PAOperator
+    peak = measured_peak_hbm()[0]
+    out = {"workload": f"jittered hex mesh, ~{target_dofs:.0e} DOFs per order, q = p + 2, x ~ U[-1,1]"}
+    for p in orders:
+        n = max(2, int(round(target_dofs ** (1.0 / 3.0) / p)))
+        for kind in ("diffusion", "mass"):
+            fes, integ, kid = build_problem(n, p, kind)
+            x = torch.from_numpy(2.0 * fem.u01_array(2, fes.ndofs) - 1.0).cuda()
+            y64 = torch.empty_like(x)
+            row = {"n": n, "ndofs": fes.ndofs}
+            for name, prec, w in (("f64", 0, 8), ("f64x2", 2, 8), ("f32", 1, 4)):
+                op = PAOperator(kid, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, precision=prec)
+                xx = x.float() if prec == 1 else x
+                yy = torch.empty_like(xx)
+                for _ in range(3):
+                    op.Mult(xx, yy)
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for _ in range(reps):
+                    op.Mult(xx, yy)
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / reps
+                ent = {"ms": round(ms, 4), "gdofs": round(fes.ndofs / (ms * 1e-3) / 1e9, 3),
+                       "hbm_frac_alg": round(algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, w, kind, False)
+                                             / (ms * 1e-3) / 1e9 / peak, 4)}
+                if prec == 0:
+                    y64.copy_(yy)
+                else:
+                    ent["rel_l2_vs_f64"] = float(torch.linalg.norm(yy.double() - y64) / torch.linalg.norm(y64))
+                row[name] = ent
+                del op
+            out[f"{kind}_p{p}"] = row
+            del fes, integ
+            torch.cuda.empty_cache()
+    return out
+
+
 def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
     """p-multigrid (next step past the Jacobi preconditioner): the precision
     form's problem (jittered n^3 mesh, lognormal kappa, RHS ~ U[0,1], seed 4,
@@ -713,6 +764,11 @@ def main():
         from mfem_gb300.pa import Device
         Device("cuda", dist_info()[2])
         print(json.dumps({"batched": run_batched_form(args.nprob)}), flush=True)
+        return 0
+    if args.sweep:
+        from mfem_gb300.pa import Device
+        Device("cuda", dist_info()[2])
+        print(json.dumps({"sweep": run_sweep_form(args.sweep_dofs)}), flush=True)
         return 0
     if args.mg:
         from mfem_gb300.pa import Device
