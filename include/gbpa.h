@@ -215,6 +215,17 @@ int gbpa_operator_destroy(gbpa_operator_t op);
 /* y = A x (L-vectors, the descriptor's precision). With ess dofs:
  * y = A (x with ess zeroed), then y[ess] = x[ess]. */
 int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y);
+/* gbpa_operator_mult with x and y in HOST memory; returns when y holds the
+ * result. Replaces the host<->device transfers MFEM's memory manager makes
+ * around a device Mult of host-valid Vectors (Vector::Read ->
+ * MemoryManager::Read_, general/mem_manager.cpp:1109-1131, copies x to the
+ * device; Vector::HostRead of y copies it back). Pinned buffers (cudaHostAlloc,
+ * cudaHostRegister) are device-mapped: the element kernel gathers x and the
+ * scatter writes y through them directly over the host-device link (NVLink-C2C
+ * on Grace-Blackwell), so the transfers run inside the apply instead of
+ * before and after it. Pageable buffers are staged through device scratch
+ * with cudaMemcpyAsync. */
+int gbpa_operator_mult_host(gbpa_operator_t op, const void *x, void *y);
 /* Element part of the operator alone: yE = A_e (R x) with the gather of x
  * fused into the sum-factorised apply (ElementRestriction::Mult followed by
  * AddMultPA on a zeroed E-vector, fem/bilinearform_ext.cpp:530-546). yE is

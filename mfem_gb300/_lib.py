@@ -85,6 +85,7 @@ SIGNATURES = {
     "gbpa_operator_create": (I, [P, ctypes.POINTER(OperatorDesc), ctypes.POINTER(P)]),
     "gbpa_operator_destroy": (I, [P]),
     "gbpa_operator_mult": (I, [P, P, P]),
+    "gbpa_operator_mult_host": (I, [P, P, P]),
     "gbpa_operator_apply_element": (I, [P, P, P]),
     "gbpa_operator_assemble_diagonal": (I, [P, P]),
     "gbpa_diffusion_mult_noalloc": (I, [P, I, I, I, I, I, P, P, P, P, P, P, P, P]),

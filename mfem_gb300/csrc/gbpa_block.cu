@@ -36,12 +36,11 @@ struct BlockState
 
 // Sums of a per-thread value grouped by right-hand side r = threadIdx.x % R
 // (the grid-stride step is a multiple of R, so each thread keeps one r).
-// Publishes the block's R partials; returns true in the last block, where
-// tot[r] (shared) holds the grid totals summed in block order.
-__device__ bool finish_rhs(double s, int R, double *partials, unsigned int *counter, double *tot)
+// block_sum_rhs: block sums of s grouped by r, in a fixed order; on return
+// out[r] (shared) holds them for every thread.
+__device__ void block_sum_rhs(double s, int R, double *out)
 {
    __shared__ double ws[32][BK_MAXR];
-   __shared__ bool last;
    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
    for (int o = 16; o >= R; o >>= 1) { s += __shfl_down_sync(0xffffffffu, s, o); }
    if (lane < R) { ws[wid][lane] = s; }
@@ -50,7 +49,22 @@ __device__ bool finish_rhs(double s, int R, double *partials, unsigned int *coun
    {
       double t = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ws[w][threadIdx.x]; }
-      partials[blockIdx.x * R + threadIdx.x] = t;
+      out[threadIdx.x] = t;
+   }
+   __syncthreads();
+}
+
+// Publishes the block's R partials; returns true in the last block, where
+// tot[r] (shared) holds the grid totals. The last block reads the partials
+// with all its threads (thread t takes blocks t / R, t / R + blockDim.x / R,
+// ... of right-hand side t % R) and reduces them with the same fixed-order
+// tree, so the totals are deterministic for a given grid.
+__device__ bool publish_rhs(int R, double *partials, unsigned int *counter, double *tot)
+{
+   __shared__ bool last;
+   if (threadIdx.x < R)
+   {
+      partials[blockIdx.x * R + threadIdx.x] = tot[threadIdx.x];
       __threadfence();
    }
    __syncthreads();
@@ -58,14 +72,44 @@ __device__ bool finish_rhs(double s, int R, double *partials, unsigned int *coun
    __syncthreads();
    if (!last) { return false; }
    __threadfence();
+   const int q = threadIdx.x % R, G = blockDim.x / R;
+   double t = 0.0;
+   for (int b = threadIdx.x / R; b < (int)gridDim.x; b += G) { t += __ldcg(partials + b * R + q); }
+   block_sum_rhs(t, R, tot);
+   return true;
+}
+
+__device__ bool finish_rhs(double s, int R, double *partials, unsigned int *counter, double *tot)
+{
+   block_sum_rhs(s, R, tot);
+   return publish_rhs(R, partials, counter, tot);
+}
+
+// Block sums of a thread's R values s[r], in a fixed order; on return out[r]
+// (shared) holds them for every thread.
+template <int R>
+__device__ void block_sum_vec(double (&s)[R], double *out)
+{
+   __shared__ double ws[32][R];
+   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+   for (int r = 0; r < R; ++r)
+   {
+      for (int o = 16; o > 0; o >>= 1) { s[r] += __shfl_down_sync(0xffffffffu, s[r], o); }
+   }
+   if (lane == 0)
+   {
+#pragma unroll
+      for (int r = 0; r < R; ++r) { ws[wid][r] = s[r]; }
+   }
+   __syncthreads();
    if (threadIdx.x < R)
    {
       double t = 0.0;
-      for (int b = 0; b < (int)gridDim.x; ++b) { t += ((volatile double *)partials)[b * R + threadIdx.x]; }
-      tot[threadIdx.x] = t;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ws[w][threadIdx.x]; }
+      out[threadIdx.x] = t;
    }
    __syncthreads();
-   return true;
 }
 
 template <typename T>
@@ -81,7 +125,7 @@ __global__ void blk_init_kernel(int64_t n, int R, const T *__restrict__ b, T *__
       const T rk = b[k];
       x[k] = T(0);
       r[k] = rk;
-      const T zk = dinv[k / R] * rk;
+      const T zk = dinv[k >> (__ffs(R) - 1)] * rk;
       z[k] = zk;
       d[k] = zk;
       s += (double)zk * (double)rk;
@@ -107,28 +151,34 @@ __global__ void blk_init_kernel(int64_t n, int R, const T *__restrict__ b, T *__
    }
 }
 
-template <typename T>
-__global__ void blk_scatter_den_kernel(int ndofs, int R, const int *__restrict__ offsets,
+// z = CSR scatter of the block E-vector (z[ess] = d[ess]) and den_r = (d_r, z_r),
+// one thread per dof for all R right-hand sides (vector loads of the R
+// interleaved values; z and d are internal, so aligned to R * sizeof(T)).
+template <typename T, int R>
+__global__ void blk_scatter_den_kernel(int ndofs, const int *__restrict__ offsets,
                                        const int *__restrict__ indices, const T *__restrict__ yE,
                                        T *__restrict__ z, const T *__restrict__ d,
                                        const unsigned char *__restrict__ mask, double *partials,
                                        BlockState *st, int first)
 {
    if (st->all_done) { return; }
+   using V = RhsVec<T, R>;
    __shared__ double tot[BK_MAXR];
-   const int64_t n = (int64_t)ndofs * R;
-   double s = 0.0;
-   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-        k += (int64_t)gridDim.x * blockDim.x)
+   double s[R];
+#pragma unroll
+   for (int r = 0; r < R; ++r) { s[r] = 0.0; }
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndofs; i += gridDim.x * blockDim.x)
    {
-      const int i = (int)(k / R), q = (int)(k % R);
-      T v;
-      if (mask && mask[i]) { v = d[k]; }
-      else { v = csr_row_sum<T>(offsets, indices, yE, i, false, R, q); }
-      z[k] = v;
-      s += (double)d[k] * (double)v;
+      const V dv = reinterpret_cast<const V *>(d)[i];
+      V v;
+      if (mask && mask[i]) { v = dv; }
+      else { csr_row_sum_rhs<T, R>(offsets, indices, yE, i, v.v); }
+      reinterpret_cast<V *>(z)[i] = v;
+#pragma unroll
+      for (int r = 0; r < R; ++r) { s[r] += (double)dv.v[r] * (double)v.v[r]; }
    }
-   if (finish_rhs(s, R, partials, &st->counter[1], tot) && threadIdx.x == 0)
+   block_sum_vec<R>(s, tot);
+   if (publish_rhs(R, partials, &st->counter[1], tot) && threadIdx.x == 0)
    {
       int active = 0;
       for (int q = 0; q < R; ++q)
@@ -167,7 +217,7 @@ __global__ void blk_update_kernel(int64_t n, int R, T *__restrict__ x, T *__rest
       x[k] += alpha * d[k];
       const T rk = r[k] - alpha * z[k];
       r[k] = rk;
-      const T zk = dinv[k / R] * rk;
+      const T zk = dinv[k >> (__ffs(R) - 1)] * rk;
       z[k] = zk;
       s += (double)rk * (double)zk;
    }
@@ -217,7 +267,7 @@ __global__ void blk_scatter_kernel(int ndofs, int R, const int *__restrict__ off
    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
         k += (int64_t)gridDim.x * blockDim.x)
    {
-      const int i = (int)(k / R), q = (int)(k % R);
+      const int i = (int)(k >> (__ffs(R) - 1)), q = (int)(k & (R - 1));   // R is a power of two
       if (mask && mask[i]) { y[k] = xc[k]; continue; }
       y[k] = csr_row_sum<T>(offsets, indices, yE, i, false, R, q);
    }
@@ -319,6 +369,26 @@ static int block_mult(gbpa_operator *op, int R, const T *x, T *y)
    return last_launch(op->ctx, "blk_scatter");
 }
 
+template <typename T>
+static int launch_scatter_den(gbpa_operator *op, int R, T *z, const T *d, double *partials,
+                              BlockState *st, int first)
+{
+   gbpa_ctx *ctx = op->ctx;
+   // 256 threads: the R = 8 variants hold 80-96 registers, three blocks per SM
+   constexpr int BS = 256;
+   const unsigned grid = grid_for(op->d.ndofs, BS, 8 * ctx->num_sms);
+   const T *yE = (const T *)op->yEb;
+   const gbpa_operator_desc &od = op->d;
+   switch (R)
+   {
+   case 1: blk_scatter_den_kernel<T, 1><<<grid, BS, 0, ctx->stream>>>(od.ndofs, od.offsets, od.indices, yE, z, d, op->mask, partials, st, first); break;
+   case 2: blk_scatter_den_kernel<T, 2><<<grid, BS, 0, ctx->stream>>>(od.ndofs, od.offsets, od.indices, yE, z, d, op->mask, partials, st, first); break;
+   case 4: blk_scatter_den_kernel<T, 4><<<grid, BS, 0, ctx->stream>>>(od.ndofs, od.offsets, od.indices, yE, z, d, op->mask, partials, st, first); break;
+   default: blk_scatter_den_kernel<T, 8><<<grid, BS, 0, ctx->stream>>>(od.ndofs, od.offsets, od.indices, yE, z, d, op->mask, partials, st, first); break;
+   }
+   return last_launch(ctx, "blk_scatter_den");
+}
+
 struct BlockWork
 {
    void *r = nullptr, *d = nullptr, *z = nullptr;
@@ -359,10 +429,7 @@ static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T 
    if (!rc) { rc = block_apply_evec<T>(op, R, d, &w.st->all_done); }
    if (!rc)
    {
-      blk_scatter_den_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(
-         op->d.ndofs, R, op->d.offsets, op->d.indices, (const T *)op->yEb, z, d, op->mask,
-         w.partials + 4096 * 4, w.st, 1);
-      rc = last_launch(ctx, "blk_scatter_den");
+      rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 1);
    }
    const int K = 10;
    int *h_done = (int *)ctx->h_pinned;
@@ -385,10 +452,7 @@ static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T 
          if (!rc) { rc = block_apply_evec<T>(op, R, d, &w.st->all_done); }
          if (!rc)
          {
-            blk_scatter_den_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(
-               op->d.ndofs, R, op->d.offsets, op->d.indices, (const T *)op->yEb, z, d, op->mask,
-               w.partials + 4096 * 4, w.st, 0);
-            rc = last_launch(ctx, "blk_scatter_den");
+            rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 0);
          }
       }
    }

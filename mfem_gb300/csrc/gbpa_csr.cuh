@@ -46,4 +46,51 @@ __device__ __forceinline__ T csr_row_sum(const int *__restrict__ offsets, const 
    }
    return v;
 }
+
+// R interleaved values of one E-vector slot (or one dof), loaded as one
+// vector: R * sizeof(T) bytes, aligned to that size.
+template <typename T, int R>
+struct alignas(sizeof(T) * R) RhsVec
+{
+   T v[R];
+};
+
+// csr_row_sum for all R interleaved right-hand sides of row i at once:
+// the row's indices are loaded once, each slot's R values in one vector load,
+// and out[r] is summed in row order (bit-identical to csr_row_sum with
+// stride R, lane r). U slots are in flight per thread, 128 bytes of values.
+template <typename T, int R>
+__device__ __forceinline__ void csr_row_sum_rhs(const int *__restrict__ offsets,
+                                                const int *__restrict__ indices,
+                                                const T *__restrict__ xE, int i, T (&out)[R])
+{
+   constexpr int UB = 128 / int(sizeof(T) * R);
+   constexpr int U = UB < 1 ? 1 : (UB > 8 ? 8 : UB);
+   using V = RhsVec<T, R>;
+   const V *xv = reinterpret_cast<const V *>(xE);
+#pragma unroll
+   for (int r = 0; r < R; ++r) { out[r] = T(0); }
+   const int j0 = offsets[i], j1 = offsets[i + 1];
+   for (int j = j0; j < j1; j += U)
+   {
+      int s[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) { s[u] = j + u < j1 ? indices[j + u] : 0; }
+      V a[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+         if (j + u < j1) { a[u] = xv[s[u] >= 0 ? s[u] : -1 - s[u]]; }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+         if (j + u < j1)
+         {
+#pragma unroll
+            for (int r = 0; r < R; ++r) { out[r] += s[u] >= 0 ? a[u].v[r] : -a[u].v[r]; }
+         }
+      }
+   }
+}
 } // namespace gbpa

@@ -315,7 +315,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->gmap_m); cudaFree(op->qd2);
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
-   cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb);
+   cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb); cudaFree(op->stage);
    delete op;
    return GBPA_SUCCESS;
 }
@@ -363,6 +363,49 @@ extern "C" int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y)
    if (op->d.ndofs == 0) { return GBPA_SUCCESS; }
    if (op->d.precision != GBPA_F32) { return op_mult<double>(op, (const double *)x, (double *)y); }
    return op_mult<float>(op, (const float *)x, (float *)y);
+}
+
+// Device address of a host buffer the kernels can access directly: memory
+// pinned by cudaHostAlloc / cudaHostRegister (device-mapped under unified
+// addressing). Pageable memory returns nullptr.
+static void *mapped_host_ptr(const void *p)
+{
+   cudaPointerAttributes a{};
+   if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+   {
+      cudaGetLastError();   // an unregistered pointer is not an error here
+      return nullptr;
+   }
+   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+extern "C" int gbpa_operator_mult_host(gbpa_operator_t op, const void *x, void *y)
+{
+   if (!op || (op->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (op->d.ndofs == 0) { return GBPA_SUCCESS; }
+   gbpa_ctx *ctx = op->ctx;
+   const size_t bytes = (size_t)op->d.ndofs * (op->d.precision == GBPA_F32 ? 4 : 8);
+   void *dx = mapped_host_ptr(x), *dy = mapped_host_ptr(y);
+   const bool stage_x = !dx, stage_y = !dy;
+   int rc = GBPA_SUCCESS;
+   if ((stage_x || stage_y) && !op->stage)
+   {
+      rc = check_cuda(cudaMalloc(&op->stage, 2 * bytes), "cudaMalloc(host staging)");
+      if (rc) { op->stage = nullptr; return rc; }
+   }
+   if (stage_x)
+   {
+      dx = op->stage;
+      rc = check_cuda(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy x");
+   }
+   if (stage_y) { dy = (unsigned char *)op->stage + bytes; }
+   if (!rc) { rc = gbpa_operator_mult(op, dx, dy); }
+   if (!rc && stage_y)
+   {
+      rc = check_cuda(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy y");
+   }
+   const int rs = check_cuda(cudaStreamSynchronize(ctx->stream), "sync");
+   return rc ? rc : rs;
 }
 
 extern "C" int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, void *yE)

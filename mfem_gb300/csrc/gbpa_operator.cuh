@@ -36,6 +36,8 @@ struct gbpa_operator
    // block (multi right-hand side) scratch: E-vector for nrhs interleaved
    void *yEb = nullptr;
    int yEb_nrhs = 0;
+   // host-buffer Mult: device staging for pageable x / y (2 L-vectors)
+   void *stage = nullptr;
 };
 
 namespace gbpa

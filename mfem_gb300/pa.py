@@ -354,6 +354,16 @@ class PAOperator:
     def Mult(self, x, y):
         check(_dev().lib.gbpa_operator_mult(self.handle, _p(x), _p(y)), "operator_mult")
 
+    def MultHost(self, x, y):
+        """Mult of host (CPU) tensors; returns when y holds the result. Pinned
+        tensors are read and written by the kernels in place; pageable ones
+        are staged through device scratch."""
+        if x.device.type != "cpu" or y.device.type != "cpu":
+            raise ValueError("MultHost takes CPU tensors")
+        if not (x.is_contiguous() and y.is_contiguous()) or x.numel() != self.ndofs or y.numel() != self.ndofs:
+            raise ValueError("MultHost takes contiguous vectors of ndofs entries")
+        check(_dev().lib.gbpa_operator_mult_host(self.handle, _p(x), _p(y)), "operator_mult_host")
+
     def AssembleDiagonal(self, diag):
         check(_dev().lib.gbpa_operator_assemble_diagonal(self.handle, _p(diag)), "operator_assemble_diagonal")
 

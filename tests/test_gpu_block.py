@@ -53,12 +53,13 @@ def test_block_mult_equals_single(R, prec):
             assert float(torch.linalg.norm(Y[:, r] - y) / torch.linalg.norm(y)) < 1e-6
 
 
-def test_block_pcg_matches_single_solves():
+@pytest.mark.parametrize("R", [1, 2, 4, 8])
+def test_block_pcg_matches_single_solves(R):
     from mfem_gb300 import _lib
     from tests.gpu_util import dev
     d = dev()
     fes, integ, A, A32, M, e = problem(4, 4)
-    n, R = fes.ndofs, 4
+    n = fes.ndofs
     gen = torch.Generator(device="cuda").manual_seed(12)
     B = torch.rand(n, R, dtype=torch.float64, device="cuda", generator=gen)
     B[torch.from_numpy(e).long().cuda()] = 0.0
