@@ -98,6 +98,39 @@ def algorithmic_bytes(ne, ndofs, D, Q, w, kind, element_only):
     return qd + maps + 2 * ndofs * w
 
 
+def element_flops(D, Q, kind):
+    """Algorithmic floating-point operations (an FMA = 2) of one element's
+    sum-factorised apply, in the kernel's contraction order. Diffusion:
+    x, y, z forward (2 D^3 Q + 3 D^2 Q^2 + 3 D Q^3 FMA), the symmetric 3x3
+    qdata product (9 Q^3), the same contractions backward. Mass: one field,
+    D^3 Q + D^2 Q^2 + D Q^3 each way, and Q^3 products."""
+    if kind == "diffusion":
+        fwd = 2 * D ** 3 * Q + 3 * D ** 2 * Q ** 2 + 3 * D * Q ** 3
+        return 2 * (2 * fwd + 9 * Q ** 3)
+    fwd = D ** 3 * Q + D ** 2 * Q ** 2 + D * Q ** 3
+    return 2 * (2 * fwd) + Q ** 3
+
+
+def measured_fp64_peak_tflops():
+    """The FP64 rate of this GPU, measured now: cuBLAS DGEMM 4096^3 (2 N^3
+    operations), best of 3 after one warm-up, CUDA events."""
+    import torch
+    n = 4096
+    a = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    b = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    c = a @ b
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -306,6 +339,14 @@ def run_gpu(args):
     peak, peak_kind = measured_peak_hbm()
     achieved = kbytes / (k_ms * 1e-3) / 1e9
     traffic, traffic_src = profiled_traffic(args.precision, args.kind, args.p, ne)
+    fp64_roof = None
+    if prec == 0:
+        fpe = element_flops(D, Q, args.kind)
+        fp64_ach = ne * fpe / (k_ms * 1e-3) / 1e12
+        fp64_peak = measured_fp64_peak_tflops()
+        fp64_roof = {"achieved": fp64_ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": fp64_ach / fp64_peak,
+                     "flops_per_element": fpe,
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (best of 3)"}
 
     # ---- end to end through the C ABI with host buffers (pinned): the
     # host-buffer Mult, whose kernels gather x from and scatter y to the
@@ -358,9 +399,10 @@ def run_gpu(args):
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                      "kernel": f"{args.kind}_apply (gather fused)",
                      "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind,
-                     "note": ("native FP64 is FP64-pipe bound on GB300 (1.26 TFLOP/s; ncu: FP64 pipe "
-                              "91.5% active); see f64x2_apply for the double-float form")
-                     if prec == 0 else None},
+                     "note": ("native FP64 is FP64-pipe bound on GB300 (ncu: FP64 pipe 91.5% active); "
+                              "fp64 below is the arithmetic roofline; see f64x2_apply for the double-float form")
+                     if prec == 0 else None,
+                     "fp64": fp64_roof},
         "e2e": {"value": e2e, "unit": "GDOF/s", "h2d_bytes_per_step": ndofs * wbytes,
                 "d2h_bytes_per_step": ndofs * wbytes, "api": "gbpa_operator_mult_host (pinned buffers, "
                 "read and written in place over the host link)", "staged_copies_value": e2e_staged},
