@@ -111,6 +111,26 @@ def element_flops(D, Q, kind):
     return 2 * (2 * fwd) + Q ** 3
 
 
+def measured_hbm_live_gbs():
+    """HBM copy bandwidth measured now, the same way as the pool's peak file:
+    b.copy_(a) over 2^30 bf16 elements (read + write bytes), best of 10."""
+    import torch
+    a = torch.empty(1 << 30, dtype=torch.bfloat16, device="cuda")
+    b = torch.empty_like(a)
+    b.copy_(a)
+    best = float("inf")
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    nbytes = 2 * a.numel() * a.element_size()
+    del a, b
+    return nbytes / (best * 1e-3) / 1e9
+
+
 def measured_fp64_peak_tflops():
     """The FP64 rate of this GPU, measured now: cuBLAS DGEMM 4096^3 (2 N^3
     operations), best of 3 after one warm-up, CUDA events."""
@@ -220,7 +240,7 @@ def build_problem(n, p, kind, seed_jitter=1):
     return fes, integ, kind_id
 
 
-def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1):
+def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False):
     """The oracle's L->L apply (gather, element kernel, CSR scatter) on the
     host cores, set up by the oracle itself from the same synthetic mesh."""
     from mfem_gb300 import fem
@@ -247,7 +267,19 @@ def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1):
     for _ in range(steps):
         o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
     dt = time.perf_counter() - t0
-    return sp.ndofs * steps / dt / 1e9, sp.ndofs, o.num_threads(), dt
+    threads = o.num_threads()
+    if not single_thread:
+        return sp.ndofs * steps / dt / 1e9, sp.ndofs, threads, dt
+    # the same applies on one thread
+    o.set_num_threads(1)
+    try:
+        t1 = time.perf_counter()
+        for _ in range(steps):
+            o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+        dt1 = time.perf_counter() - t1
+    finally:
+        o.set_num_threads(threads)
+    return sp.ndofs * steps / dt / 1e9, sp.ndofs, threads, dt, sp.ndofs * steps / dt1 / 1e9
 
 
 # ------------------------------------------------------------------- reference arm
@@ -337,6 +369,7 @@ def run_gpu(args):
     k_ms = k0.elapsed_time(k1) / nk
     kbytes = algorithmic_bytes(ne, ndofs, D, Q, wbytes, args.kind, element_only=True)
     peak, peak_kind = measured_peak_hbm()
+    hbm_live = measured_hbm_live_gbs()
     achieved = kbytes / (k_ms * 1e-3) / 1e9
     traffic, traffic_src = profiled_traffic(args.precision, args.kind, args.p, ne)
     fp64_roof = None
@@ -399,6 +432,7 @@ def run_gpu(args):
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                      "kernel": f"{args.kind}_apply (gather fused)",
                      "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind,
+                     "peak_live": hbm_live, "frac_live": achieved / hbm_live,
                      "note": ("native FP64 is FP64-pipe bound on GB300 (ncu: FP64 pipe 91.5% active); "
                               "fp64 below is the arithmetic roofline; see f64x2_apply for the double-float form")
                      if prec == 0 else None,
@@ -411,10 +445,12 @@ def run_gpu(args):
     }
     if rank == 0:
         try:
-            rate, sn, threads, dt = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, 3)
+            rate, sn, threads, dt, rate1 = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, 3,
+                                                                 single_thread=True)
             line["cpu_baseline"] = {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
                                     "sample": f"3 applies of the n={args.cpu_sample_n} p={args.p} mesh "
-                                              f"({sn} DOFs), {dt:.1f} s"}
+                                              f"({sn} DOFs), {dt:.1f} s",
+                                    "value_1_thread": rate1}
         except Exception as e:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
         line.update(extras)

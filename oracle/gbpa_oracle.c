@@ -27,6 +27,15 @@ int or_num_threads(void)
 #endif
 }
 
+void or_set_num_threads(int n)
+{
+#ifdef _OPENMP
+   if (n > 0) { omp_set_num_threads(n); }
+#else
+   (void)n;
+#endif
+}
+
 /* ------------------------------------------------------------ restriction */
 void or_restriction_build(int ne, int dof, int ndofs, const int *elem_dofs,
                           const int *dof_map, int *offsets, int *indices,
@@ -750,8 +759,7 @@ int or_pcg_diffusion(int ne, int ndofs, int symm, int d1d, int q1d,
       memset(x, 0, sizeof(double) * n);
    }
    /* OperatorJacobiSmoother::Mult, non-iterative mode: z = dinv .* r */
-   for (int k = 0; k < n; ++k) { z[k] = dinv[k] * r[k]; }
-   memcpy(d, z, sizeof(double) * n);
+   for (int k = 0; k < n; ++k) { z[k] = dinv[k] * r[k]; d[k] = z[k]; }
    nom0 = nom = dot(n, d, r);
    *converged = 0;
    if (nom < 0.0 || !isfinite(nom)) { *final_norm = nom; goto done; }

@@ -142,6 +142,8 @@ void or_domain_lf3d(int ne, int d1d, int q1d, const double *B, const double *W,
 
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int or_num_threads(void);
+/* Threads of the following OpenMP regions (timing the CPU baseline at 1 thread). */
+void or_set_num_threads(int n);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,7 @@ _SIGS = {
     "or_pcg_diffusion": [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,
                          _P, _P, _P, _D, _D, _I, _I, _P, _P],
     "or_num_threads": [],
+    "or_set_num_threads": [_I],
     "or_boolean_mask": [_I, _I, _P, _P, _P],
     "or_ptransfer_mult": [_P, _P, _P, _P],
     "or_ptransfer_mult_transpose": [_P, _P, _P, _P],
@@ -188,6 +189,9 @@ class Oracle:
 
     def num_threads(self):
         return self.lib.or_num_threads()
+
+    def set_num_threads(self, n):
+        self.lib.or_set_num_threads(int(n))
 
     def domain_lf3d(self, ne, d1d, q1d, B, W, detJ, f, ndofs, off, ind):
         b = np.zeros(ndofs)
