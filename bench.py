@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "x2"],
                     help="arithmetic of the timed operator (x2: FP64 data, double-float on FP32 pipes)")
-    ap.add_argument("--cpu-sample-n", type=int, default=38)
+    ap.add_argument("--cpu-sample-n", type=int, default=None,
+                    help="mesh of the CPU baseline (default: the GPU workload's n)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU baseline: applies timed for about this long")
     ap.add_argument("--no-pcg", action="store_true", help="skip the precision-form PCG comparison")
     ap.add_argument("--pcg-n", type=int, default=40,
                     help="mesh size of the precision-form PCG comparison (77: ~29.5 M DOFs at p=4)")
@@ -240,9 +243,11 @@ def build_problem(n, p, kind, seed_jitter=1):
     return fes, integ, kind_id
 
 
-def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False):
+def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False, seconds=None):
     """The oracle's L->L apply (gather, element kernel, CSR scatter) on the
-    host cores, set up by the oracle itself from the same synthetic mesh."""
+    host cores, set up by the oracle itself from the same synthetic mesh.
+    seconds: instead of `steps`, time as many applies as fit in about that
+    long (at least 3), from the warm-up apply's duration."""
     from mfem_gb300 import fem
     from tests import oracle_lib
     o = oracle_lib.load()
@@ -261,8 +266,12 @@ def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False):
     del J
     x = 2 * fem.u01_array(2, sp.ndofs) - 1
     kid = 0 if kind == "diffusion" else 1
-    for _ in range(warmup):
+    tw = time.perf_counter()
+    for _ in range(max(warmup, 1)):
         o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+    tw = (time.perf_counter() - tw) / max(warmup, 1)
+    if seconds is not None:
+        steps = int(min(max(3, seconds / max(tw, 1e-6)), 1000))
     t0 = time.perf_counter()
     for _ in range(steps):
         o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
@@ -270,16 +279,16 @@ def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False):
     threads = o.num_threads()
     if not single_thread:
         return sp.ndofs * steps / dt / 1e9, sp.ndofs, threads, dt
-    # the same applies on one thread
+    # two applies on one thread
     o.set_num_threads(1)
     try:
         t1 = time.perf_counter()
-        for _ in range(steps):
+        for _ in range(2):
             o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
         dt1 = time.perf_counter() - t1
     finally:
         o.set_num_threads(threads)
-    return sp.ndofs * steps / dt / 1e9, sp.ndofs, threads, dt, sp.ndofs * steps / dt1 / 1e9
+    return sp.ndofs * steps / dt / 1e9, sp.ndofs, threads, dt, sp.ndofs * 2 / dt1 / 1e9, steps
 
 
 # ------------------------------------------------------------------- reference arm
@@ -288,17 +297,18 @@ def run_reference(args):
     if rank != 0:
         return 0
     steps, warm = args.steps, args.warmup
-    rate, ndofs, threads, dt = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, steps,
+    sample_n = args.cpu_sample_n or args.n
+    rate, ndofs, threads, dt = cpu_oracle_apply_rate(sample_n, args.p, args.kind, steps,
                                                      warmup=min(warm, 2))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "GDOF/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"PA {args.kind} apply L->L, jittered hex mesh, p={args.p}, "
-                               f"q={args.p + 2}; each step one apply on the n={args.cpu_sample_n} "
-                               f"sample mesh ({ndofs} DOFs)", "p": args.p, "n": args.cpu_sample_n},
+                               f"q={args.p + 2}; each step one apply on the n={sample_n} "
+                               f"mesh ({ndofs} DOFs)", "p": args.p, "n": sample_n},
         "cpu_baseline": {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} applies of the n={args.cpu_sample_n} p={args.p} mesh "
+                         "sample": f"{steps} applies of the n={sample_n} p={args.p} mesh "
                                    f"({ndofs} DOFs), OpenMP over elements/dofs"},
         "e2e": {"value": rate, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -445,11 +455,12 @@ def run_gpu(args):
     }
     if rank == 0:
         try:
-            rate, sn, threads, dt, rate1 = cpu_oracle_apply_rate(args.cpu_sample_n, args.p, args.kind, 3,
-                                                                 single_thread=True)
+            sample_n = args.cpu_sample_n or args.n
+            rate, sn, threads, dt, rate1, csteps = cpu_oracle_apply_rate(
+                sample_n, args.p, args.kind, 3, single_thread=True, seconds=args.cpu_seconds)
             line["cpu_baseline"] = {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
-                                    "sample": f"3 applies of the n={args.cpu_sample_n} p={args.p} mesh "
-                                              f"({sn} DOFs), {dt:.1f} s",
+                                    "sample": f"{csteps} applies of the n={sample_n} p={args.p} mesh "
+                                              f"({sn} DOFs), {dt:.1f} s; 1 thread: 2 applies",
                                     "value_1_thread": rate1}
         except Exception as e:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}

@@ -128,6 +128,17 @@ int gbpa_geom_determinants3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
  * points, layout (Q^3, 3, NE). */
 int gbpa_geom_coordinates3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
                             const double *Bg, const double *X, double *XQ);
+/* Coefficient projection at the quadrature points on the device, replacing
+ * the host loop of Coefficient::Project(QuadratureFunction&) /
+ * CoefficientVector::Project (fem/coefficient.cpp:52-72,2058-2076) for the
+ * lognormal field kappa(x) = exp(sum_m amp cos(2 pi k_m . x + phi_m)) that the
+ * precision and combined forms use: out (nq, NE) from the physical
+ * coordinates XQ (nq, 3, NE) of gbpa_geom_coordinates3d (nq = Q^3).
+ * k (host, 3*nmodes integers), phi (host, nmodes), nmodes <= GBPA_MAX_MODES. */
+#define GBPA_MAX_MODES 64
+int gbpa_coefficient_lognormal3d(gbpa_ctx_t ctx, int ne, int nq, const double *XQ,
+                                 int nmodes, const int *k, const double *phi,
+                                 double amp, double *out);
 
 /* ------------------------------------------------------------ diffusion */
 /* PADiffusionSetup3D, fem/integ/bilininteg_diffusion_kernels.cpp:262-386.

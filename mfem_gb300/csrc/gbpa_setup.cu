@@ -326,6 +326,60 @@ extern "C" int gbpa_geom_coordinates3d(gbpa_ctx_t ctx, int ne, int dg, int q1d,
    return geom_common(ctx, ne, dg, q1d, Bg, nullptr, X, XQ, 2);
 }
 
+// Fourier modes of the lognormal coefficient, passed by value (kernel
+// parameter space, read through the constant cache: every thread reads the
+// same mode at the same time).
+struct LognormalModes
+{
+   int n;
+   double amp;
+   double k[GBPA_MAX_MODES][3];
+   double phi[GBPA_MAX_MODES];
+};
+
+// out(q, e) = exp(sum_m amp cos(2 pi k_m . x(q, e) + phi_m)), x from the
+// (Q^3, 3, NE) coordinates array.
+__global__ void lognormal_kernel(int64_t npts, int nq, const double *__restrict__ XQ,
+                                 const __grid_constant__ LognormalModes modes,
+                                 double *__restrict__ out)
+{
+   const double two_pi = 6.283185307179586476925286766559;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int64_t e = i / nq, q = i - e * nq;
+      const double *xe = XQ + e * 3 * nq + q;
+      const double x = xe[0], y = xe[nq], z = xe[2 * nq];
+      double g = 0.0;
+      for (int m = 0; m < modes.n; ++m)
+      {
+         const double a = two_pi * (modes.k[m][0] * x + modes.k[m][1] * y + modes.k[m][2] * z) + modes.phi[m];
+         g += modes.amp * cos(a);
+      }
+      out[i] = exp(g);
+   }
+}
+
+extern "C" int gbpa_coefficient_lognormal3d(gbpa_ctx_t ctx, int ne, int nq, const double *XQ,
+                                            int nmodes, const int *k, const double *phi, double amp,
+                                            double *out)
+{
+   if (!ctx || ne < 0 || nq < 1 || nmodes < 0 || nmodes > GBPA_MAX_MODES) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (ne == 0) { return GBPA_SUCCESS; }
+   if (!XQ || !out || (nmodes > 0 && (!k || !phi))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   LognormalModes m{};
+   m.n = nmodes;
+   m.amp = amp;
+   for (int i = 0; i < nmodes; ++i)
+   {
+      for (int d = 0; d < 3; ++d) { m.k[i][d] = (double)k[3 * i + d]; }
+      m.phi[i] = phi[i];
+   }
+   const int64_t n = (int64_t)ne * nq;
+   lognormal_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, nq, XQ, m, out);
+   return last_launch(ctx, "coefficient_lognormal");
+}
+
 static int coeff_ok(int coeff_dim, int64_t c_size, int64_t npts)
 {
    if (coeff_dim != 1 && coeff_dim != 3 && coeff_dim != 6 && coeff_dim != 9) { return 0; }

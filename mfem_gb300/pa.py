@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .fem import H1Space, Tables, kappa_eval
+from .fem import H1Space, Tables
 
 check = _lib.check
 
@@ -206,12 +206,19 @@ class _PAIntegrator:
         XQ = torch.empty(Q ** 3 * 3 * ne, dtype=torch.float64, device=dev.torch_device)
         check(dev.lib.gbpa_geom_coordinates3d(dev.ctx, ne, geom["dg"], Q, _p(geom["Bg"]),
                                               _p(geom["X"]), _p(XQ)), "geom_coordinates3d")
-        xyz = XQ.view(ne, 3, Q ** 3).permute(0, 2, 1)
         if c == "kappa":
-            vals = kappa_eval(xyz, geom["modes"])
-        else:
-            vals = c(xyz)
-        return vals.contiguous().view(-1), 1
+            # the lognormal field, evaluated by the library's kernel
+            k, phi = geom["modes"]
+            kk = np.ascontiguousarray(k, dtype=np.int32).reshape(-1)
+            ph = np.ascontiguousarray(phi, dtype=np.float64)
+            vals = torch.empty(Q ** 3 * ne, dtype=torch.float64, device=dev.torch_device)
+            check(dev.lib.gbpa_coefficient_lognormal3d(
+                dev.ctx, ne, Q ** 3, _p(XQ), len(ph), kk.ctypes.data_as(ctypes.c_void_p),
+                ph.ctypes.data_as(ctypes.c_void_p), 0.5, _p(vals)), "coefficient_lognormal3d")
+            return vals, 1
+        # a user function of the coordinates, evaluated by torch on the device
+        xyz = XQ.view(ne, 3, Q ** 3).permute(0, 2, 1)
+        return c(xyz).contiguous().view(-1), 1
 
 
 def _geometry(fes, tables, modes):

@@ -68,3 +68,36 @@ def test_linear_form_of_one_integrates_the_volume():
     lf.AddDomainIntegrator(DomainLFIntegrator(None))
     b = lf.Assemble()
     assert abs(float(b.sum()) - 1.0) < 1e-13
+
+
+def test_lognormal_coefficient_kernel_matches_numpy():
+    """gbpa_coefficient_lognormal3d against the same field evaluated by numpy
+    at the same quadrature coordinates (curved order-3 geometry)."""
+    import ctypes
+    import numpy as np
+    import torch
+    from mfem_gb300 import fem
+    from mfem_gb300.pa import FiniteElementSpace, _geometry
+    from tests.gpu_util import dev
+    d = dev()
+    mesh = fem.CartesianMesh(3, curved=True)
+    fes = FiniteElementSpace(mesh, 2)
+    t = fem.Tables(2, 5)
+    modes = fem.kappa_modes(3)
+    geom = _geometry(fes, t, modes)
+    ne, nq = fes.ne, 5 ** 3
+    XQ = torch.empty(nq * 3 * ne, dtype=torch.float64, device="cuda")
+    P = lambda a: ctypes.c_void_p(a.data_ptr())
+    assert d.lib.gbpa_geom_coordinates3d(d.ctx, ne, geom["dg"], 5, P(geom["Bg"]), P(geom["X"]), P(XQ)) == 0
+    k = np.ascontiguousarray(modes[0], np.int32).reshape(-1)
+    phi = np.ascontiguousarray(modes[1], np.float64)
+    out = torch.empty(nq * ne, dtype=torch.float64, device="cuda")
+    assert d.lib.gbpa_coefficient_lognormal3d(d.ctx, ne, nq, P(XQ), len(phi),
+                                              k.ctypes.data_as(ctypes.c_void_p),
+                                              phi.ctypes.data_as(ctypes.c_void_p), 0.5, P(out)) == 0
+    xyz = XQ.cpu().numpy().reshape(ne, 3, nq).transpose(0, 2, 1)
+    ref = fem.kappa_eval(xyz, modes).reshape(-1)
+    assert np.max(np.abs(out.cpu().numpy() - ref) / ref) < 1e-13
+    # invalid arguments
+    assert d.lib.gbpa_coefficient_lognormal3d(d.ctx, ne, nq, P(XQ), 65, k.ctypes.data_as(ctypes.c_void_p),
+                                              phi.ctypes.data_as(ctypes.c_void_p), 0.5, P(out)) < 0
