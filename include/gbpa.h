@@ -56,7 +56,8 @@ enum gbpa_error_flag
    GBPA_FLAG_NOT_FINITE = 1,
    GBPA_FLAG_ZERO_DIAGONAL = 2,
    GBPA_FLAG_INDEX = 4,
-   GBPA_FLAG_INDEFINITE = 8
+   GBPA_FLAG_INDEFINITE = 8,
+   GBPA_FLAG_TIMEOUT = 16      /* a bounded device wait ran out */
 };
 
 typedef struct gbpa_ctx *gbpa_ctx_t;
@@ -518,6 +519,16 @@ int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const double *b,
 int gbpa_set_elements_per_block(int kind, int precision, int d1d, int q1d,
                                 int nbz);
 int gbpa_get_elements_per_block(int kind, int precision, int d1d, int q1d);
+
+/* ------------------------------------------------ failure-detection test */
+/* No counterpart in the reference. Makes one of the library's bounded device
+ * waits run out on purpose -- the arrival it waits for never comes -- and
+ * reports what the wait reported: which = 0, the persistent batched kernel's
+ * grid barrier with one block never arriving (limit: spins); which = 1, the
+ * TMA staging mbarrier wait with no copy issued (limit: polls). Returns
+ * GBPA_ERR_TIMEOUT when the wait gave up as designed; the kernel has returned
+ * and the context stays usable. limit <= 2^26. */
+int gbpa_selftest_bounded_wait(gbpa_ctx_t ctx, int which, long long limit);
 
 #ifdef __cplusplus
 }

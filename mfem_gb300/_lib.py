@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbpa_geom_determinants3d": (I, [P, I, I, I, P, P, P, P]),
     "gbpa_geom_coordinates3d": (I, [P, I, I, I, P, P, P]),
     "gbpa_coefficient_lognormal3d": (I, [P, I, I, P, I, P, P, D, P]),
+    "gbpa_selftest_bounded_wait": (I, [P, I, ctypes.c_longlong]),
     "gbpa_diffusion_setup3d": (I, [P, I, I, I, P, P, P, I64, P]),
     "gbpa_diffusion_setup3d_nodes": (I, [P, I, I, I, I, P, P, P, P, P, I64, P]),
     "gbpa_diffusion_apply3d": (I, [P, I, I, I, I, P, P, P, P, P, P, P]),

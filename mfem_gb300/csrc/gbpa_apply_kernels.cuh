@@ -138,9 +138,10 @@ __device__ __forceinline__ void tma_load_1d(void *sdst, const void *gsrc, unsign
 // Returns false on expiry; the caller then writes NaN for its element, so a
 // copy that never lands shows up as a non-finite result (PCG reports
 // GBPA_ERR_NOT_FINITE) and the kernel always terminates.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          long long max_polls = 1LL << 24)
 {
-   for (long long it = 0; it < (1LL << 24); ++it)
+   for (long long it = 0; it < max_polls; ++it)
    {
       unsigned ok;
       asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"

@@ -905,9 +905,67 @@ static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *prob
    if (flags & GBPA_FLAG_NOT_FINITE) { return GBPA_ERR_NOT_FINITE; }
    return GBPA_SUCCESS;
 }
+// ------------------------------------------------ bounded-wait self-test
+// Each of the library's device waits is made to run out: the arrival it
+// waits for never comes. The wait must give up after its limit, report
+// GBPA_FLAG_TIMEOUT / a failed wait, and the kernel must return, leaving the
+// context usable.
+// (0) the persistent kernel's grid barrier, block 0 never arriving
+__global__ void selftest_barrier_kernel(BParams P)
+{
+   if (blockIdx.x == 0) { return; }
+   grid_barrier(P);
+}
+// (1) the TMA staging mbarrier wait, nothing arriving and no copy issued
+__global__ void selftest_mbarrier_kernel(long long max_polls, int *timed_out)
+{
+   __shared__ unsigned long long bar;
+   if (threadIdx.x == 0) { mbar_init(&bar, 1); }
+   __syncthreads();
+   const bool ok = mbar_wait(&bar, 0, max_polls);
+   if (!ok && threadIdx.x == 0) { atomicOr(timed_out, GBPA_FLAG_TIMEOUT); }
+}
 } // namespace gbpa
 
 using namespace gbpa;
+
+extern "C" int gbpa_selftest_bounded_wait(gbpa_ctx_t ctx, int which, long long limit)
+{
+   if (!ctx || (which != 0 && which != 1) || limit < 1 || limit > (1LL << 26))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   unsigned int *sync = nullptr;
+   int rc = check_cuda(cudaMalloc(&sync, 64 * sizeof(unsigned int)), "cudaMalloc");
+   if (rc) { return rc; }
+   rc = check_cuda(cudaMemsetAsync(sync, 0, 64 * sizeof(unsigned int), ctx->stream), "memset");
+   if (!rc && which == 0)
+   {
+      BParams P{};
+      P.bar_count = sync;
+      P.bar_gen = sync + 32;
+      P.abort = (int *)(sync + 2);
+      P.flags = ctx->d_flags;
+      P.spin_limit = limit;
+      void *args[] = {&P};
+      rc = check_cuda(cudaLaunchCooperativeKernel((const void *)selftest_barrier_kernel, dim3(2),
+                                                  dim3(64), args, 0, ctx->stream),
+                      "cudaLaunchCooperativeKernel");
+      ctx->launches++;
+   }
+   else if (!rc)
+   {
+      selftest_mbarrier_kernel<<<1, 32, 0, ctx->stream>>>(limit, ctx->d_flags);
+      rc = last_launch(ctx, "selftest_mbarrier");
+   }
+   if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+   cudaFree(sync);
+   if (rc) { return rc; }
+   int flags = 0;
+   rc = gbpa_get_error_flags(ctx, &flags);
+   if (rc) { return rc; }
+   return (flags & GBPA_FLAG_TIMEOUT) ? GBPA_ERR_TIMEOUT : GBPA_SUCCESS;
+}
 
 extern "C" int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob, const gbpa_problem_desc *probs,
                                          int precision, int schedule, double rel_tol, double abs_tol,

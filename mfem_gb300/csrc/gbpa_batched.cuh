@@ -9,7 +9,6 @@ namespace gbpa
 {
 constexpr int BATCH_THREADS = 256;   // vector-phase blocks (and the persistent kernel)
 constexpr int CHUNK = 2048;          // dofs per vector-phase block / partial sum
-constexpr int GBPA_FLAG_TIMEOUT = 16;
 
 struct BProb
 {

@@ -42,6 +42,62 @@ def test_binding_matches_header():
     assert sorted(_lib.SIGNATURES) == declared_symbols()
 
 
+def _prototypes():
+    """name -> (return type, [parameter types]) parsed from include/*.h."""
+    protos = {}
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"([A-Za-z_][\w \t\*]*?)\b(gbpa_\w+)\s*\(([^)]*)\)\s*;", src):
+            ret = " ".join(m.group(1).split())
+            params = []
+            for a in m.group(3).split(","):
+                a = " ".join(a.split())
+                if not a or a == "void":
+                    continue
+                params.append(a if a.endswith("*") else re.sub(r"\s*\b\w+$", "", a))
+            protos[m.group(2)] = (ret, params)
+    return protos
+
+
+def _c_kind(t):
+    """Type class of a C type: pointers and library handles are 'p'."""
+    t = t.replace("const ", "").strip()
+    if "*" in t or (t.startswith("gbpa_") and t.endswith("_t")):
+        return "p"
+    return {"int": "i4", "int64_t": "i8", "long long": "i8", "unsigned long long": "u8",
+            "double": "f8", "float": "f4", "void": "v"}[t]
+
+
+def _ctypes_kind(t):
+    if t is None:
+        return "v"
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and isinstance(t._type_, type):
+        return "p"
+    if t is ctypes.c_double:
+        return "f8"
+    if t is ctypes.c_float:
+        return "f4"
+    unsigned = t in (ctypes.c_uint, ctypes.c_uint64, ctypes.c_ulonglong, ctypes.c_ulong)
+    return ("u" if unsigned else "i") + str(ctypes.sizeof(t))
+
+
+def test_binding_argument_types_match_header():
+    """Every prototype's return and parameter types agree with the ctypes
+    signature the binding gives the library (count, and pointer / int /
+    64-bit int / double class of each)."""
+    from mfem_gb300 import _lib
+    protos = _prototypes()
+    assert sorted(protos) == declared_symbols()
+    bad = []
+    for name, (ret, params) in protos.items():
+        res, args = _lib.SIGNATURES[name]
+        want = [_c_kind(t) for t in params]
+        have = [_ctypes_kind(t) for t in args]
+        if want != have or _c_kind(ret) != _ctypes_kind(res):
+            bad.append((name, ret, want, _ctypes_kind(res), have))
+    assert not bad, bad
+
+
 def test_version_and_error_strings(lib):
     assert lib.gbpa_version() == 10000
     assert lib.gbpa_error_string(0) == b"success"
