@@ -570,9 +570,17 @@ def run_pcg_form(n, p, max_it=2000):
                      "inner_iterations": info.inner_iterations,
                      "true_rel_residual": info.true_rel_residual,
                      "rel_l2_vs_fp64": float(torch.linalg.norm(Xm - X64) / torch.linalg.norm(X64))}
+    # one FP32 PCG with FP64 residual replacement (reliable updates, delta 0.1)
+    Xr = torch.zeros_like(b)
+    st = dev.lib.gbpa_pcg_solve_mixed_reliable(A64.handle, A32.handle, P(d32), P(b), P(Xr), 1e-10, 0.1,
+                                               max_it, ctypes.byref(info))
+    out["mixed_reliable"] = {"status": st, "seconds": info.seconds, "replacements": info.outer_iterations,
+                             "f32_iterations": info.iterations, "true_rel_residual": info.true_rel_residual,
+                             "rel_l2_vs_fp64": float(torch.linalg.norm(Xr - X64) / torch.linalg.norm(X64))}
     t64 = out["fp64_pcg"]["seconds"]
     out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
     out["speedup_mixed_vs_f64x2_pcg"] = out["f64x2_pcg"]["seconds"] / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
+    out["speedup_mixed_reliable_vs_fp64"] = t64 / max(out["mixed_reliable"]["seconds"], 1e-30)
     return out
 
 

@@ -314,6 +314,19 @@ int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
                          const float *dinv32, const double *b, double *x,
                          double outer_rel_tol, double inner_rel_tol,
                          int max_outer, int max_inner, gbpa_solve_info *info);
+/* Mixed precision with reliable updates (no counterpart in the reference; it
+ * replaces the same CGSolver::Mult call as gbpa_pcg_solve): ONE FP32
+ * Jacobi-PCG on A32 whose iterated residual is replaced by the true FP64
+ * residual b - A64 x whenever its preconditioned norm has dropped by `delta`
+ * (0 < delta < 1, e.g. 0.1) since the last replacement; the search direction
+ * keeps its history, so no Krylov space is discarded. Stops when
+ * ||b - A64 x|| <= rel_tol ||b|| (FP64, 2-norm) or after max_it FP32
+ * iterations. info: iterations = FP32 iterations, outer_iterations =
+ * residual replacements. x starts from zero. */
+int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_t A32,
+                                  const float *dinv32, const double *b, double *x,
+                                  double rel_tol, double delta, int max_it,
+                                  gbpa_solve_info *info);
 
 /* ------------------------------------------- several right-hand sides */
 /* R = nrhs right-hand sides stored interleaved (v[i*R + r]), R in {1, 2, 4,

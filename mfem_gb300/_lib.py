@@ -96,6 +96,7 @@ SIGNATURES = {
     "gbpa_jacobi_setup": (I, [P, I64, P, P, I, D, P]),
     "gbpa_pcg_solve": (I, [P, P, P, P, D, D, I, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_pcg_solve_mixed": (I, [P, P, P, P, P, D, D, I, I, ctypes.POINTER(SolveInfo)]),
+    "gbpa_pcg_solve_mixed_reliable": (I, [P, P, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_operator_mult_block": (I, [P, I, P, P]),
     "gbpa_pcg_solve_block": (I, [P, I, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_pcg_solve_block_mixed": (I, [P, P, I, P, P, P, D, D, I, I, ctypes.POINTER(SolveInfo)]),

@@ -208,6 +208,39 @@ __global__ void set_mask_one_kernel(int ndofs, const unsigned char *mask, double
    }
 }
 
+// Reliable update of the FP32 CG (residual replaced by the true one, r
+// already written): z = dinv r, betanom = (r, z), beta = betanom / nom (the
+// direction keeps its history), and the next segment's stopping level
+// r0 = rel_tol2 * betanom (rel_tol2 holds delta^2).
+__global__ void pcg_restart_kernel(int64_t n, const float *__restrict__ r, float *__restrict__ z,
+                                   const float *__restrict__ dinv, double *partials, PcgState *st)
+{
+   __shared__ double ws[32];
+   double s = 0.0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const float zi = dinv[i] * r[i];
+      z[i] = zi;
+      s += (double)r[i] * (double)zi;
+   }
+   s = block_sum_d(s, ws);
+   double bn;
+   if (finish_partial(s, partials, &st->counter_init, &bn, ws) && threadIdx.x == 0)
+   {
+      st->betanom = bn;
+      st->converged = 0;
+      st->done = 0;
+      if (!isfinite(bn)) { st->status = GBPA_ERR_NOT_FINITE; st->done = 1; st->final_iter = st->iter; }
+      else if (bn <= 0.0) { st->done = 1; st->final_iter = st->iter; }
+      else
+      {
+         st->beta = bn / st->nom;
+         st->r0 = st->rel_tol2 * bn;
+      }
+   }
+}
+
 // mixed-precision helpers
 __global__ void scale_to_f32_kernel(int64_t n, const double *r, const double *nrm2, float *r32)
 {
@@ -367,7 +400,8 @@ extern "C" int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y)
 
 // Device address of a host buffer the kernels can access directly: memory
 // pinned by cudaHostAlloc / cudaHostRegister (device-mapped under unified
-// addressing). Pageable memory returns nullptr.
+// addressing). Pageable memory returns nullptr, and so does any other kind
+// (managed, device), which the caller then stages with cudaMemcpyDefault.
 static void *mapped_host_ptr(const void *p)
 {
    cudaPointerAttributes a{};
@@ -396,13 +430,13 @@ extern "C" int gbpa_operator_mult_host(gbpa_operator_t op, const void *x, void *
    if (stage_x)
    {
       dx = op->stage;
-      rc = check_cuda(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy x");
+      rc = check_cuda(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyDefault, ctx->stream), "copy x");
    }
    if (stage_y) { dy = (unsigned char *)op->stage + bytes; }
    if (!rc) { rc = gbpa_operator_mult(op, dx, dy); }
    if (!rc && stage_y)
    {
-      rc = check_cuda(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, ctx->stream), "copy y");
+      rc = check_cuda(cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDefault, ctx->stream), "copy y");
    }
    const int rs = check_cuda(cudaStreamSynchronize(ctx->stream), "sync");
    return rc ? rc : rs;
@@ -496,47 +530,15 @@ static int pcg_iteration(gbpa_operator *op, T *x, const T *dinv, unsigned grid)
    return last_launch(ctx, "pcg_scatter_den");
 }
 
+// Runs captured K-iteration graphs of pcg_iteration (x, dinv fixed) until
+// the device state reports done, polling the flag between graph launches.
 template <typename T>
-static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double rel_tol,
-                   double abs_tol, int max_it, int iterative, gbpa_solve_info *info,
-                   float *elapsed_ms)
+static int pcg_graph_loop(gbpa_operator *op, T *x, const T *dinv, int max_it)
 {
    gbpa_ctx *ctx = op->ctx;
    const int64_t n = op->d.ndofs;
-   int rc = ensure_pcg_workspace(op);
-   if (rc) { return rc; }
-   T *r = (T *)op->r, *d = (T *)op->dv, *z = (T *)op->z;
-   // 4 blocks of 512 threads per SM: full occupancy for the streaming vector
-   // phases (partials buffer holds 2048 entries per reduction)
    const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
-   PcgState h{};
-   h.rel_tol2 = rel_tol * rel_tol;
-   h.abs_tol2 = abs_tol * abs_tol;
-   h.max_it = max_it;
-   rc = check_cuda(cudaMemcpyAsync(op->state, &h, sizeof(PcgState), cudaMemcpyHostToDevice,
-                                   ctx->stream), "cudaMemcpyAsync(state)");
-   if (rc) { return rc; }
-   if (iterative)
-   {
-      rc = op_mult<T>(op, x, r);   // r = A x, then r = b - r in the init kernel
-      if (rc) { return rc; }
-   }
-   pcg_init_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, b, x, r, z, d, dinv, iterative,
-                                                         op->partials, op->state);
-   rc = last_launch(ctx, "pcg_init");
-   if (rc) { return rc; }
-   // z = A d, den = (d, z), alpha = nom / den
-   rc = apply_evec<T>(op, d, &op->state->done);
-   if (rc) { return rc; }
-   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
-      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
-      op->partials + 2048, op->state, 1);
-   rc = last_launch(ctx, "pcg_scatter_den");
-   if (rc) { return rc; }
-
+   int rc = GBPA_SUCCESS;
    const int K = pcg_check_every();
    if (!op->graph || op->graph_x != (const void *)x || op->graph_dinv != (const void *)dinv)
    {
@@ -587,6 +589,52 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
       if (rc) { return rc; }
       ctx->launches += (int64_t)K * per_iter;
    }
+   return GBPA_SUCCESS;
+}
+
+template <typename T>
+static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double rel_tol,
+                   double abs_tol, int max_it, int iterative, gbpa_solve_info *info,
+                   float *elapsed_ms)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = op->d.ndofs;
+   int rc = ensure_pcg_workspace(op);
+   if (rc) { return rc; }
+   T *r = (T *)op->r, *d = (T *)op->dv, *z = (T *)op->z;
+   // 4 blocks of 512 threads per SM: full occupancy for the streaming vector
+   // phases (partials buffer holds 2048 entries per reduction)
+   const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   PcgState h{};
+   h.rel_tol2 = rel_tol * rel_tol;
+   h.abs_tol2 = abs_tol * abs_tol;
+   h.max_it = max_it;
+   rc = check_cuda(cudaMemcpyAsync(op->state, &h, sizeof(PcgState), cudaMemcpyHostToDevice,
+                                   ctx->stream), "cudaMemcpyAsync(state)");
+   if (rc) { return rc; }
+   if (iterative)
+   {
+      rc = op_mult<T>(op, x, r);   // r = A x, then r = b - r in the init kernel
+      if (rc) { return rc; }
+   }
+   pcg_init_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, b, x, r, z, d, dinv, iterative,
+                                                         op->partials, op->state);
+   rc = last_launch(ctx, "pcg_init");
+   if (rc) { return rc; }
+   // z = A d, den = (d, z), alpha = nom / den
+   rc = apply_evec<T>(op, d, &op->state->done);
+   if (rc) { return rc; }
+   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
+      op->partials + 2048, op->state, 1);
+   rc = last_launch(ctx, "pcg_scatter_den");
+   if (rc) { return rc; }
+
+   rc = pcg_graph_loop<T>(op, x, dinv, max_it);
+   if (rc) { return rc; }
    cudaEventRecord(e1, ctx->stream);
    cudaEventSynchronize(e1);
    float ms = 0.f;
@@ -749,6 +797,156 @@ extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, co
    inf->iterations = inner_total;
    inf->converged = converged;
    inf->true_rel_residual = rel;
+   inf->final_norm = sqrt(hb[0]);
+   return converged ? GBPA_SUCCESS : GBPA_ERR_NOT_CONVERGED;
+}
+
+// Mixed precision with reliable updates: ONE FP32 Jacobi-PCG on A32 whose
+// iterated residual is replaced by the true FP64 residual b - A64 x each time
+// it has dropped by delta since the last replacement, the search direction
+// keeping its history (residual replacement: Sleijpen and van der Vorst 1996;
+// van der Vorst and Ye 2000). Unlike restarted defect correction the Krylov
+// space is never discarded, so the FP32 iteration count stays close to the
+// FP64 one. The FP32 vectors carry the problem scaled by 1/||b||; x and the
+// true residual stay FP64; stop when ||b - A64 x|| <= rel_tol ||b||.
+extern "C" int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_t A32,
+                                             const float *dinv32, const double *b, double *x,
+                                             double rel_tol, double delta, int max_it,
+                                             gbpa_solve_info *info)
+{
+   if (!A64 || !A32 || A64->d.precision == GBPA_F32 || A32->d.precision != GBPA_F32 ||
+       A64->d.ndofs != A32->d.ndofs || A64->ctx != A32->ctx || max_it < 1 || rel_tol < 0 ||
+       !(delta > 0.0 && delta < 1.0))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const int64_t n = A64->d.ndofs;
+   if (n > 0 && (!dinv32 || !b || !x)) { return GBPA_ERR_INVALID_ARGUMENT; }
+   gbpa_solve_info tmp{};
+   gbpa_solve_info *inf = info ? info : &tmp;
+   memset(inf, 0, sizeof(*inf));
+   if (n == 0) { inf->converged = 1; return GBPA_SUCCESS; }
+   gbpa_ctx *ctx = A64->ctx;
+   gbpa_operator *op = A32;
+   int rc = ensure_pcg_workspace(op);
+   if (rc) { return rc; }
+   if (!A64->r64)
+   {
+      rc = check_cuda(cudaMalloc(&A64->r64, sizeof(double) * n), "cudaMalloc(r64)");
+      if (!rc) { rc = check_cuda(cudaMalloc(&A64->t64, sizeof(double) * 8), "cudaMalloc(t64)"); }
+      if (rc) { return rc; }
+   }
+   // FP32 correction since the last update (x32) and the scaled right-hand side (b32)
+   float *x32 = (float *)scratch(ctx, SLOT_PCG32, sizeof(float) * 2 * n);
+   if (!x32) { return GBPA_ERR_OUT_OF_MEMORY; }
+   float *b32 = x32 + n;
+   float *r = (float *)op->r, *d = (float *)op->dv, *z = (float *)op->z;
+   const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
+   const unsigned vg = grid_for(n, 256, 8 * ctx->num_sms);
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   double hb[2] = {0.0, 0.0};
+   double rel = 1.0;
+   int updates = 0, converged = 0;
+   PcgState h{};
+   // x = 0; t64[1] = (b, b); b32 = b / ||b||
+   rc = check_cuda(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream), "memset(x)");
+   if (!rc) { rc = launch_dot<double>(ctx, n, b, b, A64->t64 + 1); }
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(hb + 1, A64->t64 + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"); }
+   if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+   if (rc) { return rc; }
+   if (!std::isfinite(hb[1])) { return GBPA_ERR_NOT_FINITE; }
+   if (hb[1] == 0.0)
+   {
+      inf->converged = 1;
+      return GBPA_SUCCESS;
+   }
+   scale_to_f32_kernel<<<vg, 256, 0, ctx->stream>>>(n, b, A64->t64 + 1, b32);
+   rc = last_launch(ctx, "scale_to_f32");
+   if (rc) { return rc; }
+   // FP32 CG start: x32 = 0, r = b32, z = dinv r, d = z, segment ends at delta^2 (r, z)
+   h.rel_tol2 = delta * delta;
+   h.max_it = max_it;
+   rc = check_cuda(cudaMemcpyAsync(op->state, &h, sizeof(PcgState), cudaMemcpyHostToDevice,
+                                   ctx->stream), "cudaMemcpyAsync(state)");
+   if (rc) { return rc; }
+   pcg_init_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, b32, x32, r, z, d, dinv32, 0,
+                                                              op->partials, op->state);
+   rc = last_launch(ctx, "pcg_init");
+   if (!rc) { rc = apply_evec<float>(op, d, &op->state->done); }
+   if (!rc)
+   {
+      pcg_scatter_den_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+         n, op->d.offsets, op->d.indices, (const float *)op->yE, z, d, op->mask, op->partials + 2048,
+         op->state, 1);
+      rc = last_launch(ctx, "pcg_scatter_den");
+   }
+   if (rc) { return rc; }
+   for (;;)
+   {
+      // FP32 iterations of this segment
+      rc = pcg_graph_loop<float>(op, x32, dinv32, max_it);
+      if (rc) { return rc; }
+      rc = check_cuda(cudaMemcpyAsync(&h, op->state, sizeof(PcgState), cudaMemcpyDeviceToHost,
+                                      ctx->stream), "copy(state)");
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+      if (rc) { return rc; }
+      if (h.status) { return h.status; }
+      // reliable update: x += ||b|| x32, x32 = 0, r64 = b - A64 x (FP64)
+      correct_kernel<<<vg, 256, 0, ctx->stream>>>(n, x, x32, A64->t64 + 1);
+      rc = last_launch(ctx, "correct");
+      if (!rc) { rc = check_cuda(cudaMemsetAsync(x32, 0, sizeof(float) * n, ctx->stream), "memset"); }
+      if (!rc) { rc = op_mult<double>(A64, x, A64->r64); }
+      if (!rc)
+      {
+         residual_kernel<<<vg, 256, 0, ctx->stream>>>(n, b, A64->r64);
+         rc = last_launch(ctx, "residual");
+      }
+      if (!rc) { rc = launch_dot<double>(ctx, n, A64->r64, A64->r64, A64->t64); }
+      if (!rc) { rc = check_cuda(cudaMemcpyAsync(hb, A64->t64, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "copy"); }
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+      if (rc) { return rc; }
+      ++updates;
+      rel = sqrt(hb[0] / hb[1]);
+      if (!std::isfinite(rel)) { return GBPA_ERR_NOT_FINITE; }
+      if (rel <= rel_tol) { converged = 1; break; }
+      if (h.iter > max_it || (h.done && !h.converged)) { break; }   // iteration cap or breakdown
+      // r = r64 / ||b|| in FP32; z = dinv r; beta; the direction continues
+      scale_to_f32_kernel<<<vg, 256, 0, ctx->stream>>>(n, A64->r64, A64->t64 + 1, r);
+      rc = last_launch(ctx, "scale_to_f32");
+      if (!rc)
+      {
+         pcg_restart_kernel<<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, r, z, dinv32, op->partials, op->state);
+         rc = last_launch(ctx, "pcg_restart");
+      }
+      if (!rc)
+      {
+         pcg_direction_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, z, d, op->state);
+         rc = last_launch(ctx, "pcg_direction");
+      }
+      if (!rc) { rc = apply_evec<float>(op, d, &op->state->done); }
+      if (!rc)
+      {
+         pcg_scatter_den_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+            n, op->d.offsets, op->d.indices, (const float *)op->yE, z, d, op->mask,
+            op->partials + 2048, op->state, 0);
+         rc = last_launch(ctx, "pcg_scatter_den");
+      }
+      if (rc) { return rc; }
+   }
+   cudaEventRecord(e1, ctx->stream);
+   cudaEventSynchronize(e1);
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, e0, e1);
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   inf->seconds = ms * 1e-3;
+   inf->outer_iterations = updates;
+   inf->inner_iterations = h.iter;
+   inf->iterations = h.iter;
+   inf->converged = converged;
+   inf->true_rel_residual = rel;
+   inf->initial_norm = sqrt(hb[1]);
    inf->final_norm = sqrt(hb[0]);
    return converged ? GBPA_SUCCESS : GBPA_ERR_NOT_CONVERGED;
 }

@@ -94,6 +94,88 @@ def test_mixed_precision_matches_reference_solve():
     assert info.outer_iterations >= 2
 
 
+@pytest.mark.parametrize("delta", [0.1, 0.01])
+def test_mixed_reliable_matches_reference_solve(delta):
+    """One FP32 PCG with FP64 residual replacement: the reference's solution
+    within 1e-9, true residual within the tolerance, FP32 iterations close to
+    the reference's FP64 count (no Krylov restarts)."""
+    import ctypes
+    from mfem_gb300 import _lib
+    from tests.gpu_util import T, H, p, zeros, relerr, dev
+    g, ndofs, A, A32 = cfg1_operator()
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    st = dev().lib.gbpa_pcg_solve_mixed_reliable(A.handle, A32.handle, p(dinv.float()), p(T(g["B_rhs"])),
+                                                 p(X), 1e-10, delta, 1000, ctypes.byref(info))
+    assert st == 0, info.as_dict()
+    assert info.converged == 1 and info.true_rel_residual <= 1e-10
+    assert relerr(H(X), g["X"]) < 1e-9
+    assert info.outer_iterations >= 2
+    assert info.iterations <= 1.3 * int(g["cg_info"][0]) + 10
+
+
+def test_mixed_reliable_on_jittered_lognormal_problem():
+    """A harder case (jittered p=4 mesh, lognormal kappa): the reliable mixed
+    solution matches FP64 PCG to 1e-8 and needs no more FP32 iterations than
+    the restarted defect correction."""
+    import ctypes
+    from mfem_gb300 import _lib, fem
+    from mfem_gb300.pa import DiffusionIntegrator, FiniteElementSpace, OperatorJacobiSmoother, PAOperator
+    from tests.gpu_util import dev
+    d = dev()
+    mesh = fem.CartesianMesh(10, jitter=0.1, seed=1)
+    fes = FiniteElementSpace(mesh, 4)
+    integ = DiffusionIntegrator("kappa")
+    integ.AssemblePA(fes, modes=fem.kappa_modes(3))
+    e = fes.GetBoundaryTrueDofs()
+    A = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=e)
+    A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=e, precision=1)
+    M = OperatorJacobiSmoother(A, e)
+    n = fes.ndofs
+    gen = torch.Generator(device="cuda").manual_seed(41)
+    b = torch.rand(n, dtype=torch.float64, device="cuda", generator=gen)
+    b[torch.from_numpy(e).long().cuda()] = 0.0
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    x64 = torch.zeros_like(b)
+    i64 = _lib.SolveInfo()
+    assert d.lib.gbpa_pcg_solve(A.handle, P(M.dinv), P(b), P(x64), 1e-12, 0.0, 20000, 0, ctypes.byref(i64)) == 0
+    dinv32 = M.dinv.float()
+    xr = torch.zeros_like(b)
+    ir = _lib.SolveInfo()
+    assert d.lib.gbpa_pcg_solve_mixed_reliable(A.handle, A32.handle, P(dinv32), P(b), P(xr), 1e-10, 0.1,
+                                               20000, ctypes.byref(ir)) == 0
+    xm = torch.zeros_like(b)
+    im = _lib.SolveInfo()
+    assert d.lib.gbpa_pcg_solve_mixed(A.handle, A32.handle, P(dinv32), P(b), P(xm), 1e-10, 1e-5, 30, 20000,
+                                      ctypes.byref(im)) == 0
+    assert ir.converged == 1 and ir.true_rel_residual <= 1e-10
+    assert float(torch.linalg.norm(xr - x64) / torch.linalg.norm(x64)) < 1e-8
+    assert ir.iterations <= im.inner_iterations
+
+
+def test_mixed_reliable_rejects_bad_arguments():
+    import ctypes
+    from mfem_gb300 import _lib
+    from tests.gpu_util import T, p, zeros, dev
+    g, ndofs, A, A32 = cfg1_operator()
+    _, dinv = jacobi(g, A, ndofs)
+    X = zeros(ndofs)
+    info = _lib.SolveInfo()
+    lib = dev().lib
+    b = T(g["B_rhs"])
+    for delta in (0.0, 1.0, -0.5):
+        assert lib.gbpa_pcg_solve_mixed_reliable(A.handle, A32.handle, p(dinv.float()), p(b), p(X), 1e-10,
+                                                 delta, 100, ctypes.byref(info)) == -1
+    # operators swapped (the FP32 one must be second)
+    assert lib.gbpa_pcg_solve_mixed_reliable(A32.handle, A.handle, p(dinv.float()), p(b), p(X), 1e-10,
+                                             0.1, 100, ctypes.byref(info)) == -1
+    # iteration cap: not converged, reported as such
+    st = lib.gbpa_pcg_solve_mixed_reliable(A.handle, A32.handle, p(dinv.float()), p(b), p(X), 1e-10,
+                                           0.1, 5, ctypes.byref(info))
+    assert st == -6 and info.converged == 0
+
+
 def test_max_iterations_not_converged():
     import ctypes
     from mfem_gb300 import _lib
