@@ -850,6 +850,22 @@ def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
         seq += si.seconds
     out["seconds_sequential_mixed"] = seq
     out["speedup_block_vs_sequential"] = seq / max(info[0].seconds, 1e-30)
+    # reliable updates (one FP32 PCG, FP64 residual replacement, delta 0.1): block and one at a time
+    XR = torch.zeros_like(B)
+    ir = (_lib.SolveInfo * nrhs)()
+    st3 = dev.lib.gbpa_pcg_solve_block_mixed_reliable(A64.handle, A32.handle, nrhs, P(M.dinv.float()), P(B),
+                                                      P(XR), 1e-10, 0.1, 20000, ir)
+    seqr = 0.0
+    for r in range(nrhs):
+        xr = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        b = B[:, r].contiguous()
+        dev.lib.gbpa_pcg_solve_mixed_reliable(A64.handle, A32.handle, P(M.dinv.float()), P(b), P(xr), 1e-10,
+                                              0.1, 20000, ctypes.byref(si))
+        seqr += si.seconds
+    out["reliable"] = {"status": st3, "seconds_block": ir[0].seconds, "seconds_sequential": seqr,
+                       "f32_iterations": [ir[r].iterations for r in range(nrhs)],
+                       "replacements": [ir[r].outer_iterations for r in range(nrhs)],
+                       "true_rel_residual": [ir[r].true_rel_residual for r in range(nrhs)]}
     if with_reference:
         X64 = torch.zeros_like(B)
         i64 = (_lib.SolveInfo * nrhs)()
@@ -858,6 +874,8 @@ def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
                                  "iterations": [i64[r].iterations for r in range(nrhs)]}
         out["rel_l2_vs_fp64"] = [float(torch.linalg.norm(X[:, r] - X64[:, r]) / torch.linalg.norm(X64[:, r]))
                                  for r in range(nrhs)]
+        out["reliable"]["rel_l2_vs_fp64"] = [float(torch.linalg.norm(XR[:, r] - X64[:, r]) /
+                                                   torch.linalg.norm(X64[:, r])) for r in range(nrhs)]
     return out
 
 

@@ -348,6 +348,16 @@ int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A32,
                                double *x, double outer_rel_tol,
                                double inner_rel_tol, int max_outer,
                                int max_inner, gbpa_solve_info *info);
+/* Block form of gbpa_pcg_solve_mixed_reliable: one FP32 block PCG whose
+ * residuals are replaced by the true FP64 block residual once every
+ * right-hand side still running has dropped by `delta` since its last
+ * replacement. info[r]: iterations = FP32 iterations, outer_iterations =
+ * replacements; each right-hand side stops on its own true FP64 residual. */
+int gbpa_pcg_solve_block_mixed_reliable(gbpa_operator_t A64, gbpa_operator_t A32,
+                                        int nrhs, const float *dinv32,
+                                        const double *b, double *x, double rel_tol,
+                                        double delta, int max_it,
+                                        gbpa_solve_info *info);
 
 /* ---------------------------------------------------------- batched PCG */
 /* Batching form: many independent Dirichlet problems of uneven size and

@@ -100,6 +100,7 @@ SIGNATURES = {
     "gbpa_operator_mult_block": (I, [P, I, P, P]),
     "gbpa_pcg_solve_block": (I, [P, I, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_pcg_solve_block_mixed": (I, [P, P, I, P, P, P, D, D, I, I, ctypes.POINTER(SolveInfo)]),
+    "gbpa_pcg_solve_block_mixed_reliable": (I, [P, P, I, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_batched_pcg_solve":(I, [P, I, ctypes.POINTER(ProblemDesc), D, D, I, P, P, P,
                                    ctypes.POINTER(D)]),
     "gbpa_batched_pcg_solve_precision": (I, [P, I, ctypes.POINTER(ProblemDesc), I, D, D, I, P, P, P,

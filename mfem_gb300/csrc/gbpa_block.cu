@@ -288,6 +288,46 @@ __global__ void blk_dot_kernel(int64_t n, int R, const T *__restrict__ a, const 
    if (finish_rhs(s, R, partials, counter, tot) && threadIdx.x < R) { out[threadIdx.x] = tot[threadIdx.x]; }
 }
 
+// Reliable update of the FP32 block PCG (residuals already replaced by the
+// true ones, zero where converged): z = dinv r, betanom_r = (r_r, z_r),
+// beta_r = betanom_r / nom_r, next segment level r0_r = rel2 * betanom_r
+// (rel2 holds delta^2); converged right-hand sides stay done.
+__global__ void blk_restart_kernel(int64_t n, int R, const float *__restrict__ r,
+                                   float *__restrict__ z, const float *__restrict__ dinv,
+                                   const int *__restrict__ conv, double *partials, BlockState *st)
+{
+   __shared__ double tot[BK_MAXR];
+   double s = 0.0;
+   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+        k += (int64_t)gridDim.x * blockDim.x)
+   {
+      const float zk = dinv[k >> (__ffs(R) - 1)] * r[k];
+      z[k] = zk;
+      s += (double)r[k] * (double)zk;
+   }
+   if (finish_rhs(s, R, partials, &st->counter[3], tot) && threadIdx.x == 0)
+   {
+      int active = 0;
+      for (int q = 0; q < R; ++q)
+      {
+         if (conv[q]) { st->done[q] = 1; continue; }
+         const double bn = tot[q];
+         st->betanom[q] = bn;
+         st->converged[q] = 0;
+         st->done[q] = 0;
+         if (!isfinite(bn)) { st->status = GBPA_ERR_NOT_FINITE; st->done[q] = 1; st->final_iter[q] = st->iter[q]; }
+         else if (bn <= 0.0) { st->done[q] = 1; st->final_iter[q] = st->iter[q]; }
+         else
+         {
+            st->beta[q] = bn / st->nom[q];
+            st->r0[q] = st->rel2 * bn;
+         }
+         active += !st->done[q];
+      }
+      st->all_done = active == 0;
+   }
+}
+
 // mixed-precision helpers: r32 = r / ||r|| (zero where converged), x += ||r|| c
 __global__ void blk_scale_kernel(int64_t n, int R, const double *r, const double *nrm2,
                                  const int *conv, float *r32)
@@ -397,6 +437,44 @@ struct BlockWork
    void free_all() { cudaFree(r); cudaFree(d); cudaFree(z); cudaFree(partials); cudaFree(st); }
 };
 
+// Block PCG iterations (update, direction, A d, den) in batches of K between
+// host polls of the all-done flag, until every right-hand side is done.
+template <typename T>
+static int block_iterate(gbpa_operator *op, int R, T *x, T *r, T *z, T *d, const T *dinv,
+                         BlockWork &w, int max_it)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = (int64_t)op->d.ndofs * R;
+   const unsigned grid = grid_for(n, BK_BLOCK, 4 * ctx->num_sms);
+   const int K = 10;
+   int *h_done = (int *)ctx->h_pinned;
+   int rc = GBPA_SUCCESS;
+   for (int launched = 0; !rc; launched += K)
+   {
+      rc = check_cuda(cudaMemcpyAsync(h_done, &w.st->all_done, sizeof(int), cudaMemcpyDeviceToHost,
+                                      ctx->stream), "copy");
+      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
+      if (rc || *h_done || launched > max_it + K) { break; }
+      for (int k = 0; k < K && !rc; ++k)
+      {
+         blk_update_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, x, r, z, d, dinv, w.partials,
+                                                                 w.st);
+         rc = last_launch(ctx, "blk_update");
+         if (!rc)
+         {
+            blk_direction_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, z, d, w.st);
+            rc = last_launch(ctx, "blk_direction");
+         }
+         if (!rc) { rc = block_apply_evec<T>(op, R, d, &w.st->all_done); }
+         if (!rc)
+         {
+            rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 0);
+         }
+      }
+   }
+   return rc;
+}
+
 template <typename T>
 static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T *x,
                          double rel_tol, double abs_tol, int max_it, BlockState *h_out,
@@ -431,31 +509,7 @@ static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T 
    {
       rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 1);
    }
-   const int K = 10;
-   int *h_done = (int *)ctx->h_pinned;
-   for (int launched = 0; !rc; launched += K)
-   {
-      rc = check_cuda(cudaMemcpyAsync(h_done, &w.st->all_done, sizeof(int), cudaMemcpyDeviceToHost,
-                                      ctx->stream), "copy");
-      if (!rc) { rc = check_cuda(cudaStreamSynchronize(ctx->stream), "sync"); }
-      if (rc || *h_done || launched > max_it + K) { break; }
-      for (int k = 0; k < K && !rc; ++k)
-      {
-         blk_update_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, x, r, z, d, dinv, w.partials,
-                                                                 w.st);
-         rc = last_launch(ctx, "blk_update");
-         if (!rc)
-         {
-            blk_direction_kernel<T><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, z, d, w.st);
-            rc = last_launch(ctx, "blk_direction");
-         }
-         if (!rc) { rc = block_apply_evec<T>(op, R, d, &w.st->all_done); }
-         if (!rc)
-         {
-            rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 0);
-         }
-      }
-   }
+   if (!rc) { rc = block_iterate<T>(op, R, x, r, z, d, dinv, w, max_it); }
    cudaEventRecord(e1, ctx->stream);
    cudaEventSynchronize(e1);
    float ms = 0.f;
@@ -620,6 +674,166 @@ extern "C" int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A
       f.final_norm = sqrt(rn2[q]);
       f.seconds = ms * 1e-3;
       all &= conv[q];
+   }
+   if (rc) { return rc; }
+   return all ? GBPA_SUCCESS : GBPA_ERR_NOT_CONVERGED;
+}
+
+// Block form of the reliable-update mixed solver: one FP32 block PCG on A32
+// (each right-hand side scaled by 1/||b_r||) whose iterated residuals are
+// replaced by the true FP64 block residual b - A64 x once every right-hand
+// side still running has dropped its preconditioned residual by delta since
+// its last replacement; search directions keep their history. Right-hand
+// sides stop on their own true FP64 residual.
+extern "C" int gbpa_pcg_solve_block_mixed_reliable(gbpa_operator_t A64, gbpa_operator_t A32, int nrhs,
+                                                   const float *dinv32, const double *b, double *x,
+                                                   double rel_tol, double delta, int max_it,
+                                                   gbpa_solve_info *info)
+{
+   if (!A64 || !A32 || !rhs_ok(nrhs) || !info || A64->d.precision == GBPA_F32 ||
+       A32->d.precision != GBPA_F32 || A64->d.ndofs != A32->d.ndofs || A64->ctx != A32->ctx ||
+       max_it < 1 || rel_tol < 0 || !(delta > 0.0 && delta < 1.0) || A64->d.kind != GBPA_DIFFUSION ||
+       A32->d.kind != GBPA_DIFFUSION)
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const int R = nrhs;
+   const int64_t n = (int64_t)A64->d.ndofs * R;
+   if (n == 0) { return GBPA_SUCCESS; }
+   if (!dinv32 || !b || !x) { return GBPA_ERR_INVALID_ARGUMENT; }
+   gbpa_ctx *ctx = A64->ctx;
+   gbpa_operator *op = A32;
+   int rc = ensure_block_scratch(op, R);
+   if (rc) { return rc; }
+   double *r64 = nullptr, *red = nullptr;
+   float *b32 = nullptr, *x32 = nullptr;
+   int *conv_d = nullptr;
+   BlockWork w;
+   rc = check_cuda(cudaMalloc(&r64, sizeof(double) * n), "cudaMalloc");
+   if (!rc) { rc = check_cuda(cudaMalloc(&b32, sizeof(float) * n), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&x32, sizeof(float) * n), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&red, sizeof(double) * (4096 * BK_MAXR + 64)), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&conv_d, sizeof(int) * BK_MAXR), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&w.r, sizeof(float) * n), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&w.d, sizeof(float) * n), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&w.z, sizeof(float) * n), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&w.partials, sizeof(double) * 4096 * BK_MAXR), "cudaMalloc"); }
+   if (!rc) { rc = check_cuda(cudaMalloc(&w.st, sizeof(BlockState)), "cudaMalloc"); }
+   auto cleanup = [&]() {
+      cudaFree(r64); cudaFree(b32); cudaFree(x32); cudaFree(red); cudaFree(conv_d); w.free_all();
+   };
+   if (rc) { cleanup(); return rc; }
+   float *r = (float *)w.r, *d = (float *)w.d, *z = (float *)w.z;
+   unsigned int *counter = (unsigned int *)(red + 4096 * BK_MAXR);
+   double *d_out = red + 4096 * BK_MAXR + 16;
+   double *d_nb2 = red + 4096 * BK_MAXR + 32;
+   const unsigned grid = grid_for(n, BK_BLOCK, 4 * ctx->num_sms);
+   cudaEvent_t e0, e1;
+   cudaEventCreate(&e0); cudaEventCreate(&e1);
+   cudaEventRecord(e0, ctx->stream);
+   double nb2[BK_MAXR] = {0}, rn2[BK_MAXR] = {0};
+   int conv[BK_MAXR] = {0}, repl[BK_MAXR] = {0};
+   BlockState hs{};
+   rc = check_cuda(cudaMemsetAsync(counter, 0, sizeof(unsigned int) * 4, ctx->stream), "memset");
+   if (!rc) { rc = check_cuda(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream), "memset"); }
+   if (!rc) { rc = block_dots<double>(ctx, n, R, b, b, red, counter, d_out, nb2); }
+   for (int q = 0; !rc && q < R; ++q)
+   {
+      if (!std::isfinite(nb2[q])) { rc = GBPA_ERR_NOT_FINITE; }
+      conv[q] = nb2[q] == 0.0;   // b_r = 0: x_r = 0 is the solution
+      if (conv[q]) { nb2[q] = 1.0; }
+   }
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(d_nb2, nb2, sizeof(double) * R, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
+   if (!rc) { rc = check_cuda(cudaMemcpyAsync(conv_d, conv, sizeof(int) * R, cudaMemcpyHostToDevice, ctx->stream), "copy"); }
+   if (!rc)
+   {
+      // b32 = b_r / ||b_r|| (zero for a zero right-hand side)
+      blk_scale_kernel<<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, b, d_nb2, conv_d, b32);
+      rc = last_launch(ctx, "blk_scale");
+   }
+   if (!rc)
+   {
+      BlockState h{};
+      h.nrhs = R; h.max_it = max_it; h.rel2 = delta * delta; h.abs2 = 0.0;
+      rc = check_cuda(cudaMemcpyAsync(w.st, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream), "copy");
+   }
+   if (!rc)
+   {
+      blk_init_kernel<float><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, b32, x32, r, z, d, dinv32, w.partials, w.st);
+      rc = last_launch(ctx, "blk_init");
+   }
+   if (!rc) { rc = block_apply_evec<float>(op, R, d, &w.st->all_done); }
+   if (!rc) { rc = launch_scatter_den<float>(op, R, z, d, w.partials + 4096 * 4, w.st, 1); }
+   int all = 0;
+   while (!rc)
+   {
+      rc = block_iterate<float>(op, R, x32, r, z, d, dinv32, w, max_it);
+      if (!rc) { rc = check_cuda(cudaMemcpy(&hs, w.st, sizeof(BlockState), cudaMemcpyDeviceToHost), "copy"); }
+      if (!rc && hs.status) { rc = hs.status; }
+      if (rc) { break; }
+      // replacement: x += ||b_r|| x32, x32 = 0, r64 = b - A64 x (FP64)
+      blk_correct_kernel<<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, x, x32, d_nb2, conv_d);
+      rc = last_launch(ctx, "blk_correct");
+      if (!rc) { rc = check_cuda(cudaMemsetAsync(x32, 0, sizeof(float) * n, ctx->stream), "memset"); }
+      if (!rc) { rc = block_mult<double>(A64, R, x, r64); }
+      if (!rc)
+      {
+         blk_residual_kernel<<<grid, BK_BLOCK, 0, ctx->stream>>>(n, b, r64);
+         rc = last_launch(ctx, "blk_residual");
+      }
+      if (!rc) { rc = block_dots<double>(ctx, n, R, r64, r64, red, counter, d_out, rn2); }
+      if (rc) { break; }
+      all = 1;
+      int capped = 0;
+      for (int q = 0; q < R; ++q)
+      {
+         if (!std::isfinite(rn2[q])) { rc = GBPA_ERR_NOT_FINITE; break; }
+         if (!conv[q])
+         {
+            ++repl[q];
+            if (sqrt(rn2[q] / nb2[q]) <= rel_tol) { conv[q] = 1; }
+            else if (hs.iter[q] > max_it || (hs.done[q] && !hs.converged[q])) { capped = 1; }
+         }
+         all &= conv[q];
+      }
+      if (rc || all || capped) { break; }
+      // r = r64_r / ||b_r|| (zero where converged); z, betanom, beta; directions continue
+      rc = check_cuda(cudaMemcpyAsync(conv_d, conv, sizeof(int) * R, cudaMemcpyHostToDevice, ctx->stream), "copy");
+      if (!rc)
+      {
+         blk_scale_kernel<<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, r64, d_nb2, conv_d, r);
+         rc = last_launch(ctx, "blk_scale");
+      }
+      if (!rc)
+      {
+         blk_restart_kernel<<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, r, z, dinv32, conv_d, w.partials, w.st);
+         rc = last_launch(ctx, "blk_restart");
+      }
+      if (!rc)
+      {
+         blk_direction_kernel<float><<<grid, BK_BLOCK, 0, ctx->stream>>>(n, R, z, d, w.st);
+         rc = last_launch(ctx, "blk_direction");
+      }
+      if (!rc) { rc = block_apply_evec<float>(op, R, d, &w.st->all_done); }
+      if (!rc) { rc = launch_scatter_den<float>(op, R, z, d, w.partials + 4096 * 4, w.st, 0); }
+   }
+   cudaEventRecord(e1, ctx->stream);
+   cudaEventSynchronize(e1);
+   float ms = 0.f;
+   cudaEventElapsedTime(&ms, e0, e1);
+   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   cleanup();
+   for (int q = 0; q < R; ++q)
+   {
+      gbpa_solve_info &f = info[q];
+      memset(&f, 0, sizeof(f));
+      f.converged = conv[q];
+      f.outer_iterations = repl[q];
+      f.inner_iterations = hs.iter[q];
+      f.iterations = hs.iter[q];
+      f.true_rel_residual = sqrt(rn2[q] / nb2[q]);
+      f.final_norm = sqrt(rn2[q]);
+      f.seconds = ms * 1e-3;
    }
    if (rc) { return rc; }
    return all ? GBPA_SUCCESS : GBPA_ERR_NOT_CONVERGED;
