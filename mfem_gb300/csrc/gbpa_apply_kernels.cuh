@@ -566,8 +566,8 @@ __global__ void diffusion_apply_kernel(int ne, int symm, int d1d, int q1d,
 // block's qdata is staged once in shared memory (TMA bulk copy, when the
 // 16-byte rules hold) and reused for all R vectors, so HBM delivers it once
 // per R applies; otherwise the R passes re-read it through L1/L2.
-template <typename AR, int TD, int TQ>
-__global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d, int q1d,
+template <typename AR, int TD, int TQ, int TR = 0>
+__global__ void diffusion_apply_block_kernel(int ne, int nrhs_rt, int symm, int d1d, int q1d,
                                              const typename AR::In *__restrict__ gB,
                                              const typename AR::In *__restrict__ gG,
                                              const typename AR::Qd *__restrict__ qd,
@@ -580,6 +580,7 @@ __global__ void diffusion_apply_block_kernel(int ne, int nrhs, int symm, int d1d
    using V = typename AR::V;
    using Qd = typename AR::Qd;
    if (skip && *skip) { return; }
+   const int nrhs = TR ? TR : nrhs_rt;   // TR > 0: the count (and strides) known at compile time
    const int D = TD ? TD : d1d;
    const int Q = TQ ? TQ : q1d;
    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;

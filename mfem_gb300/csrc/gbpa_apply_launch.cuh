@@ -72,10 +72,15 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
 // Block (multi right-hand side) diffusion apply: compile-time kernels for
 // Q = D + 1, the generic kernel otherwise.
 template <typename AR>
-static const void *diffusion_block_kernel_for(int D, int Q)
+static const void *diffusion_block_kernel_for(int D, int Q, int nrhs)
 {
+   // 8 right-hand sides (the combined form's count): strides known at compile time
 #define GBPA_CASE(d) \
-   if (D == d && Q == d + 1) { return (const void *)diffusion_apply_block_kernel<AR, d, d + 1>; }
+   if (D == d && Q == d + 1) \
+   { \
+      return nrhs == 8 ? (const void *)diffusion_apply_block_kernel<AR, d, d + 1, 8> \
+                       : (const void *)diffusion_apply_block_kernel<AR, d, d + 1>; \
+   }
    GBPA_CASE(2) GBPA_CASE(3) GBPA_CASE(4) GBPA_CASE(5) GBPA_CASE(6) GBPA_CASE(7) GBPA_CASE(8)
 #undef GBPA_CASE
    return (const void *)diffusion_apply_block_kernel<AR, 0, 0>;
@@ -89,7 +94,7 @@ int launch_diffusion_block_ar(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, 
                               typename AR::In *y, const int *skip)
 {
    if (ne == 0) { return GBPA_SUCCESS; }
-   const void *k = diffusion_block_kernel_for<AR>(D, Q);
+   const void *k = diffusion_block_kernel_for<AR>(D, Q, nrhs);
    const int max_thr = max_threads_for(k);   // register-limited block size
    if (Q * Q > max_thr) { return GBPA_ERR_UNSUPPORTED; }
    const int prec = sizeof(typename AR::V) == 4 ? GBPA_F32 : GBPA_F64;
