@@ -203,6 +203,10 @@ enum gbpa_kind { GBPA_DIFFUSION = 0, GBPA_MASS = 1 };
  * operation) -- because GB300's FP32 rate is ~58x its FP64 rate. The operator
  * keeps an internal (hi, lo) float copy of qdata (same bytes as FP64). */
 enum gbpa_precision { GBPA_F64 = 0, GBPA_F32 = 1, GBPA_F64X2 = 2 };
+/* GBPA_SCATTER_CSR: deterministic row sums in the reference's order (default).
+ * GBPA_SCATTER_ATOMIC: the element kernel adds its results into y through the
+ * gather map (no E-vector); reproducible to rounding only; y must not alias x.
+ * The block and batched solvers always use the CSR scatter. */
 enum gbpa_scatter { GBPA_SCATTER_CSR = 0, GBPA_SCATTER_ATOMIC = 1 };
 
 typedef struct gbpa_operator_desc

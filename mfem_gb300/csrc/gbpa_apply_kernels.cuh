@@ -191,6 +191,31 @@ __device__ __forceinline__ typename AR::V gather_value(const typename AR::In *__
    return g >= 0 ? v : AR::neg(v);
 }
 
+// One E-slot's result r. mode 0: y[k] = r; 1: y[k] += r (E-vector y);
+// GBPA_OUT_ATOMIC: r is added atomically, with the slot's sign, into the
+// L-vector y at the dof the gather map gives the slot (ElementRestriction::
+// MultTranspose fused into the apply, summed in arrival order instead of the
+// CSR row order); constrained slots (GBPA_GATHER_SKIP, or masked dofs) add
+// nothing.
+template <typename T>
+__device__ __forceinline__ void store_result(T *y, long long k, long long slot, T r, int mode,
+                                             const int *__restrict__ gmap,
+                                             const unsigned char *__restrict__ mask)
+{
+   if (mode == GBPA_OUT_ATOMIC)
+   {
+      const int g = __ldg(gmap + slot);
+      if (g == GBPA_GATHER_SKIP) { return; }
+      const int j = g >= 0 ? g : -1 - g;
+      if (mask && __ldg(mask + j)) { return; }
+      atomicAdd(y + j, g >= 0 ? r : -r);
+   }
+   else
+   {
+      y[k] = mode ? y[k] + r : r;
+   }
+}
+
 // Shared memory (in V units) per element for the diffusion apply.
 __host__ __device__ inline int diff_smem_per_elem(int D, int Q)
 {
@@ -474,9 +499,9 @@ diffusion_element(long long e, bool active, bool part, int D, int Q, int tx, int
                   AR::mac(v, cGx[qx], U0[o]);
                   AR::mac(v, cBx[qx], U12[o]);
                }
-               const long long k = (base + dx + D * (dy + D * dz)) * ys;
+               const long long slot = base + dx + D * (dy + D * dz);
                const typename AR::In r = qok ? AR::out(AR::fin(v)) : (typename AR::In)NAN;
-               y[k] = accumulate ? y[k] + r : r;
+               store_result(y, slot * ys, slot, r, accumulate, gmap, mask);
             }
          }
       }
@@ -756,7 +781,7 @@ __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
                }
                const long long k = base + dx + D * (dy + D * dz);
                const typename AR::In rr = AR::out(AR::fin(v));
-               y[k] = accumulate ? y[k] + rr : rr;
+               store_result(y, k, k, rr, accumulate, gmap, mask);
             }
          }
    }

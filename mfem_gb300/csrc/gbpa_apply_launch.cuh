@@ -38,7 +38,7 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
                         const typename AR::In *B, const typename AR::In *G,
                         const typename AR::Qd *qd, const typename AR::In *x,
                         const int *gather_map, const unsigned char *ess_mask,
-                        typename AR::In *y, bool accumulate, const int *skip)
+                        typename AR::In *y, int accumulate, const int *skip)
 {
    if (ne == 0) { return GBPA_SUCCESS; }
    if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
@@ -61,7 +61,7 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
       if (with <= 200 * 1024) { smem = with; }
       else { tma = 0; }
    }
-   int acc = accumulate ? 1 : 0;
+   int acc = accumulate;
    void *args[] = {&ne, &symm, &D, &Q, (void *)&B, (void *)&G, (void *)&qd,
                    (void *)&x, (void *)&gather_map, (void *)&ess_mask, &y, &acc,
                    (void *)&skip, &tma};
@@ -120,7 +120,7 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
                    const typename AR::In *B, const typename AR::Qd *qd,
                    const typename AR::In *x, const int *gather_map,
                    const unsigned char *ess_mask, typename AR::In *y,
-                   bool accumulate, const int *skip, int qdiv = 1)
+                   int accumulate, const int *skip, int qdiv = 1)
 {
    if (ne == 0) { return GBPA_SUCCESS; }
    if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
@@ -131,7 +131,7 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
    const int nbz = std::max(1, std::min(elements_per_block(GBPA_MASS, prec, D, Q),
                                         max_threads_for(k) / (Q * Q)));
    const size_t smem = sizeof(typename AR::V) * (Q * D + (size_t)nbz * mass_smem_per_elem(D, Q));
-   int acc = accumulate ? 1 : 0;
+   int acc = accumulate;
    void *args[] = {&ne, &D, &Q, (void *)&B, (void *)&qd, (void *)&x,
                    (void *)&gather_map, (void *)&ess_mask, &y, &acc, (void *)&skip, &qdiv};
    return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, nbz),

@@ -7,7 +7,7 @@ namespace gbpa
 int launch_diffusion_apply_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
                               const double *G, const float2 *qd, const double *x,
                               const int *gather_map, const unsigned char *ess_mask, double *y,
-                              bool accumulate, const int *skip)
+                              int accumulate, const int *skip)
 {
    return launch_diffusion_ar<ArX2, 10, false>(ctx, GBPA_F64X2, ne, symm, D, Q, B, G, qd, x, gather_map,
                                     ess_mask, y, accumulate, skip);

@@ -6,7 +6,7 @@ namespace gbpa
 {
 int launch_mass_apply_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const float2 *qd,
                          const double *x, const int *gather_map, const unsigned char *ess_mask,
-                         double *y, bool accumulate, const int *skip)
+                         double *y, int accumulate, const int *skip)
 {
    return launch_mass_ar<ArX2, 10, false>(ctx, GBPA_F64X2, ne, D, Q, B, qd, x, gather_map, ess_mask, y,
                                accumulate, skip);

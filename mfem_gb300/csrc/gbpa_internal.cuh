@@ -59,42 +59,47 @@ inline unsigned grid_for(int64_t n, int block, int max_blocks = 1 << 20)
 // E-vector apply kernels (2D-slab: one thread per (qx,qy) column, z in
 // registers, nbz elements per block). gather_map != nullptr: x is an
 // L-vector gathered (with sign) through the map; ess_mask zeroes
-// constrained dofs on the fly. accumulate: y += result, else y = result.
+// constrained dofs on the fly. accumulate (the output mode): 0 y = result,
+// 1 y += result (E-vector y), GBPA_OUT_ATOMIC: each E-slot's result is added
+// atomically into the L-vector y at the dof the gather map gives it (the
+// scatter fused into the apply; y must be zeroed first, constrained slots add
+// nothing).
+constexpr int GBPA_OUT_ATOMIC = 2;
 template <typename T>
 int launch_diffusion_apply(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
                            const T *B, const T *G, const T *qd, const T *x,
                            const int *gather_map, const unsigned char *ess_mask,
-                           T *y, bool accumulate, const int *skip = nullptr);
+                           T *y, int accumulate, const int *skip = nullptr);
 template <typename T>
 int launch_mass_apply(gbpa_ctx *ctx, int ne, int D, int Q, const T *B,
                       const T *qd, const T *x, const int *gather_map,
-                      const unsigned char *ess_mask, T *y, bool accumulate,
+                      const unsigned char *ess_mask, T *y, int accumulate,
                       const int *skip = nullptr);
 template <>
 int launch_diffusion_apply<double>(gbpa_ctx *, int, int, int, int, const double *, const double *,
                                    const double *, const double *, const int *,
-                                   const unsigned char *, double *, bool, const int *);
+                                   const unsigned char *, double *, int, const int *);
 template <>
 int launch_diffusion_apply<float>(gbpa_ctx *, int, int, int, int, const float *, const float *,
                                   const float *, const float *, const int *,
-                                  const unsigned char *, float *, bool, const int *);
+                                  const unsigned char *, float *, int, const int *);
 template <>
 int launch_mass_apply<double>(gbpa_ctx *, int, int, int, const double *, const double *,
-                              const double *, const int *, const unsigned char *, double *, bool,
+                              const double *, const int *, const unsigned char *, double *, int,
                               const int *);
 template <>
 int launch_mass_apply<float>(gbpa_ctx *, int, int, int, const float *, const float *,
-                             const float *, const int *, const unsigned char *, float *, bool,
+                             const float *, const int *, const unsigned char *, float *, int,
                              const int *);
 // FP64-accurate double-float arithmetic on the FP32 pipes (qdata split into
 // float2 (hi, lo) by launch_split_x2).
 int launch_diffusion_apply_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
                               const double *G, const float2 *qd, const double *x,
                               const int *gather_map, const unsigned char *ess_mask, double *y,
-                              bool accumulate, const int *skip = nullptr);
+                              int accumulate, const int *skip = nullptr);
 int launch_mass_apply_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const float2 *qd,
                          const double *x, const int *gather_map, const unsigned char *ess_mask,
-                         double *y, bool accumulate, const int *skip = nullptr);
+                         double *y, int accumulate, const int *skip = nullptr);
 int launch_split_x2(gbpa_ctx *ctx, int64_t n, const double *a, float2 *b);
 // FP64 E-vector mass apply (y += A_e x) where element e reads the qdata of
 // element e / qdiv.

@@ -123,7 +123,8 @@ __global__ void pcg_scatter_den_kernel(int ndofs, const int *__restrict__ offset
    {
       T v;
       if (mask && mask[i]) { v = d[i]; }
-      else { v = csr_row_sum<T>(offsets, indices, yE, i); }
+      else if (offsets) { v = csr_row_sum<T>(offsets, indices, yE, i); }
+      else { v = z[i]; }   // summed into z by the apply's atomic scatter
       z[i] = v;
       s += (double)d[i] * (double)v;
    }
@@ -197,6 +198,19 @@ __global__ void fill_mask_kernel(int n, const int *ess, unsigned char *mask, int
       const int k = ess[i];
       if (k < 0 || k >= ndofs) { atomicOr(flags, GBPA_FLAG_INDEX); continue; }
       mask[k] = 1;
+   }
+}
+
+// y[i] = x[i] on constrained dofs (ConstrainedOperator::Mult, after the
+// atomic scatter left them zero)
+template <typename T>
+__global__ void copy_masked_kernel(int64_t n, const unsigned char *__restrict__ mask,
+                                   const T *__restrict__ x, T *__restrict__ y)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      if (mask[i]) { y[i] = x[i]; }
    }
 }
 
@@ -353,9 +367,11 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    return GBPA_SUCCESS;
 }
 
-// yE = A_e (R x) with the gather fused (ess dofs read as zero)
+// out = A_e (R x) with the gather fused (ess dofs read as zero): the E-vector
+// (mode 0), or with GBPA_OUT_ATOMIC the L-vector R^T A_e R x summed by atomics
+// in the apply itself (out zeroed by the caller).
 template <typename T>
-static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
+static int apply_to(gbpa_operator *op, const T *x, T *out, int mode, const int *skip)
 {
    const gbpa_operator_desc &d = op->d;
    if (d.precision == GBPA_F64X2)
@@ -365,34 +381,57 @@ static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
       {
          return launch_diffusion_apply_x2(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
                                           (const double *)d.B, (const double *)d.G, op->qd2, xd,
-                                          op->gather(), op->gather_mask(), (double *)op->yE, false, skip);
+                                          op->gather(), op->gather_mask(), (double *)out, mode, skip);
       }
       return launch_mass_apply_x2(op->ctx, d.ne, d.d1d, d.q1d, (const double *)d.B, op->qd2, xd,
-                                  op->gather(), op->gather_mask(), (double *)op->yE, false, skip);
+                                  op->gather(), op->gather_mask(), (double *)out, mode, skip);
    }
    if (d.kind == GBPA_DIFFUSION)
    {
       return launch_diffusion_apply<T>(op->ctx, d.ne, d.symm ? 1 : 0, d.d1d, d.q1d,
                                        (const T *)d.B, (const T *)d.G, (const T *)d.qdata, x,
-                                       op->gather(), op->gather_mask(), (T *)op->yE, false, skip);
+                                       op->gather(), op->gather_mask(), out, mode, skip);
    }
    return launch_mass_apply<T>(op->ctx, d.ne, d.d1d, d.q1d, (const T *)d.B,
-                               (const T *)d.qdata, x, op->gather(), op->gather_mask(), (T *)op->yE,
-                               false, skip);
+                               (const T *)d.qdata, x, op->gather(), op->gather_mask(), out, mode,
+                               skip);
 }
+
+template <typename T>
+static int apply_evec(gbpa_operator *op, const T *x, const int *skip)
+{
+   return apply_to<T>(op, x, (T *)op->yE, 0, skip);
+}
+
+static bool atomic_scatter(const gbpa_operator *op) { return op->d.scatter == GBPA_SCATTER_ATOMIC; }
 
 template <typename T>
 static int op_mult(gbpa_operator *op, const T *x, T *y)
 {
+   gbpa_ctx *ctx = op->ctx;
+   if (atomic_scatter(op))
+   {
+      // y = R^T A_e R x by atomics inside the apply, then y[ess] = x[ess]
+      const int64_t n = op->d.ndofs;
+      int rc = check_cuda(cudaMemsetAsync(y, 0, sizeof(T) * n, ctx->stream), "memset(y)");
+      if (!rc) { rc = apply_to<T>(op, x, y, GBPA_OUT_ATOMIC, nullptr); }
+      if (!rc && op->mask)
+      {
+         copy_masked_kernel<T><<<grid_for(n, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(n, op->mask, x, y);
+         rc = last_launch(ctx, "copy_masked");
+      }
+      return rc;
+   }
    int rc = apply_evec<T>(op, x, nullptr);
    if (rc) { return rc; }
-   return launch_csr_scatter<T>(op->ctx, op->d.ndofs, op->d.offsets, op->d.indices,
+   return launch_csr_scatter<T>(ctx, op->d.ndofs, op->d.offsets, op->d.indices,
                                 (const T *)op->yE, y, op->mask, x, false, false);
 }
 
 extern "C" int gbpa_operator_mult(gbpa_operator_t op, const void *x, void *y)
 {
    if (!op || (op->d.ndofs > 0 && (!x || !y))) { return GBPA_ERR_INVALID_ARGUMENT; }
+   if (atomic_scatter(op) && x == y) { return GBPA_ERR_INVALID_ARGUMENT; }   // y is summed while x is read
    if (op->d.ndofs == 0) { return GBPA_SUCCESS; }
    if (op->d.precision != GBPA_F32) { return op_mult<double>(op, (const double *)x, (double *)y); }
    return op_mult<float>(op, (const float *)x, (float *)y);
@@ -508,7 +547,34 @@ static int pcg_check_every()
    return k >= 1 && k <= 1000 ? k : 10;
 }
 
-// One PCG iteration body: update (x, r, z, betanom), direction, A d, den.
+// z = A d (constrained: z[ess] = d[ess]), den = (d, z), alpha = nom / den:
+// the element apply into the E-vector then the CSR scatter with the dot, or,
+// for an operator with the atomic scatter, the apply summing into z (zeroed
+// first) then the dot. Both skip their work once the state reports done.
+template <typename T>
+static int pcg_apply_den(gbpa_operator *op, T *d, T *z, unsigned grid, int first)
+{
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t n = op->d.ndofs;
+   int rc;
+   if (atomic_scatter(op))
+   {
+      rc = check_cuda(cudaMemsetAsync(z, 0, sizeof(T) * n, ctx->stream), "memset(z)");
+      if (!rc) { rc = apply_to<T>(op, d, z, GBPA_OUT_ATOMIC, &op->state->done); }
+      if (rc) { return rc; }
+      pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+         op->d.ndofs, nullptr, nullptr, nullptr, z, d, op->mask, op->partials + 2048, op->state, first);
+      return last_launch(ctx, "pcg_den");
+   }
+   rc = apply_evec<T>(op, d, &op->state->done);
+   if (rc) { return rc; }
+   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
+      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
+      op->partials + 2048, op->state, first);
+   return last_launch(ctx, "pcg_scatter_den");
+}
+
+// One PCG iteration body: update (x, r, z, betanom), direction, A d, den.// One PCG iteration body: update (x, r, z, betanom), direction, A d, den.
 template <typename T>
 static int pcg_iteration(gbpa_operator *op, T *x, const T *dinv, unsigned grid)
 {
@@ -522,12 +588,7 @@ static int pcg_iteration(gbpa_operator *op, T *x, const T *dinv, unsigned grid)
    pcg_direction_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, z, d, op->state);
    rc = last_launch(ctx, "pcg_direction");
    if (rc) { return rc; }
-   rc = apply_evec<T>(op, d, &op->state->done);
-   if (rc) { return rc; }
-   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
-      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
-      op->partials + 2048, op->state, 0);
-   return last_launch(ctx, "pcg_scatter_den");
+   return pcg_apply_den<T>(op, d, z, grid, 0);
 }
 
 // Runs captured K-iteration graphs of pcg_iteration (x, dinv fixed) until
@@ -625,12 +686,7 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
    rc = last_launch(ctx, "pcg_init");
    if (rc) { return rc; }
    // z = A d, den = (d, z), alpha = nom / den
-   rc = apply_evec<T>(op, d, &op->state->done);
-   if (rc) { return rc; }
-   pcg_scatter_den_kernel<T><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
-      op->d.ndofs, op->d.offsets, op->d.indices, (const T *)op->yE, z, d, op->mask,
-      op->partials + 2048, op->state, 1);
-   rc = last_launch(ctx, "pcg_scatter_den");
+   rc = pcg_apply_den<T>(op, d, z, grid, 1);
    if (rc) { return rc; }
 
    rc = pcg_graph_loop<T>(op, x, dinv, max_it);
@@ -874,14 +930,7 @@ extern "C" int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_
    pcg_init_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, b32, x32, r, z, d, dinv32, 0,
                                                               op->partials, op->state);
    rc = last_launch(ctx, "pcg_init");
-   if (!rc) { rc = apply_evec<float>(op, d, &op->state->done); }
-   if (!rc)
-   {
-      pcg_scatter_den_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
-         n, op->d.offsets, op->d.indices, (const float *)op->yE, z, d, op->mask, op->partials + 2048,
-         op->state, 1);
-      rc = last_launch(ctx, "pcg_scatter_den");
-   }
+   if (!rc) { rc = pcg_apply_den<float>(op, d, z, grid, 1); }
    if (rc) { return rc; }
    for (;;)
    {
@@ -925,14 +974,7 @@ extern "C" int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_
          pcg_direction_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(n, z, d, op->state);
          rc = last_launch(ctx, "pcg_direction");
       }
-      if (!rc) { rc = apply_evec<float>(op, d, &op->state->done); }
-      if (!rc)
-      {
-         pcg_scatter_den_kernel<float><<<grid, PCG_BLOCK, 0, ctx->stream>>>(
-            n, op->d.offsets, op->d.indices, (const float *)op->yE, z, d, op->mask,
-            op->partials + 2048, op->state, 0);
-         rc = last_launch(ctx, "pcg_scatter_den");
-      }
+      if (!rc) { rc = pcg_apply_den<float>(op, d, z, grid, 0); }
       if (rc) { return rc; }
    }
    cudaEventRecord(e1, ctx->stream);
