@@ -130,3 +130,11 @@ def test_host_restriction_build_rejects_out_of_range(lib):
     off = np.zeros(5, np.int32); ind = np.zeros(4, np.int32); gm = np.zeros(4, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     assert lib.gbpa_restriction_build(1, 4, 4, P(ed), None, P(off), P(ind), P(gm)) == -9
+
+
+def test_every_entry_point_is_documented_for_integrators():
+    """INTEGRATION.md names every exported entry point (call-site table or
+    the list of the remaining ones)."""
+    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    missing = [n for n in declared_symbols() if n not in doc]
+    assert not missing, missing
