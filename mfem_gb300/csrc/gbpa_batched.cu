@@ -569,9 +569,7 @@ int run_graph_schedule(gbpa_ctx *ctx, int precision, const std::vector<BProb> &h
                       "cudaStreamCreate(capture)");
       if (rc) { return rc; }
    }
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    if (nchunk_all > 0)
    {
       bg_init_kernel<<<nchunk_all, BATCH_THREADS, 0, ctx->stream>>>(G);
@@ -668,11 +666,7 @@ int run_graph_schedule(gbpa_ctx *ctx, int precision, const std::vector<BProb> &h
       ctx->launches += (int64_t)K * per_iter;
       launched += K;
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float t = 0.f;
-   cudaEventElapsedTime(&t, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float t = timer.stop(ctx->stream);
    if (exec) { cudaGraphExecDestroy(exec); }
    if (ms) { *ms = t; }
    return rc;
@@ -876,16 +870,11 @@ static int batched_solve(gbpa_ctx *ctx, int nprob, const gbpa_problem_desc *prob
       if (per_sm < 1) { return GBPA_ERR_UNSUPPORTED; }
       const int grid = per_sm * ctx->num_sms;
       void *args[] = {&P};
-      cudaEvent_t e0, e1;
-      cudaEventCreate(&e0); cudaEventCreate(&e1);
-      cudaEventRecord(e0, ctx->stream);
+      StreamTimer timer(ctx->stream);
       rc = check_cuda(cudaLaunchCooperativeKernel(kfn, dim3(grid), dim3(BATCH_THREADS), args, smem_max,
                                                   ctx->stream), "cudaLaunchCooperativeKernel");
       ctx->launches++;
-      cudaEventRecord(e1, ctx->stream);
-      if (!rc) { rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize"); }
-      if (!rc) { cudaEventElapsedTime(&ms, e0, e1); }
-      cudaEventDestroy(e0); cudaEventDestroy(e1);
+      if (!rc) { ms = timer.stop(ctx->stream); }
       if (rc) { return rc; }
       rc = check_cuda(cudaMemcpy(hs.data(), base + o_scal, sizeof(BScal) * nprob, cudaMemcpyDeviceToHost),
                       "copy back");

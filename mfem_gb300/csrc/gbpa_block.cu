@@ -495,9 +495,7 @@ static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T 
    const unsigned grid = grid_for(n, BK_BLOCK, 4 * ctx->num_sms);
    BlockState h{};
    h.nrhs = R; h.max_it = max_it; h.rel2 = rel_tol * rel_tol; h.abs2 = abs_tol * abs_tol;
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    rc = check_cuda(cudaMemcpyAsync(w.st, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream), "copy");
    if (!rc)
    {
@@ -510,11 +508,7 @@ static int block_pcg_run(gbpa_operator *op, int R, const T *dinv, const T *b, T 
       rc = launch_scatter_den<T>(op, R, z, d, w.partials + 4096 * 4, w.st, 1);
    }
    if (!rc) { rc = block_iterate<T>(op, R, x, r, z, d, dinv, w, max_it); }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    if (ms_out) { *ms_out = ms; }
    if (!rc) { rc = check_cuda(cudaMemcpy(h_out, w.st, sizeof(BlockState), cudaMemcpyDeviceToHost), "copy"); }
    w.free_all();
@@ -610,9 +604,7 @@ extern "C" int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A
    unsigned int *counter = (unsigned int *)(red + 4096 * BK_MAXR);
    double *d_out = red + 4096 * BK_MAXR + 16;
    cudaMemsetAsync(counter, 0, sizeof(unsigned int) * 4, ctx->stream);
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    double nb2[BK_MAXR] = {0}, rn2[BK_MAXR] = {0};
    int conv[BK_MAXR] = {0}, outer_its[BK_MAXR] = {0}, inner_its[BK_MAXR] = {0};
    rc = check_cuda(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream), "memset");
@@ -655,11 +647,7 @@ extern "C" int gbpa_pcg_solve_block_mixed(gbpa_operator_t A64, gbpa_operator_t A
          rc = last_launch(ctx, "blk_residual");
       }
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    cleanup();
    int all = 1;
    for (int q = 0; q < R; ++q)
@@ -728,9 +716,7 @@ extern "C" int gbpa_pcg_solve_block_mixed_reliable(gbpa_operator_t A64, gbpa_ope
    double *d_out = red + 4096 * BK_MAXR + 16;
    double *d_nb2 = red + 4096 * BK_MAXR + 32;
    const unsigned grid = grid_for(n, BK_BLOCK, 4 * ctx->num_sms);
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    double nb2[BK_MAXR] = {0}, rn2[BK_MAXR] = {0};
    int conv[BK_MAXR] = {0}, repl[BK_MAXR] = {0};
    BlockState hs{};
@@ -817,11 +803,7 @@ extern "C" int gbpa_pcg_solve_block_mixed_reliable(gbpa_operator_t A64, gbpa_ope
       if (!rc) { rc = block_apply_evec<float>(op, R, d, &w.st->all_done); }
       if (!rc) { rc = launch_scatter_den<float>(op, R, z, d, w.partials + 4096 * 4, w.st, 0); }
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    cleanup();
    for (int q = 0; q < R; ++q)
    {

@@ -55,6 +55,34 @@ inline unsigned grid_for(int64_t n, int block, int max_blocks = 1 << 20)
    return (unsigned)g;
 }
 
+// Device time of a stretch of work on a stream: started at construction,
+// read by stop(); the events are released on every return path.
+struct StreamTimer
+{
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   explicit StreamTimer(cudaStream_t s)
+   {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, s);
+   }
+   // milliseconds since construction (waits for the stream's work so far)
+   float stop(cudaStream_t s)
+   {
+      cudaEventRecord(e1, s);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) == cudaSuccess) { cudaEventElapsedTime(&ms, e0, e1); }
+      return ms;
+   }
+   ~StreamTimer()
+   {
+      if (e0) { cudaEventDestroy(e0); }
+      if (e1) { cudaEventDestroy(e1); }
+   }
+   StreamTimer(const StreamTimer &) = delete;
+   StreamTimer &operator=(const StreamTimer &) = delete;
+};
+
 // ---------------------------------------------------------------- kernels
 // E-vector apply kernels (2D-slab: one thread per (qx,qy) column, z in
 // registers, nbz elements per block). gather_map != nullptr: x is an

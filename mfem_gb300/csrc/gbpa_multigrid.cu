@@ -814,9 +814,7 @@ extern "C" int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const do
    int rc = dev_alloc((void **)&r, sizeof(double) * n);
    if (!rc) { rc = dev_alloc((void **)&d, sizeof(double) * n); }
    if (!rc) { rc = dev_alloc((void **)&z, sizeof(double) * n); }
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    M->coarse_iterations = 0;
    int final_iter = 0, converged = 0, status = GBPA_SUCCESS;
    double nom = 0.0, nom0 = 0.0, den = 0.0, betanom = 0.0;
@@ -859,11 +857,7 @@ extern "C" int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const do
          }
       }
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    cudaFree(r); cudaFree(d); cudaFree(z);
    if (info)
    {

@@ -666,9 +666,7 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
    // 4 blocks of 512 threads per SM: full occupancy for the streaming vector
    // phases (partials buffer holds 2048 entries per reduction)
    const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    PcgState h{};
    h.rel_tol2 = rel_tol * rel_tol;
    h.abs_tol2 = abs_tol * abs_tol;
@@ -691,11 +689,7 @@ static int pcg_run(gbpa_operator *op, const T *dinv, const T *b, T *x, double re
 
    rc = pcg_graph_loop<T>(op, x, dinv, max_it);
    if (rc) { return rc; }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    if (elapsed_ms) { *elapsed_ms = ms; }
    rc = check_cuda(cudaMemcpy(&h, op->state, sizeof(PcgState), cudaMemcpyDeviceToHost),
                    "cudaMemcpy(state)");
@@ -799,9 +793,7 @@ extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, co
    float *r32 = (float *)scratch(ctx, SLOT_PCG32, sizeof(float) * 2 * n);
    if (!r32) { return GBPA_ERR_OUT_OF_MEMORY; }
    float *c32 = r32 + n;
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    // x = 0, r = b
    rc = check_cuda(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream), "memset(x)");
    if (!rc) { rc = check_cuda(cudaMemcpyAsync(A64->r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream), "copy"); }
@@ -842,11 +834,7 @@ extern "C" int gbpa_pcg_solve_mixed(gbpa_operator_t A64, gbpa_operator_t A32, co
       rc = last_launch(ctx, "residual");
       if (rc) { return rc; }
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    inf->seconds = ms * 1e-3;
    inf->outer_iterations = outer;
    inf->inner_iterations = inner_total;
@@ -899,9 +887,7 @@ extern "C" int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_
    float *r = (float *)op->r, *d = (float *)op->dv, *z = (float *)op->z;
    const unsigned grid = grid_for(n, PCG_BLOCK, 4 * ctx->num_sms);
    const unsigned vg = grid_for(n, 256, 8 * ctx->num_sms);
-   cudaEvent_t e0, e1;
-   cudaEventCreate(&e0); cudaEventCreate(&e1);
-   cudaEventRecord(e0, ctx->stream);
+   StreamTimer timer(ctx->stream);
    double hb[2] = {0.0, 0.0};
    double rel = 1.0;
    int updates = 0, converged = 0;
@@ -977,11 +963,7 @@ extern "C" int gbpa_pcg_solve_mixed_reliable(gbpa_operator_t A64, gbpa_operator_
       if (!rc) { rc = pcg_apply_den<float>(op, d, z, grid, 0); }
       if (rc) { return rc; }
    }
-   cudaEventRecord(e1, ctx->stream);
-   cudaEventSynchronize(e1);
-   float ms = 0.f;
-   cudaEventElapsedTime(&ms, e0, e1);
-   cudaEventDestroy(e0); cudaEventDestroy(e1);
+   const float ms = timer.stop(ctx->stream);
    inf->seconds = ms * 1e-3;
    inf->outer_iterations = updates;
    inf->inner_iterations = h.iter;
