@@ -18,6 +18,7 @@ GBPA_DIFFUSION, GBPA_MASS = 0, 1
 GBPA_F64, GBPA_F32, GBPA_F64X2 = 0, 1, 2
 GBPA_SCATTER_CSR, GBPA_SCATTER_ATOMIC = 0, 1
 GBPA_BATCH_GRAPH, GBPA_BATCH_PERSISTENT = 0, 1
+GBPA_LAYOUT_SLAB2D, GBPA_LAYOUT_3D = 0, 1
 
 STATUS = {
     0: "success", -1: "invalid argument", -2: "unsupported", -3: "CUDA error",
@@ -126,6 +127,8 @@ SIGNATURES = {
     "gbpa_pcg_solve_mg": (I, [P, P, P, P, D, D, I, ctypes.POINTER(SolveInfo)]),
     "gbpa_set_elements_per_block": (I, [I, I, I, I, I]),
     "gbpa_get_elements_per_block": (I, [I, I, I, I]),
+    "gbpa_set_apply_layout": (I, [I, I, I, I, I, I]),
+    "gbpa_get_apply_layout": (I, [I, I, I, I, ctypes.POINTER(I)]),
 }
 
 _lib = None

@@ -1,11 +1,15 @@
-"""Autotuner for the apply kernels' block shape.
+"""Autotuner for the apply kernels' thread layout and block shape.
 
 For each (integrator, arithmetic, order p) the 2D-slab apply kernel runs with
 block (Q, Q, nbz); nbz -- elements per block -- sets the block size, the
-shared memory per block and therefore the occupancy. The tuner times the
-gather-fused element kernel on a synthetic jittered mesh for every feasible
-nbz and keeps the fastest. The table is saved as JSON (mfem_gb300/tuning.json)
-and applied by Device() on start-up through gbpa_set_elements_per_block.
+shared memory per block and therefore the occupancy. For diffusion the 3D
+layout (block (Q, Q, Q*nbz), one thread per quadrature point) is a
+second candidate. The tuner times the gather-fused element kernel on a
+synthetic jittered mesh for every feasible (layout, nbz) and keeps the
+fastest. The table is saved as JSON (mfem_gb300/tuning.json: "nbz" for the 2D
+slab, "layout3d" for the orders where the 3D layout won) and applied by
+Device() on start-up through gbpa_set_elements_per_block and
+gbpa_set_apply_layout.
 
     python -m mfem_gb300.autotune [--orders 1-8] [--dofs 2e6] [--out path]
 """
@@ -35,11 +39,38 @@ def apply_table(lib, table):
     return n
 
 
+# (D, Q) pairs with a compile-time 3D-layout diffusion kernel (GBPA_DQ3_LIST)
+DQ3 = {(2, 2), (2, 3), (3, 3), (3, 4), (4, 4), (4, 5), (5, 5), (5, 6), (6, 6), (6, 7), (7, 7), (7, 8),
+       (8, 8), (8, 9), (9, 9), (9, 10), (4, 6), (5, 8)}
+
+
+def apply_layouts(lib, layout3d):
+    """Install the 3D-layout entries {key: nbz} (diffusion only)."""
+    n = 0
+    for k, nbz in layout3d.items():
+        kind, prec, D, Q = k.split(":")
+        if lib.gbpa_set_apply_layout(KINDS[kind], PRECS[prec], int(D), int(Q), 1, int(nbz)) == 0:
+            n += 1
+    return n
+
+
 def load_default(lib):
     if os.path.exists(TUNING):
         with open(TUNING) as f:
-            return apply_table(lib, json.load(f).get("nbz", {}))
+            t = json.load(f)
+        return apply_table(lib, t.get("nbz", {})) + apply_layouts(lib, t.get("layout3d", {}))
     return 0
+
+
+def candidates_3d(prec, D, Q):
+    w = 4 if prec == "f32" else 8
+    per = max(D ** 3, 3 * D * Q * Q) + max(2 * D * D * Q, 3 * Q ** 3)
+    out = []
+    for nbz in range(1, 65):
+        if nbz * Q ** 3 > 1024 or nbz * Q > 64 or w * (2 * Q * D + nbz * per) > 200 * 1024:
+            break
+        out.append(nbz)
+    return out
 
 
 def smem_bytes(kind, w, D, Q, nbz):
@@ -84,7 +115,7 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
     from .pa import DiffusionIntegrator, Device, FiniteElementSpace, MassIntegrator, PAOperator
     dev = Device.get()
     lib = dev.lib
-    table, timings = {}, {}
+    table, timings, layout3d = {}, {}, {}
     for p in orders:
         n = max(2, int(round((target_dofs ** (1 / 3) - 1) / p)))
         mesh = fem.CartesianMesh(n, jitter=0.1, seed=1)
@@ -109,17 +140,31 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
                     res[nbz] = ms
                     best = min(best, (ms, nbz))
                 lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, 0)
+                res3, best3 = {}, (float("inf"), None)
+                if kind == "diffusion" and (D, Q) in DQ3:
+                    for nbz in candidates_3d(prec, D, Q):
+                        lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 1, nbz)
+                        ms = time_nbz(lib, op, x, yE, reps)
+                        res3[nbz] = ms
+                        best3 = min(best3, (ms, nbz))
+                    lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 0, 0)
                 if best[1] is not None:
-                    table[key(kind, prec, D, Q)] = best[1]
-                    timings[key(kind, prec, D, Q)] = {"ne": fes.ne, "ndofs": fes.ndofs, "ms": res}
+                    k = key(kind, prec, D, Q)
+                    table[k] = best[1]
+                    timings[k] = {"ne": fes.ne, "ndofs": fes.ndofs, "ms": res}
+                    if res3:
+                        timings[k]["ms_3d"] = res3
+                    if best3[1] is not None and best3[0] < best[0]:
+                        layout3d[k] = best3[1]
                     if verbose:
                         default = lib.gbpa_get_elements_per_block(KINDS[kind], pid, D, Q)
+                        l3 = f"; 3D best nbz={best3[1]} {best3[0]:.4f} ms" if res3 else ""
                         print(f"{kind:9s} {prec:6s} p={p} D={D} Q={Q}: best nbz={best[1]} "
-                              f"{best[0]:.4f} ms (default nbz={default}: {res.get(default, float('nan')):.4f} ms)",
-                              flush=True)
+                              f"{best[0]:.4f} ms (default nbz={default}: {res.get(default, float('nan')):.4f} ms)"
+                              f"{l3}", flush=True)
                 del op, x, yE
             del integ
-    return table, timings
+    return table, timings, layout3d
 
 
 def main():
@@ -127,13 +172,15 @@ def main():
     ap.add_argument("--orders", default="1-8")
     ap.add_argument("--dofs", type=float, default=2e6)
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--kinds", default="diffusion,mass")
     ap.add_argument("--out", default=TUNING)
     args = ap.parse_args()
     lo, hi = (int(v) for v in args.orders.split("-"))
-    table, timings = tune(range(lo, hi + 1), target_dofs=args.dofs, reps=args.reps)
+    table, timings, layout3d = tune(range(lo, hi + 1), kinds=tuple(args.kinds.split(",")),
+                                    target_dofs=args.dofs, reps=args.reps)
     with open(args.out, "w") as f:
-        json.dump({"nbz": table, "timings_ms": timings}, f, indent=1, sort_keys=True)
-    print(f"wrote {args.out} ({len(table)} entries)")
+        json.dump({"nbz": table, "layout3d": layout3d, "timings_ms": timings}, f, indent=1, sort_keys=True)
+    print(f"wrote {args.out} ({len(table)} entries, 3D layout for {len(layout3d)})")
 
 
 if __name__ == "__main__":

@@ -14,15 +14,3 @@ int launch_diffusion_apply<float>(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
                                      ess_mask, y, accumulate, skip);
 }
 } // namespace gbpa
-
-namespace gbpa
-{
-int launch_diffusion_block_f32(gbpa_ctx *ctx, int ne, int nrhs, int symm, int D, int Q,
-                               const float *B, const float *G, const float *qd, const float *x,
-                               const int *gather_map, const unsigned char *ess_mask, float *y,
-                               const int *skip)
-{
-   return launch_diffusion_block_ar<ArF32>(ctx, ne, nrhs, symm, D, Q, B, G, qd, x, gather_map,
-                                           ess_mask, y, skip);
-}
-} // namespace gbpa

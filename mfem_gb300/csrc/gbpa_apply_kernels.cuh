@@ -650,6 +650,186 @@ __global__ void diffusion_apply_block_kernel(int ne, int nrhs_rt, int symm, int 
    }
 }
 
+// 3D layout: block (Q, Q, Q * nbz), one thread per quadrature point (qx, qy,
+// qz) of element blockIdx.x * nbz + threadIdx.z / Q. Every contraction goes
+// through shared memory (six barriers per element); in the stages whose
+// index runs over D < Q the threads beyond D idle. Same contraction sequence
+// and arithmetic as the 2D slab; qdata is read fully coalesced (one point per
+// thread). Per element two buffers are reused stage to stage:
+//   buf1: X (D^3) -> A, Bv, C [dz][qy][qx] -> T0, T1, T2 [dz][qy][qx]
+//   buf2: BX, GX [dz][dy][qx] -> O0, O1, O2 [qz][qy][qx] -> U0, U12 [dz][dy][qx]
+template <int D, int Q>
+__host__ __device__ constexpr int diff3d_buf1() { return D * D * D > 3 * D * Q * Q ? D * D * D : 3 * D * Q * Q; }
+template <int D, int Q>
+__host__ __device__ constexpr int diff3d_buf2() { return 2 * D * D * Q > 3 * Q * Q * Q ? 2 * D * D * Q : 3 * Q * Q * Q; }
+
+template <typename AR, int D, int Q>
+__global__ void diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ gB,
+                                          const typename AR::In *__restrict__ gG,
+                                          const typename AR::Qd *__restrict__ qd,
+                                          const typename AR::In *__restrict__ x,
+                                          const int *__restrict__ gmap,
+                                          const unsigned char *__restrict__ mask,
+                                          typename AR::In *__restrict__ y, int mode,
+                                          const int *__restrict__ skip)
+{
+   using V = typename AR::V;
+   constexpr int D3 = D * D * D, Q3 = Q * Q * Q, DQQ = D * Q * Q, DDQ = D * D * Q;
+   constexpr int S1 = diff3d_buf1<D, Q>(), S2 = diff3d_buf2<D, Q>();
+   if (skip && *skip) { return; }
+   const int tx = threadIdx.x, ty = threadIdx.y;
+   const int tz = threadIdx.z % Q, ez = threadIdx.z / Q;
+   const int nbz = blockDim.z / Q;
+   const long long e = (long long)blockIdx.x * nbz + ez;
+   const bool active = e < ne;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   V *sB = reinterpret_cast<V *>(smem_raw);   // [Q][D]
+   V *sG = sB + Q * D;
+   V *buf1 = sG + Q * D + (size_t)ez * (S1 + S2);
+   V *buf2 = buf1 + S1;
+   const int tid = tx + Q * (ty + Q * threadIdx.z);
+   for (int i = tid; i < Q * D; i += Q * Q * blockDim.z)
+   {
+      const int q = i % Q, d = i / Q;
+      sB[q * D + d] = AR::in(gB[i]);
+      sG[q * D + d] = AR::in(gG[i]);
+   }
+   // gather: the element's thread t loads E-slot t (Q >= D, so Q^3 >= D^3)
+   const int t = tx + Q * (ty + Q * tz);
+   if (t < D3) { buf1[t] = active ? gather_value<AR>(x, gmap, mask, e * D3 + t) : AR::zero(); }
+   __syncthreads();
+   // stage 1 (x), thread (qx, dy, dz): BX, GX
+   if (ty < D && tz < D)
+   {
+      V u = AR::zero(), v = AR::zero();
+      const V *xr = buf1 + D * (ty + D * tz);
+#pragma unroll
+      for (int dx = 0; dx < D; ++dx)
+      {
+         const V xv = xr[dx];
+         AR::mac(u, xv, sB[tx * D + dx]);
+         AR::mac(v, xv, sG[tx * D + dx]);
+      }
+      const int o = (tz * D + ty) * Q + tx;
+      buf2[o] = AR::fin(u);
+      buf2[DDQ + o] = AR::fin(v);
+   }
+   __syncthreads();
+   // stage 2 (y), thread (qx, qy, dz): A = G_x B_y, Bv = B_x G_y, C = B_x B_y
+   if (tz < D)
+   {
+      V a = AR::zero(), b = AR::zero(), c = AR::zero();
+#pragma unroll
+      for (int dy = 0; dy < D; ++dy)
+      {
+         const int o = (tz * D + dy) * Q + tx;
+         const V bx = buf2[o], gx = buf2[DDQ + o];
+         const V by = sB[ty * D + dy], gy = sG[ty * D + dy];
+         AR::mac(a, gx, by);
+         AR::mac(b, bx, gy);
+         AR::mac(c, bx, by);
+      }
+      const int o = (tz * Q + ty) * Q + tx;
+      buf1[o] = AR::fin(a);
+      buf1[DQQ + o] = AR::fin(b);
+      buf1[2 * DQQ + o] = AR::fin(c);
+   }
+   __syncthreads();
+   // stage 3 (z) and the pointwise 3x3 qdata product, thread (qx, qy, qz)
+   {
+      V gx = AR::zero(), gy = AR::zero(), gz = AR::zero();
+#pragma unroll
+      for (int dz = 0; dz < D; ++dz)
+      {
+         const int o = (dz * Q + ty) * Q + tx;
+         const V bz = sB[tz * D + dz], gzv = sG[tz * D + dz];
+         AR::mac(gx, bz, buf1[o]);
+         AR::mac(gy, bz, buf1[DQQ + o]);
+         AR::mac(gz, gzv, buf1[2 * DQQ + o]);
+      }
+      gx = AR::fin(gx); gy = AR::fin(gy); gz = AR::fin(gz);
+      V ox = AR::zero(), oy = AR::zero(), oz = AR::zero();
+      if (active)
+      {
+         const typename AR::Qd *qp = qd + e * (symm ? 6 : 9) * Q3 + t;
+         if (symm)
+         {
+            const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
+            const V O22 = AR::ldq(qp + 3 * Q3), O23 = AR::ldq(qp + 4 * Q3), O33 = AR::ldq(qp + 5 * Q3);
+            AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
+            AR::mac(oy, O12, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
+            AR::mac(oz, O13, gx); AR::mac(oz, O23, gy); AR::mac(oz, O33, gz);
+         }
+         else
+         {
+            const V O11 = AR::ldq(qp), O12 = AR::ldq(qp + Q3), O13 = AR::ldq(qp + 2 * Q3);
+            const V O21 = AR::ldq(qp + 3 * Q3), O22 = AR::ldq(qp + 4 * Q3);
+            const V O23 = AR::ldq(qp + 5 * Q3), O31 = AR::ldq(qp + 6 * Q3);
+            const V O32 = AR::ldq(qp + 7 * Q3), O33 = AR::ldq(qp + 8 * Q3);
+            AR::mac(ox, O11, gx); AR::mac(ox, O12, gy); AR::mac(ox, O13, gz);
+            AR::mac(oy, O21, gx); AR::mac(oy, O22, gy); AR::mac(oy, O23, gz);
+            AR::mac(oz, O31, gx); AR::mac(oz, O32, gy); AR::mac(oz, O33, gz);
+         }
+      }
+      const int o = (tz * Q + ty) * Q + tx;
+      buf2[o] = AR::fin(ox);
+      buf2[Q3 + o] = AR::fin(oy);
+      buf2[2 * Q3 + o] = AR::fin(oz);
+   }
+   __syncthreads();
+   // backward z, thread (qx, qy, dz): T0 = B_z O0, T1 = B_z O1, T2 = G_z O2
+   if (tz < D)
+   {
+      V a = AR::zero(), b = AR::zero(), c = AR::zero();
+#pragma unroll
+      for (int qz = 0; qz < Q; ++qz)
+      {
+         const int o = (qz * Q + ty) * Q + tx;
+         const V bz = sB[qz * D + tz], gzv = sG[qz * D + tz];
+         AR::mac(a, bz, buf2[o]);
+         AR::mac(b, bz, buf2[Q3 + o]);
+         AR::mac(c, gzv, buf2[2 * Q3 + o]);
+      }
+      const int o = (tz * Q + ty) * Q + tx;
+      buf1[o] = AR::fin(a);
+      buf1[DQQ + o] = AR::fin(b);
+      buf1[2 * DQQ + o] = AR::fin(c);
+   }
+   __syncthreads();
+   // backward y, thread (qx, dy, dz): U0 = B_y T0, U12 = G_y T1 + B_y T2
+   if (ty < D && tz < D)
+   {
+      V a = AR::zero(), b = AR::zero();
+#pragma unroll
+      for (int qy = 0; qy < Q; ++qy)
+      {
+         const int o = (tz * Q + qy) * Q + tx;
+         const V by = sB[qy * D + ty], gy = sG[qy * D + ty];
+         AR::mac(a, buf1[o], by);
+         AR::mac(b, buf1[DQQ + o], gy);
+         AR::mac(b, buf1[2 * DQQ + o], by);
+      }
+      const int o = (tz * D + ty) * Q + tx;
+      buf2[o] = AR::fin(a);
+      buf2[DDQ + o] = AR::fin(b);
+   }
+   __syncthreads();
+   // backward x, thread (dx, dy, dz): y = G_x U0 + B_x U12
+   if (active && tx < D && ty < D && tz < D)
+   {
+      V v = AR::zero();
+#pragma unroll
+      for (int qx = 0; qx < Q; ++qx)
+      {
+         const int o = (tz * D + ty) * Q + qx;
+         AR::mac(v, sG[qx * D + tx], buf2[o]);
+         AR::mac(v, sB[qx * D + tx], buf2[DDQ + o]);
+      }
+      const long long slot = e * D3 + tx + D * (ty + D * tz);
+      store_result(y, slot, slot, AR::out(AR::fin(v)), mode, gmap, mask);
+   }
+}
+
 template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
 __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
                                   const typename AR::In *__restrict__ gB,

@@ -9,6 +9,7 @@
 #include "gbpa_apply_kernels.cuh"
 #include "gbpa_dispatch.cuh"
 #include <algorithm>
+#include <type_traits>
 
 namespace gbpa
 {
@@ -33,6 +34,39 @@ static const void *mass_kernel_for(int D, int Q)
    return (const void *)mass_apply_kernel<AR, 0, 0, GATHER, GEN, GEN>;
 }
 
+template <typename AR>
+static const void *diffusion_3d_kernel_for(int D, int Q)
+{
+#define GBPA_CASE(d, q) \
+   if (D == d && Q == q) { return (const void *)diffusion_apply_3d_kernel<AR, d, q>; }
+   GBPA_DQ3_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return nullptr;
+}
+
+// Gather-fused diffusion apply in the 3D layout; GBPA_ERR_UNSUPPORTED when no
+// compile-time kernel exists for (D, Q).
+template <typename AR>
+int launch_diffusion_3d_ar(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
+                           const typename AR::In *B, const typename AR::In *G,
+                           const typename AR::Qd *qd, const typename AR::In *x,
+                           const int *gather_map, const unsigned char *ess_mask,
+                           typename AR::In *y, int mode, const int *skip, int nbz)
+{
+   const void *k = diffusion_3d_kernel_for<AR>(D, Q);
+   if (!k || !gather_map) { return GBPA_ERR_UNSUPPORTED; }
+   const int q3 = Q * Q * Q;
+   // blockDim.z = Q * nbz is limited to 64, the block to the kernel's thread limit
+   nbz = std::max(1, std::min(nbz, std::min(max_threads_for(k) / q3, 64 / Q)));
+   if (q3 > max_threads_for(k)) { return GBPA_ERR_UNSUPPORTED; }
+   const int b1 = std::max(D * D * D, 3 * D * Q * Q), b2 = std::max(2 * D * D * Q, 3 * q3);
+   const size_t smem = sizeof(typename AR::V) * (2 * Q * D + (size_t)nbz * (b1 + b2));
+   void *args[] = {&ne, &symm, (void *)&B, (void *)&G, (void *)&qd, (void *)&x,
+                   (void *)&gather_map, (void *)&ess_mask, &y, &mode, (void *)&skip};
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, Q * nbz), args, smem,
+                         "diffusion_apply_3d");
+}
+
 template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
 int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
                         const typename AR::In *B, const typename AR::In *G,
@@ -42,6 +76,27 @@ int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
 {
    if (ne == 0) { return GBPA_SUCCESS; }
    if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
+   int nbz3 = 0;
+   if (gather_map && apply_layout(GBPA_DIFFUSION, prec, D, Q, &nbz3) == GBPA_LAYOUT_3D)
+   {
+      int rc;
+      if constexpr (std::is_same<AR, ArF64>::value)
+      {
+         rc = launch_diffusion_3d_f64(ctx, ne, symm, D, Q, B, G, qd, x, gather_map, ess_mask, y, accumulate,
+                                      skip, nbz3);
+      }
+      else if constexpr (std::is_same<AR, ArF32>::value)
+      {
+         rc = launch_diffusion_3d_f32(ctx, ne, symm, D, Q, B, G, qd, x, gather_map, ess_mask, y, accumulate,
+                                      skip, nbz3);
+      }
+      else
+      {
+         rc = launch_diffusion_3d_x2(ctx, ne, symm, D, Q, B, G, qd, x, gather_map, ess_mask, y, accumulate,
+                                     skip, nbz3);
+      }
+      if (rc != GBPA_ERR_UNSUPPORTED) { return rc; }
+   }
    const void *k = nullptr;
    if (gather_map) { k = diffusion_kernel_for<AR, true, GEN>(D, Q); }
    else if constexpr (PLAIN) { k = diffusion_kernel_for<AR, false, GEN>(D, Q); }

@@ -1,0 +1,14 @@
+// Double-float diffusion apply in the 3D thread layout (its own translation unit so
+// that it compiles in parallel with the 2D-slab kernels).
+#include "gbpa_apply_launch.cuh"
+
+namespace gbpa
+{
+int launch_diffusion_3d_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
+                           const double *G, const float2 *qd, const double *x, const int *gather_map,
+                           const unsigned char *ess_mask, double *y, int mode, const int *skip, int nbz)
+{
+   return launch_diffusion_3d_ar<ArX2>(ctx, ne, symm, D, Q, B, G, qd, x, gather_map, ess_mask, y, mode, skip,
+                                       nbz);
+}
+} // namespace gbpa

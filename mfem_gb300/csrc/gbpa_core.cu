@@ -716,3 +716,38 @@ extern "C" int gbpa_get_elements_per_block(int kind, int precision, int d1d, int
    if (kind < 0 || kind > 1 || precision < 0 || precision > 2) { return GBPA_ERR_INVALID_ARGUMENT; }
    return elements_per_block(kind, precision, d1d, q1d);
 }
+
+// ------------------------------------------------------ apply layout table
+static std::unordered_map<int, int> g_layout;   // key -> nbz of the 3D layout
+
+int gbpa::apply_layout(int kind, int precision, int D, int Q, int *nbz)
+{
+   std::lock_guard<std::mutex> lock(g_nbz_mu);
+   auto it = g_layout.find(nbz_key(kind, precision, D, Q));
+   if (it == g_layout.end()) { return GBPA_LAYOUT_SLAB2D; }
+   if (nbz) { *nbz = it->second; }
+   return GBPA_LAYOUT_3D;
+}
+
+extern "C" int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, int layout, int nbz)
+{
+   if (kind != GBPA_DIFFUSION || precision < 0 || precision > 2 || d1d < 1 || q1d < 1 ||
+       d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || (layout != GBPA_LAYOUT_SLAB2D && layout != GBPA_LAYOUT_3D) ||
+       (layout == GBPA_LAYOUT_3D && (nbz < 1 || nbz * q1d * q1d * q1d > 1024 || nbz * q1d > 64)))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   std::lock_guard<std::mutex> lock(g_nbz_mu);
+   if (layout == GBPA_LAYOUT_SLAB2D) { g_layout.erase(nbz_key(kind, precision, d1d, q1d)); }
+   else { g_layout[nbz_key(kind, precision, d1d, q1d)] = nbz; }
+   return GBPA_SUCCESS;
+}
+
+extern "C" int gbpa_get_apply_layout(int kind, int precision, int d1d, int q1d, int *nbz)
+{
+   if (kind < 0 || kind > 1 || precision < 0 || precision > 2) { return GBPA_ERR_INVALID_ARGUMENT; }
+   int n = 0;
+   const int layout = gbpa::apply_layout(kind, precision, d1d, q1d, &n);
+   if (nbz) { *nbz = layout == GBPA_LAYOUT_3D ? n : elements_per_block(kind, precision, d1d, q1d); }
+   return layout;
+}

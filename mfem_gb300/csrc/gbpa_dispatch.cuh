@@ -12,6 +12,10 @@
    X(2, 2) X(2, 3) X(3, 3) X(3, 4) X(4, 4) X(4, 5) X(5, 5) X(5, 6) X(6, 6)    \
    X(6, 7) X(7, 7) X(7, 8) X(8, 8) X(8, 9) X(9, 9) X(9, 10) X(4, 6) X(5, 8)
 
+// (D, Q) pairs with a compile-time 3D-layout diffusion kernel: all of the
+// above (Q^3 <= 1000 threads per element).
+#define GBPA_DQ3_LIST(X) GBPA_DQ_LIST(X)
+
 namespace gbpa
 {
 // Raise the dynamic shared-memory limit of a kernel once per size class.

@@ -129,6 +129,17 @@ int launch_mass_apply_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, c
                          const double *x, const int *gather_map, const unsigned char *ess_mask,
                          double *y, int accumulate, const int *skip = nullptr);
 int launch_split_x2(gbpa_ctx *ctx, int64_t n, const double *a, float2 *b);
+// Gather-fused diffusion apply in the 3D thread layout (one translation unit
+// per arithmetic); GBPA_ERR_UNSUPPORTED when (D, Q) has no 3D kernel.
+int launch_diffusion_3d_f64(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
+                            const double *G, const double *qd, const double *x, const int *gather_map,
+                            const unsigned char *ess_mask, double *y, int mode, const int *skip, int nbz);
+int launch_diffusion_3d_f32(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const float *B,
+                            const float *G, const float *qd, const float *x, const int *gather_map,
+                            const unsigned char *ess_mask, float *y, int mode, const int *skip, int nbz);
+int launch_diffusion_3d_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
+                           const double *G, const float2 *qd, const double *x, const int *gather_map,
+                           const unsigned char *ess_mask, double *y, int mode, const int *skip, int nbz);
 // FP64 E-vector mass apply (y += A_e x) where element e reads the qdata of
 // element e / qdiv.
 int launch_mass_apply_qdiv(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const double *qd,
@@ -153,6 +164,10 @@ int launch_masked_gather_map(gbpa_ctx *ctx, int64_t n, const int *gather_map,
 
 // nbz chosen for (kind, precision, D, Q): tuned table or default.
 int elements_per_block(int kind, int precision, int D, int Q);
+// Thread layout of the gather-fused apply for (kind, precision, D, Q):
+// GBPA_LAYOUT_SLAB2D (default) or GBPA_LAYOUT_3D, with *nbz the 3D kernel's
+// elements per block.
+int apply_layout(int kind, int precision, int D, int Q, int *nbz);
 
 // Deterministic two-level dot product into a device scalar (double).
 template <typename T>
