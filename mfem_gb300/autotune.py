@@ -134,6 +134,8 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
                 yE = torch.empty(fes.ne * D ** 3, dtype=dt, device="cuda")
                 best = (float("inf"), None)
                 res = {}
+                if kind == "diffusion":   # time the 2D slab even if a table selected the 3D layout
+                    lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 0, 0)
                 for nbz in candidates(kind, prec, D, Q):
                     lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, nbz)
                     ms = time_nbz(lib, op, x, yE, reps)

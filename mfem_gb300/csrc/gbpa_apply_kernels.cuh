@@ -664,7 +664,7 @@ template <int D, int Q>
 __host__ __device__ constexpr int diff3d_buf2() { return 2 * D * D * Q > 3 * Q * Q * Q ? 2 * D * D * Q : 3 * Q * Q * Q; }
 
 template <typename AR, int D, int Q>
-__global__ void diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ gB,
+__global__ void __launch_bounds__(1024, 2) diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ gB,
                                           const typename AR::In *__restrict__ gG,
                                           const typename AR::Qd *__restrict__ qd,
                                           const typename AR::In *__restrict__ x,
