@@ -663,25 +663,26 @@ __host__ __device__ constexpr int diff3d_buf1() { return D * D * D > 3 * D * Q *
 template <int D, int Q>
 __host__ __device__ constexpr int diff3d_buf2() { return 2 * D * D * Q > 3 * Q * Q * Q ? 2 * D * D * Q : 3 * Q * Q * Q; }
 
+// One block's share in the 3D layout: elements [e0, e0 + cnt) (cnt <=
+// blockDim.z / Q) of an operator; shared by the single-operator kernel and the
+// batched grouped apply.
 template <typename AR, int D, int Q>
-__global__ void __launch_bounds__(1024, 2) diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ gB,
-                                          const typename AR::In *__restrict__ gG,
-                                          const typename AR::Qd *__restrict__ qd,
-                                          const typename AR::In *__restrict__ x,
-                                          const int *__restrict__ gmap,
-                                          const unsigned char *__restrict__ mask,
-                                          typename AR::In *__restrict__ y, int mode,
-                                          const int *__restrict__ skip)
+__device__ __forceinline__ void diffusion_3d_block(long long e0, int cnt, int symm,
+                                                   const typename AR::In *__restrict__ gB,
+                                                   const typename AR::In *__restrict__ gG,
+                                                   const typename AR::Qd *__restrict__ qd,
+                                                   const typename AR::In *__restrict__ x,
+                                                   const int *__restrict__ gmap,
+                                                   const unsigned char *__restrict__ mask,
+                                                   typename AR::In *__restrict__ y, int mode)
 {
    using V = typename AR::V;
    constexpr int D3 = D * D * D, Q3 = Q * Q * Q, DQQ = D * Q * Q, DDQ = D * D * Q;
    constexpr int S1 = diff3d_buf1<D, Q>(), S2 = diff3d_buf2<D, Q>();
-   if (skip && *skip) { return; }
    const int tx = threadIdx.x, ty = threadIdx.y;
    const int tz = threadIdx.z % Q, ez = threadIdx.z / Q;
-   const int nbz = blockDim.z / Q;
-   const long long e = (long long)blockIdx.x * nbz + ez;
-   const bool active = e < ne;
+   const long long e = e0 + ez;
+   const bool active = ez < cnt;
    extern __shared__ __align__(16) unsigned char smem_raw[];
    V *sB = reinterpret_cast<V *>(smem_raw);   // [Q][D]
    V *sG = sB + Q * D;
@@ -828,6 +829,20 @@ __global__ void __launch_bounds__(1024, 2) diffusion_apply_3d_kernel(int ne, int
       const long long slot = e * D3 + tx + D * (ty + D * tz);
       store_result(y, slot, slot, AR::out(AR::fin(v)), mode, gmap, mask);
    }
+}
+
+template <typename AR, int D, int Q>
+__global__ void __launch_bounds__(1024, 2)
+diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ gB,
+                          const typename AR::In *__restrict__ gG, const typename AR::Qd *__restrict__ qd,
+                          const typename AR::In *__restrict__ x, const int *__restrict__ gmap,
+                          const unsigned char *__restrict__ mask, typename AR::In *__restrict__ y, int mode,
+                          const int *__restrict__ skip)
+{
+   if (skip && *skip) { return; }   // uniform per launch: solver finished
+   const int nbz = blockDim.z / Q;
+   const long long e0 = (long long)blockIdx.x * nbz;
+   diffusion_3d_block<AR, D, Q>(e0, (int)min((long long)nbz, ne - e0), symm, gB, gG, qd, x, gmap, mask, y, mode);
 }
 
 template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
