@@ -1,0 +1,77 @@
+"""Host-side checks of the autotuner's table and candidate sets, and of the
+bench's algorithmic work accounting (no GPU)."""
+import json
+import os
+
+import pytest
+
+from tests.conftest import REPO
+
+
+def tuning():
+    with open(os.path.join(REPO, "mfem_gb300", "tuning.json")) as f:
+        return json.load(f)
+
+
+def test_tuning_table_entries_are_launchable():
+    """Every 2D-slab entry fits a 1024-thread block with blockDim.z <= 64 and
+    the autotuner's shared-memory budget; every 3D-layout entry names a
+    diffusion order that has a compile-time 3D kernel and fits the 3D limits."""
+    from mfem_gb300 import autotune as at
+    t = tuning()
+    assert t["nbz"], "empty tuning table"
+    for k, nbz in t["nbz"].items():
+        kind, prec, D, Q = k.split(":")
+        D, Q = int(D), int(Q)
+        assert kind in at.KINDS and prec in at.PRECS
+        assert 1 <= nbz <= 64 and nbz * Q * Q <= 1024, k
+        assert nbz in at.candidates(kind, prec, D, Q), k
+    for k, nbz in t.get("layout3d", {}).items():
+        kind, prec, D, Q = k.split(":")
+        D, Q = int(D), int(Q)
+        assert kind == "diffusion" and (D, Q) in at.DQ3, k
+        assert nbz in at.candidates_3d(prec, D, Q), k
+        assert nbz * Q <= 64 and nbz * Q ** 3 <= 1024, k
+
+
+def test_3d_candidates_respect_block_limits():
+    from mfem_gb300 import autotune as at
+    for (D, Q) in sorted(at.DQ3):
+        for prec in at.PRECS:
+            c = at.candidates_3d(prec, D, Q)
+            assert c and c[0] == 1
+            assert all(n * Q <= 64 and n * Q ** 3 <= 1024 for n in c)
+
+
+def test_3d_kernel_list_matches_library_dispatch():
+    """The tuner's DQ3 set is the library's GBPA_DQ3_LIST (= GBPA_DQ_LIST)."""
+    import re
+    from mfem_gb300 import autotune as at
+    src = open(os.path.join(REPO, "mfem_gb300", "csrc", "gbpa_dispatch.cuh")).read()
+    body = src[src.index("#define GBPA_DQ_LIST"):src.index("#define GBPA_DQ3_LIST")]
+    pairs = {(int(a), int(b)) for a, b in re.findall(r"X\((\d+),\s*(\d+)\)", body)}
+    assert "GBPA_DQ3_LIST(X) GBPA_DQ_LIST(X)" in src
+    assert pairs == at.DQ3
+
+
+@pytest.mark.parametrize("p", range(1, 9))
+def test_element_flops_against_the_closed_form(p):
+    """The bench's diffusion flop count is the kernel's contraction sequence:
+    the reference's formula 2[2D^3Q + 3D^2Q^2 + 3DQ^3 + 9Q^3 + 3DQ^3 + 3D^2Q^2
+    + 3D^3Q] minus the D^3 Q multiply-adds the fused backward x stage saves."""
+    import bench
+    D, Q = p + 1, p + 2
+    ref = 2 * (2 * D ** 3 * Q + 3 * D ** 2 * Q ** 2 + 3 * D * Q ** 3 + 9 * Q ** 3 + 3 * D * Q ** 3
+               + 3 * D ** 2 * Q ** 2 + 3 * D ** 3 * Q)
+    assert bench.element_flops(D, Q, "diffusion") == ref - 2 * D ** 3 * Q
+    mass = 2 * 2 * (D ** 3 * Q + D ** 2 * Q ** 2 + D * Q ** 3) + Q ** 3
+    assert bench.element_flops(D, Q, "mass") == mass
+
+
+def test_algorithmic_bytes_at_the_headline_size():
+    """p=4, n=77: the element kernel's algorithmic bytes quoted in the docs."""
+    import bench
+    ne, D, Q = 77 ** 3, 5, 6
+    ndofs = (4 * 77 + 1) ** 3
+    b = bench.algorithmic_bytes(ne, ndofs, D, Q, 8, "diffusion", element_only=True)
+    assert abs(b / 1e9 - 5.654) < 0.002
