@@ -546,8 +546,8 @@ int gbpa_pcg_solve_mg(gbpa_operator_t A, gbpa_multigrid_t M, const double *b,
 int gbpa_set_elements_per_block(int kind, int precision, int d1d, int q1d,
                                 int nbz);
 int gbpa_get_elements_per_block(int kind, int precision, int d1d, int q1d);
-/* Thread layout of the gather-fused diffusion apply (the operator path) for
- * (precision, d1d, q1d): GBPA_LAYOUT_SLAB2D (default; block (Q, Q, nbz), one
+/* Thread layout of the gather-fused diffusion or mass apply (the operator
+ * path) for (kind, precision, d1d, q1d): GBPA_LAYOUT_SLAB2D (default; block (Q, Q, nbz), one
  * thread per (qx, qy) column, z in registers) or GBPA_LAYOUT_3D (block
  * (Q, Q, Q*nbz), one thread per quadrature point, every contraction through
  * shared memory; compile-time kernels for the (D, Q) pairs the 2D slab

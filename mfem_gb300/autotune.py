@@ -2,7 +2,7 @@
 
 For each (integrator, arithmetic, order p) the 2D-slab apply kernel runs with
 block (Q, Q, nbz); nbz -- elements per block -- sets the block size, the
-shared memory per block and therefore the occupancy. For diffusion the 3D
+shared memory per block and therefore the occupancy. The 3D
 layout (block (Q, Q, Q*nbz), one thread per quadrature point) is a
 second candidate. The tuner times the gather-fused element kernel on a
 synthetic jittered mesh for every feasible (layout, nbz) and keeps the
@@ -45,7 +45,7 @@ DQ3 = {(2, 2), (2, 3), (3, 3), (3, 4), (4, 4), (4, 5), (5, 5), (5, 6), (6, 6), (
 
 
 def apply_layouts(lib, layout3d):
-    """Install the 3D-layout entries {key: nbz} (diffusion only)."""
+    """Install the 3D-layout entries {key: nbz}."""
     n = 0
     for k, nbz in layout3d.items():
         kind, prec, D, Q = k.split(":")
@@ -62,9 +62,12 @@ def load_default(lib):
     return 0
 
 
-def candidates_3d(prec, D, Q):
+def candidates_3d(prec, D, Q, kind="diffusion"):
     w = 4 if prec == "f32" else 8
-    per = max(D ** 3, 3 * D * Q * Q) + max(2 * D * D * Q, 3 * Q ** 3)
+    if kind == "diffusion":
+        per = max(D ** 3, 3 * D * Q * Q) + max(2 * D * D * Q, 3 * Q ** 3)
+    else:
+        per = max(D ** 3, D * Q * Q) + max(D * D * Q, Q ** 3)
     out = []
     for nbz in range(1, 65):
         if nbz * Q ** 3 > 1024 or nbz * Q > 64 or w * (2 * Q * D + nbz * per) > 200 * 1024:
@@ -134,8 +137,8 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
                 yE = torch.empty(fes.ne * D ** 3, dtype=dt, device="cuda")
                 best = (float("inf"), None)
                 res = {}
-                if kind == "diffusion":   # time the 2D slab even if a table selected the 3D layout
-                    lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 0, 0)
+                # time the 2D slab even if a table selected the 3D layout
+                lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 0, 0)
                 for nbz in candidates(kind, prec, D, Q):
                     lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, nbz)
                     ms = time_nbz(lib, op, x, yE, reps)
@@ -143,8 +146,8 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
                     best = min(best, (ms, nbz))
                 lib.gbpa_set_elements_per_block(KINDS[kind], pid, D, Q, 0)
                 res3, best3 = {}, (float("inf"), None)
-                if kind == "diffusion" and (D, Q) in DQ3:
-                    for nbz in candidates_3d(prec, D, Q):
+                if (D, Q) in DQ3:
+                    for nbz in candidates_3d(prec, D, Q, kind):
                         lib.gbpa_set_apply_layout(KINDS[kind], pid, D, Q, 1, nbz)
                         ms = time_nbz(lib, op, x, yE, reps)
                         res3[nbz] = ms

@@ -845,6 +845,98 @@ diffusion_apply_3d_kernel(int ne, int symm, const typename AR::In *__restrict__ 
    diffusion_3d_block<AR, D, Q>(e0, (int)min((long long)nbz, ne - e0), symm, gB, gG, qd, x, gmap, mask, y, mode);
 }
 
+// Mass apply in the 3D layout (block (Q, Q, Q * nbz), one thread per
+// quadrature point, gather fused), the 2D slab's multiply-adds in the same
+// order. Per element: buf1 X (D^3) -> BBX [dz][qy][qx] -> T [dz][qy][qx];
+// buf2 BX [dz][dy][qx] -> W [qz][qy][qx] -> U [dz][dy][qx].
+template <int D, int Q>
+__host__ __device__ constexpr int mass3d_buf1() { return D * D * D > D * Q * Q ? D * D * D : D * Q * Q; }
+template <int D, int Q>
+__host__ __device__ constexpr int mass3d_buf2() { return D * D * Q > Q * Q * Q ? D * D * Q : Q * Q * Q; }
+
+template <typename AR, int D, int Q>
+__global__ void __launch_bounds__(1024, 2)
+mass_apply_3d_kernel(int ne, const typename AR::In *__restrict__ gB, const typename AR::Qd *__restrict__ qd,
+                     const typename AR::In *__restrict__ x, const int *__restrict__ gmap,
+                     const unsigned char *__restrict__ mask, typename AR::In *__restrict__ y, int mode,
+                     const int *__restrict__ skip)
+{
+   using V = typename AR::V;
+   constexpr int D3 = D * D * D, Q3 = Q * Q * Q;
+   constexpr int S1 = mass3d_buf1<D, Q>(), S2 = mass3d_buf2<D, Q>();
+   if (skip && *skip) { return; }
+   const int tx = threadIdx.x, ty = threadIdx.y;
+   const int tz = threadIdx.z % Q, ez = threadIdx.z / Q;
+   const int nbz = blockDim.z / Q;
+   const long long e = (long long)blockIdx.x * nbz + ez;
+   const bool active = e < ne;
+   extern __shared__ __align__(16) unsigned char smem_raw[];
+   V *sB = reinterpret_cast<V *>(smem_raw);   // [Q][D]
+   V *buf1 = sB + Q * D + (size_t)ez * (S1 + S2);
+   V *buf2 = buf1 + S1;
+   const int tid = tx + Q * (ty + Q * threadIdx.z);
+   for (int i = tid; i < Q * D; i += Q * Q * blockDim.z) { sB[(i % Q) * D + i / Q] = AR::in(gB[i]); }
+   const int t = tx + Q * (ty + Q * tz);
+   if (t < D3) { buf1[t] = active ? gather_value<AR>(x, gmap, mask, e * D3 + t) : AR::zero(); }
+   __syncthreads();
+   // x, thread (qx, dy, dz)
+   if (ty < D && tz < D)
+   {
+      V u = AR::zero();
+      const V *xr = buf1 + D * (ty + D * tz);
+#pragma unroll
+      for (int dx = 0; dx < D; ++dx) { AR::mac(u, xr[dx], sB[tx * D + dx]); }
+      buf2[(tz * D + ty) * Q + tx] = AR::fin(u);
+   }
+   __syncthreads();
+   // y, thread (qx, qy, dz)
+   if (tz < D)
+   {
+      V a = AR::zero();
+#pragma unroll
+      for (int dy = 0; dy < D; ++dy) { AR::mac(a, buf2[(tz * D + dy) * Q + tx], sB[ty * D + dy]); }
+      buf1[(tz * Q + ty) * Q + tx] = AR::fin(a);
+   }
+   __syncthreads();
+   // z and the pointwise qdata product, thread (qx, qy, qz)
+   {
+      V v = AR::zero();
+#pragma unroll
+      for (int dz = 0; dz < D; ++dz) { AR::mac(v, sB[tz * D + dz], buf1[(dz * Q + ty) * Q + tx]); }
+      V w = AR::zero();
+      if (active) { AR::mac(w, AR::fin(v), AR::ldq(qd + e * Q3 + t)); }
+      buf2[(tz * Q + ty) * Q + tx] = AR::fin(w);
+   }
+   __syncthreads();
+   // backward z, thread (qx, qy, dz)
+   if (tz < D)
+   {
+      V o = AR::zero();
+#pragma unroll
+      for (int qz = 0; qz < Q; ++qz) { AR::mac(o, sB[qz * D + tz], buf2[(qz * Q + ty) * Q + tx]); }
+      buf1[(tz * Q + ty) * Q + tx] = AR::fin(o);
+   }
+   __syncthreads();
+   // backward y, thread (qx, dy, dz)
+   if (ty < D && tz < D)
+   {
+      V a = AR::zero();
+#pragma unroll
+      for (int qy = 0; qy < Q; ++qy) { AR::mac(a, buf1[(tz * Q + qy) * Q + tx], sB[qy * D + ty]); }
+      buf2[(tz * D + ty) * Q + tx] = AR::fin(a);
+   }
+   __syncthreads();
+   // backward x, thread (dx, dy, dz)
+   if (active && tx < D && ty < D && tz < D)
+   {
+      V v = AR::zero();
+#pragma unroll
+      for (int qx = 0; qx < Q; ++qx) { AR::mac(v, sB[qx * D + tx], buf2[(tz * D + ty) * Q + qx]); }
+      const long long slot = e * D3 + tx + D * (ty + D * tz);
+      store_result(y, slot, slot, AR::out(AR::fin(v)), mode, gmap, mask);
+   }
+}
+
 template <typename AR, int TD, int TQ, bool GATHER, int MAXD = GBPA_MAX_1D, int MAXQ = GBPA_MAX_1D>
 __global__ void mass_apply_kernel(int ne, int d1d, int q1d,
                                   const typename AR::In *__restrict__ gB,

@@ -67,6 +67,35 @@ int launch_diffusion_3d_ar(gbpa_ctx *ctx, int ne, int symm, int D, int Q,
                          "diffusion_apply_3d");
 }
 
+template <typename AR>
+static const void *mass_3d_kernel_for(int D, int Q)
+{
+#define GBPA_CASE(d, q) \
+   if (D == d && Q == q) { return (const void *)mass_apply_3d_kernel<AR, d, q>; }
+   GBPA_DQ3_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return nullptr;
+}
+
+// Gather-fused mass apply in the 3D layout; GBPA_ERR_UNSUPPORTED when (D, Q)
+// has no 3D kernel.
+template <typename AR>
+int launch_mass_3d_ar(gbpa_ctx *ctx, int ne, int D, int Q, const typename AR::In *B,
+                      const typename AR::Qd *qd, const typename AR::In *x, const int *gather_map,
+                      const unsigned char *ess_mask, typename AR::In *y, int mode, const int *skip, int nbz)
+{
+   const void *k = mass_3d_kernel_for<AR>(D, Q);
+   if (!k || !gather_map) { return GBPA_ERR_UNSUPPORTED; }
+   const int q3 = Q * Q * Q;
+   if (q3 > max_threads_for(k)) { return GBPA_ERR_UNSUPPORTED; }
+   nbz = std::max(1, std::min(nbz, std::min(max_threads_for(k) / q3, 64 / Q)));
+   const int b1 = std::max(D * D * D, D * Q * Q), b2 = std::max(D * D * Q, q3);
+   const size_t smem = sizeof(typename AR::V) * (Q * D + (size_t)nbz * (b1 + b2));
+   void *args[] = {&ne, (void *)&B, (void *)&qd, (void *)&x, (void *)&gather_map, (void *)&ess_mask, &y,
+                   &mode, (void *)&skip};
+   return launch_generic(ctx, k, dim3((ne + nbz - 1) / nbz), dim3(Q, Q, Q * nbz), args, smem, "mass_apply_3d");
+}
+
 template <typename AR, int GEN = GBPA_MAX_1D, bool PLAIN = true>
 int launch_diffusion_ar(gbpa_ctx *ctx, int prec, int ne, int symm, int D, int Q,
                         const typename AR::In *B, const typename AR::In *G,
@@ -179,6 +208,24 @@ int launch_mass_ar(gbpa_ctx *ctx, int prec, int ne, int D, int Q,
 {
    if (ne == 0) { return GBPA_SUCCESS; }
    if (D > GEN || Q > GEN) { return GBPA_ERR_UNSUPPORTED; }
+   int nbz3 = 0;
+   if (gather_map && qdiv == 1 && apply_layout(GBPA_MASS, prec, D, Q, &nbz3) == GBPA_LAYOUT_3D)
+   {
+      int rc;
+      if constexpr (std::is_same<AR, ArF64>::value)
+      {
+         rc = launch_mass_3d_f64(ctx, ne, D, Q, B, qd, x, gather_map, ess_mask, y, accumulate, skip, nbz3);
+      }
+      else if constexpr (std::is_same<AR, ArF32>::value)
+      {
+         rc = launch_mass_3d_f32(ctx, ne, D, Q, B, qd, x, gather_map, ess_mask, y, accumulate, skip, nbz3);
+      }
+      else
+      {
+         rc = launch_mass_3d_x2(ctx, ne, D, Q, B, qd, x, gather_map, ess_mask, y, accumulate, skip, nbz3);
+      }
+      if (rc != GBPA_ERR_UNSUPPORTED) { return rc; }
+   }
    const void *k = nullptr;
    if (gather_map) { k = mass_kernel_for<AR, true, GEN>(D, Q); }
    else if constexpr (PLAIN) { k = mass_kernel_for<AR, false, GEN>(D, Q); }

@@ -731,7 +731,7 @@ int gbpa::apply_layout(int kind, int precision, int D, int Q, int *nbz)
 
 extern "C" int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, int layout, int nbz)
 {
-   if (kind != GBPA_DIFFUSION || precision < 0 || precision > 2 || d1d < 1 || q1d < 1 ||
+   if (kind < 0 || kind > 1 || precision < 0 || precision > 2 || d1d < 1 || q1d < 1 ||
        d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || (layout != GBPA_LAYOUT_SLAB2D && layout != GBPA_LAYOUT_3D) ||
        (layout == GBPA_LAYOUT_3D && (nbz < 1 || nbz * q1d * q1d * q1d > 1024 || nbz * q1d > 64)))
    {

@@ -140,6 +140,16 @@ int launch_diffusion_3d_f32(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const
 int launch_diffusion_3d_x2(gbpa_ctx *ctx, int ne, int symm, int D, int Q, const double *B,
                            const double *G, const float2 *qd, const double *x, const int *gather_map,
                            const unsigned char *ess_mask, double *y, int mode, const int *skip, int nbz);
+// The same for the mass apply.
+int launch_mass_3d_f64(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const double *qd, const double *x,
+                       const int *gather_map, const unsigned char *ess_mask, double *y, int mode,
+                       const int *skip, int nbz);
+int launch_mass_3d_f32(gbpa_ctx *ctx, int ne, int D, int Q, const float *B, const float *qd, const float *x,
+                       const int *gather_map, const unsigned char *ess_mask, float *y, int mode,
+                       const int *skip, int nbz);
+int launch_mass_3d_x2(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const float2 *qd, const double *x,
+                      const int *gather_map, const unsigned char *ess_mask, double *y, int mode,
+                      const int *skip, int nbz);
 // FP64 E-vector mass apply (y += A_e x) where element e reads the qdata of
 // element e / qdiv.
 int launch_mass_apply_qdiv(gbpa_ctx *ctx, int ne, int D, int Q, const double *B, const double *qd,

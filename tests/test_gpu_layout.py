@@ -83,10 +83,39 @@ def test_3d_layout_nbz_sweep_and_ragged_last_block():
         set_layout(d, 0, D, Q, 0, 0)
 
 
+@pytest.mark.parametrize("p", [1, 3, 5, 8])
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_3d_layout_mass_matches_slab(p, precision):
+    from mfem_gb300 import fem
+    from mfem_gb300.pa import FiniteElementSpace, MassIntegrator, PAOperator
+    from tests.gpu_util import dev
+    d = dev()
+    mesh = fem.CartesianMesh(4, jitter=0.1, seed=9)
+    fes = FiniteElementSpace(mesh, p)
+    integ = MassIntegrator("kappa")
+    integ.AssemblePA(fes, modes=fem.kappa_modes(3))
+    A = PAOperator(1, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=fes.GetBoundaryTrueDofs(),
+                   precision=precision)
+    D, Q = integ.D, integ.Q
+    dt = torch.float32 if precision == 1 else torch.float64
+    gen = torch.Generator(device="cuda").manual_seed(62)
+    x = (torch.rand(fes.ndofs, dtype=torch.float64, device="cuda", generator=gen) - 0.5).to(dt)
+    y2, y3 = torch.empty_like(x), torch.full_like(x, float("nan"))
+    A.Mult(x, y2)
+    nbz = max(1, min(4, 1024 // Q ** 3, 64 // Q))
+    assert d.lib.gbpa_set_apply_layout(1, precision, D, Q, 1, nbz) == 0
+    try:
+        A.Mult(x, y3)
+        torch.cuda.synchronize()
+    finally:
+        d.lib.gbpa_set_apply_layout(1, precision, D, Q, 0, 0)
+    assert torch.equal(y3, y2)
+
+
 def test_layout_arguments_validated():
     from tests.gpu_util import dev
     d = dev()
-    assert d.lib.gbpa_set_apply_layout(1, 0, 4, 5, 1, 1) == -1      # mass: 2D slab only
+    assert d.lib.gbpa_set_apply_layout(2, 0, 4, 5, 1, 1) == -1      # unknown kind
     assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 2, 1) == -1      # unknown layout
     assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 1, 0) == -1      # nbz < 1
     assert d.lib.gbpa_set_apply_layout(0, 0, 9, 10, 1, 2) == -1     # 2000 threads

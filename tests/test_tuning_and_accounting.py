@@ -29,8 +29,8 @@ def test_tuning_table_entries_are_launchable():
     for k, nbz in t.get("layout3d", {}).items():
         kind, prec, D, Q = k.split(":")
         D, Q = int(D), int(Q)
-        assert kind == "diffusion" and (D, Q) in at.DQ3, k
-        assert nbz in at.candidates_3d(prec, D, Q), k
+        assert (D, Q) in at.DQ3, k
+        assert nbz in at.candidates_3d(prec, D, Q, kind), k
         assert nbz * Q <= 64 and nbz * Q ** 3 <= 1024, k
 
 
@@ -38,9 +38,10 @@ def test_3d_candidates_respect_block_limits():
     from mfem_gb300 import autotune as at
     for (D, Q) in sorted(at.DQ3):
         for prec in at.PRECS:
-            c = at.candidates_3d(prec, D, Q)
-            assert c and c[0] == 1
-            assert all(n * Q <= 64 and n * Q ** 3 <= 1024 for n in c)
+            for kind in at.KINDS:
+                c = at.candidates_3d(prec, D, Q, kind)
+                assert c and c[0] == 1
+                assert all(n * Q <= 64 and n * Q ** 3 <= 1024 for n in c)
 
 
 def test_3d_kernel_list_matches_library_dispatch():
