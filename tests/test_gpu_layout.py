@@ -28,8 +28,15 @@ def op(p, precision, ess, scatter=0, n=4):
     return fes, integ, A
 
 
-def set_layout(d, precision, D, Q, layout, nbz):
-    return d.lib.gbpa_set_apply_layout(0, precision, D, Q, layout, nbz)
+def set_layout(d, precision, D, Q, layout, nbz, kind=0):
+    return d.lib.gbpa_set_apply_layout(kind, precision, D, Q, layout, nbz)
+
+
+def saved_layout(d, precision, D, Q, kind=0):
+    """The installed (layout, nbz) of an order, to put back after a test."""
+    n = ctypes.c_int(0)
+    layout = d.lib.gbpa_get_apply_layout(kind, precision, D, Q, ctypes.byref(n))
+    return layout, (n.value if layout == 1 else 0)
 
 
 @pytest.mark.parametrize("p", DQ3_P)
@@ -44,16 +51,18 @@ def test_3d_layout_matches_slab(p, precision, ess, scatter):
     gen = torch.Generator(device="cuda").manual_seed(61)
     x = (torch.rand(fes.ndofs, dtype=torch.float64, device="cuda", generator=gen) - 0.5).to(dt)
     y2, y3 = torch.empty_like(x), torch.full_like(x, float("nan"))
-    A.Mult(x, y2)
     nbz = max(1, min(4, 1024 // Q ** 3))
-    assert set_layout(d, precision, D, Q, 1, nbz) == 0
+    before = saved_layout(d, precision, D, Q)
+    assert set_layout(d, precision, D, Q, 0, 0) == 0
     try:
+        A.Mult(x, y2)
+        assert set_layout(d, precision, D, Q, 1, nbz) == 0
         n = ctypes.c_int(0)
         assert d.lib.gbpa_get_apply_layout(0, precision, D, Q, ctypes.byref(n)) == 1 and n.value == nbz
         A.Mult(x, y3)
         torch.cuda.synchronize()
     finally:
-        set_layout(d, precision, D, Q, 0, 0)
+        set_layout(d, precision, D, Q, *before)
     if scatter == 0:
         # same multiply-adds in the same order (explicit FMAs): bit-identical
         assert torch.equal(y3, y2)
@@ -71,8 +80,10 @@ def test_3d_layout_nbz_sweep_and_ragged_last_block():
     D, Q = integ.D, integ.Q
     x = torch.rand(fes.ndofs, dtype=torch.float64, device="cuda")
     ref = torch.empty_like(x)
-    A.Mult(x, ref)
+    before = saved_layout(d, 0, D, Q)
     try:
+        set_layout(d, 0, D, Q, 0, 0)
+        A.Mult(x, ref)
         for nbz in (1, 2, 3, 7, 64 // Q):
             assert set_layout(d, 0, D, Q, 1, nbz) == 0
             y = torch.full_like(x, float("nan"))
@@ -80,7 +91,7 @@ def test_3d_layout_nbz_sweep_and_ragged_last_block():
             torch.cuda.synchronize()
             assert float(torch.linalg.norm(y - ref) / torch.linalg.norm(ref)) < 1e-13, nbz
     finally:
-        set_layout(d, 0, D, Q, 0, 0)
+        set_layout(d, 0, D, Q, *before)
 
 
 @pytest.mark.parametrize("p", [1, 3, 5, 8])
@@ -101,14 +112,16 @@ def test_3d_layout_mass_matches_slab(p, precision):
     gen = torch.Generator(device="cuda").manual_seed(62)
     x = (torch.rand(fes.ndofs, dtype=torch.float64, device="cuda", generator=gen) - 0.5).to(dt)
     y2, y3 = torch.empty_like(x), torch.full_like(x, float("nan"))
-    A.Mult(x, y2)
     nbz = max(1, min(4, 1024 // Q ** 3, 64 // Q))
-    assert d.lib.gbpa_set_apply_layout(1, precision, D, Q, 1, nbz) == 0
+    before = saved_layout(d, precision, D, Q, kind=1)
     try:
+        assert set_layout(d, precision, D, Q, 0, 0, kind=1) == 0
+        A.Mult(x, y2)
+        assert set_layout(d, precision, D, Q, 1, nbz, kind=1) == 0
         A.Mult(x, y3)
         torch.cuda.synchronize()
     finally:
-        d.lib.gbpa_set_apply_layout(1, precision, D, Q, 0, 0)
+        set_layout(d, precision, D, Q, *before, kind=1)
     assert torch.equal(y3, y2)
 
 
