@@ -54,12 +54,20 @@ def apply_layouts(lib, layout3d):
     return n
 
 
-def load_default(lib):
-    if os.path.exists(TUNING):
-        with open(TUNING) as f:
+def load_default(lib, path=TUNING):
+    """Install a saved table; a missing, unreadable or malformed file leaves the
+    library's defaults in place (with a warning), and entries the library
+    rejects are skipped. Returns the number of entries installed."""
+    if not os.path.exists(path):
+        return 0
+    try:
+        with open(path) as f:
             t = json.load(f)
-        return apply_table(lib, t.get("nbz", {})) + apply_layouts(lib, t.get("layout3d", {}))
-    return 0
+        return apply_table(lib, dict(t.get("nbz", {}))) + apply_layouts(lib, dict(t.get("layout3d", {})))
+    except (OSError, ValueError, TypeError, AttributeError, KeyError) as e:
+        import warnings
+        warnings.warn(f"tuning table {path} not applied ({type(e).__name__}: {e}); using the defaults")
+        return 0
 
 
 def candidates_3d(prec, D, Q, kind="diffusion"):

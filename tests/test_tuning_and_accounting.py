@@ -76,3 +76,48 @@ def test_algorithmic_bytes_at_the_headline_size():
     ndofs = (4 * 77 + 1) ** 3
     b = bench.algorithmic_bytes(ne, ndofs, D, Q, 8, "diffusion", element_only=True)
     assert abs(b / 1e9 - 5.654) < 0.002
+
+
+class _FakeLib:
+    """Records the tuning calls; rejects what the library would reject."""
+
+    def __init__(self):
+        self.nbz, self.layout = {}, {}
+
+    def gbpa_set_elements_per_block(self, kind, prec, D, Q, nbz):
+        if nbz < 0 or nbz * Q * Q > 1024:
+            return -1
+        self.nbz[(kind, prec, D, Q)] = nbz
+        return 0
+
+    def gbpa_set_apply_layout(self, kind, prec, D, Q, layout, nbz):
+        if nbz < 1 or nbz * Q > 64 or nbz * Q ** 3 > 1024:
+            return -1
+        self.layout[(kind, prec, D, Q)] = (layout, nbz)
+        return 0
+
+
+def test_load_default_installs_the_committed_table():
+    from mfem_gb300 import autotune as at
+    lib = _FakeLib()
+    t = tuning()
+    n = at.load_default(lib)
+    assert n == len(t["nbz"]) + len(t.get("layout3d", {}))
+    assert len(lib.layout) == len(t.get("layout3d", {}))
+
+
+def test_load_default_tolerates_bad_files(tmp_path):
+    from mfem_gb300 import autotune as at
+    lib = _FakeLib()
+    assert at.load_default(lib, str(tmp_path / "absent.json")) == 0
+    bad = tmp_path / "bad.json"
+    bad.write_text("{not json")
+    with pytest.warns(UserWarning):
+        assert at.load_default(lib, str(bad)) == 0
+    odd = tmp_path / "odd.json"
+    odd.write_text(json.dumps({"nbz": {"diffusion:f64:5:6": 7, "diffusion:f64:5:6:x": 1}}))
+    with pytest.warns(UserWarning):
+        at.load_default(lib, str(odd))
+    rejected = tmp_path / "rejected.json"
+    rejected.write_text(json.dumps({"nbz": {"diffusion:f64:5:6": 500}, "layout3d": {"diffusion:f64:9:10": 2}}))
+    assert at.load_default(lib, str(rejected)) == 0   # both entries refused by the library, none installed
