@@ -372,9 +372,14 @@ void or_diffusion_setup3d(int ne, int q1d, int coeff_dim, const double *W,
       }
 }
 
-void or_diffusion_apply3d(int ne, int symm, int d1d, int q1d, const double *B,
-                          const double *G, const double *Dq, const double *X,
-                          double *Y)
+/* The body is inlined into size-specialised wrappers below: with D and Q
+ * literal constants the compiler unrolls the contractions, as the
+ * reference's compile-time kernel instances do on the CPU
+ * (fem/integ/bilininteg_diffusion_kernels.cpp:64-83). The arithmetic and its
+ * order are the same for every instance. */
+static inline __attribute__((always_inline)) void
+diff_apply_body(int ne, int symm, int d1d, int q1d, const double *B, const double *G,
+                const double *Dq, const double *X, double *Y)
 {
    const int D = d1d, Q = q1d, Q3 = Q * Q * Q, D3 = D * D * D, S = symm ? 6 : 9;
 #pragma omp parallel for schedule(static)
@@ -494,6 +499,19 @@ void or_diffusion_apply3d(int ne, int symm, int d1d, int q1d, const double *B,
    }
 }
 
+
+#define OR_DIFF_CASE(d, q) \
+   if (d1d == d && q1d == q) { diff_apply_body(ne, symm, d, q, B, G, Dq, X, Y); return; }
+
+void or_diffusion_apply3d(int ne, int symm, int d1d, int q1d, const double *B,
+                          const double *G, const double *Dq, const double *X,
+                          double *Y)
+{
+   OR_DIFF_CASE(2, 3) OR_DIFF_CASE(3, 4) OR_DIFF_CASE(4, 5) OR_DIFF_CASE(5, 6)
+   OR_DIFF_CASE(6, 7) OR_DIFF_CASE(7, 8) OR_DIFF_CASE(8, 9) OR_DIFF_CASE(9, 10)
+   diff_apply_body(ne, symm, d1d, q1d, B, G, Dq, X, Y);
+}
+#undef OR_DIFF_CASE
 void or_diffusion_diagonal3d(int ne, int symm, int d1d, int q1d,
                              const double *B, const double *G, const double *Dq,
                              double *Y)
