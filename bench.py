@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU baseline: applies timed for about this long")
     ap.add_argument("--no-pcg", action="store_true", help="skip the precision-form PCG comparison")
-    ap.add_argument("--pcg-n", type=int, default=40,
+    ap.add_argument("--pcg-n", type=int, default=77,
                     help="mesh size of the precision-form PCG comparison (77: ~29.5 M DOFs at p=4)")
     ap.add_argument("--pcg-only", action="store_true", help="run only the precision-form PCG comparison")
     ap.add_argument("--pcg-max-it", type=int, default=20000)
@@ -229,6 +229,21 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def workload_config(args, world=1):
+    """The `config` dict of both arms (GPU and reference): the same workload
+    described from the command line alone."""
+    n, p = args.n, args.p
+    ne, ndofs, Q = n ** 3, (p * n + 1) ** 3, p + 2
+    S = 6 if args.kind == "diffusion" else 1
+    return {"workload": f"PA {args.kind} operator apply L->L (BilinearForm::Mult, AssemblyLevel::PARTIAL), "
+                        f"jittered hex mesh n={n}^3 (interior vertices +-0.1h, seed 1), H1 p={p}, "
+                        f"Gauss-Lobatto basis, q={Q} Gauss points per direction, coefficient 1, "
+                        f"{ndofs} DOFs, x~U[-1,1] (seed 2); one step = one apply",
+            "ne": ne, "ndofs": ndofs, "p": p, "q1d": Q, "kind": args.kind,
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (qdata %.2f GB in FP64); no flush" % (ne * S * Q ** 3 * 8 / 1e9)}
+
+
 # ----------------------------------------------------------------- problem set-up
 def build_problem(n, p, kind, seed_jitter=1):
     """Mesh, maps and qdata on the device through the library."""
@@ -243,11 +258,12 @@ def build_problem(n, p, kind, seed_jitter=1):
     return fes, integ, kind_id
 
 
-def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False, seconds=None):
+def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False, seconds=None, keep_y=None):
     """The oracle's L->L apply (gather, element kernel, CSR scatter) on the
     host cores, set up by the oracle itself from the same synthetic mesh.
     seconds: instead of `steps`, time as many applies as fit in about that
-    long (at least 3), from the warm-up apply's duration."""
+    long (at least 3), from the warm-up apply's duration. keep_y: a list that
+    receives the oracle's y = A x (the parity check of the GPU arm)."""
     from mfem_gb300 import fem
     from tests import oracle_lib
     o = oracle_lib.load()
@@ -268,7 +284,9 @@ def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False, seco
     kid = 0 if kind == "diffusion" else 1
     tw = time.perf_counter()
     for _ in range(max(warmup, 1)):
-        o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+        y = o.pa_mult(kid, mesh.ne, sp.ndofs, True, D, Q, gm, off, ind, t.B, t.G, qd, x)
+    if keep_y is not None:
+        keep_y.append(y)
     tw = (time.perf_counter() - tw) / max(warmup, 1)
     if seconds is not None:
         steps = int(min(max(3, seconds / max(tw, 1e-6)), 1000))
@@ -292,24 +310,72 @@ def cpu_oracle_apply_rate(n, p, kind, steps, warmup=1, single_thread=False, seco
 
 
 # ------------------------------------------------------------------- reference arm
+REF_BUILD = os.path.join(REPO, "baseline", "_ref", "build")
+
+
+def mfem_cpu_apply(n, p, steps, warmup, backend="omp", threads=None, timeout=1200):
+    """The reference MFEM's own PA diffusion apply (BilinearForm::Mult,
+    AssemblyLevel::PARTIAL) on the host cores: oracle/ref/bench_driver.cpp
+    linked to the unmodified reference sources, built for this host by
+    build() into baseline/_ref/build. Returns (result dict, None) or (None,
+    reason)."""
+    exe = os.path.join(REF_BUILD, "bench_driver")
+    if not os.path.exists(exe):
+        return None, "reference MFEM not built on this host (baseline/_ref/build/bench_driver absent)"
+    env = dict(os.environ)
+    env["OMP_NUM_THREADS"] = str(threads or os.cpu_count() or 1)
+    try:
+        r = subprocess.run([exe, str(n), str(p), str(steps), str(warmup), backend], capture_output=True,
+                           text=True, env=env, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return None, f"reference bench driver exceeded {timeout} s"
+    if r.returncode != 0:
+        return None, f"reference bench driver rc={r.returncode}: {r.stderr.strip()[-200:]}"
+    return json.loads(r.stdout.strip().splitlines()[-1]), None
+
+
+def mfem_sample_text(res):
+    return (f"{res['steps']} applies (after {res['warmup']} warm-up) of BilinearForm::Mult, "
+            f"AssemblyLevel::PARTIAL, Device(\"{res['backend']}\"), {res['threads']} OpenMP threads, "
+            f"n={round(res['ne'] ** (1 / 3))} p={res['p']} ({res['ndofs']} DOFs): the unmodified reference MFEM "
+            f"built from source on this host (g++ -O3, OpenMP); set-up {res['setup_s']:.1f} s untimed")
+
+
 def run_reference(args):
+    """The reference arm: the reference's own CPU implementation of the path,
+    timed on the host cores with every thread, on the GPU arm's workload
+    (same config dict). It loads no part of the CUDA library."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
     steps, warm = args.steps, args.warmup
-    sample_n = args.cpu_sample_n or args.n
-    rate, ndofs, threads, dt = cpu_oracle_apply_rate(sample_n, args.p, args.kind, steps,
-                                                     warmup=min(warm, 2))
+    cfg = workload_config(args, world)
+    res, why = (mfem_cpu_apply(args.n, args.p, steps, warm) if args.kind == "diffusion"
+                else (None, "the MFEM bench driver times the diffusion operator only"))
+    port = None
+    try:
+        prate, pnd, pthreads, pdt = cpu_oracle_apply_rate(args.n, args.p, args.kind, 3, warmup=1)
+        port = {"value": prate, "unit": "GDOF/s", "cores": pthreads, "kind": "port",
+                "sample": f"3 applies of the oracle (plain-C restatement of the reference's PA path), "
+                          f"n={args.n} p={args.p} ({pnd} DOFs)"}
+    except Exception as e:  # reported, never required
+        port = {"value": None, "error": str(e)[:200]}
+    if res is not None:
+        rate = res["ndofs"] * steps / res["total_s"] / 1e9
+        ms = res["total_s"] / steps * 1e3
+        base = {"value": rate, "unit": "GDOF/s", "cores": res["threads"], "kind": "reference",
+                "sample": mfem_sample_text(res), "median_apply_s": res["median_s"], "sum_y": res["sum_y"]}
+    else:
+        if port.get("value") is None:
+            print(json.dumps({"impl": "reference", "unavailable": f"{why}; port: {port.get('error')}"}))
+            return 0
+        rate, ms = port["value"], None
+        base = dict(port, note=why)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "GDOF/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"PA {args.kind} apply L->L, jittered hex mesh, p={args.p}, "
-                               f"q={args.p + 2}; each step one apply on the n={sample_n} "
-                               f"mesh ({ndofs} DOFs)", "p": args.p, "n": sample_n},
-        "cpu_baseline": {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} applies of the n={sample_n} p={args.p} mesh "
-                                   f"({ndofs} DOFs), OpenMP over elements/dofs"},
+        "steps": steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "cpu_baseline": base, "port_baseline": port,
         "e2e": {"value": rate, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -361,6 +427,7 @@ def run_gpu(args):
         barrier()
     ms = e0.elapsed_time(e1)
     launches = dev.launches() - launches0
+    y_check = y.clone()
     ms = max_over_ranks(ms, world)
     value = job_throughput(ndofs, args.steps, world, ms)
 
@@ -433,11 +500,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {0: "f64", 1: "f32", 2: "f64x2"}[prec], "data": "synthetic",
-        "config": {"workload": f"FP64 PA {args.kind} operator apply L->L (gather fused, CSR scatter), "
-                               f"jittered hex mesh n={args.n}^3, p={args.p}, q={args.p + 2}, "
-                               f"{ndofs} DOFs per GPU, x~U[-1,1]",
-                   "ne": ne, "ndofs": ndofs, "p": args.p, "q1d": Q, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (qdata %.2f GB); no flush" % (integ.qdata.numel() * 8 / 1e9)},
+        "config": workload_config(args, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                      "kernel": f"{args.kind}_apply (gather fused)",
@@ -453,22 +516,46 @@ def run_gpu(args):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    parity_ok = True
     if rank == 0:
+        # the oracle on the same mesh and x (its own maps, geometry and qdata,
+        # built on the host): the parity check at the benchmark's full size,
+        # and the port's CPU figure
+        sample_n = args.cpu_sample_n or args.n
+        port = None
         try:
-            sample_n = args.cpu_sample_n or args.n
+            ys = []
             rate, sn, threads, dt, rate1, csteps = cpu_oracle_apply_rate(
-                sample_n, args.p, args.kind, 3, single_thread=True, seconds=args.cpu_seconds)
-            line["cpu_baseline"] = {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
-                                    "sample": f"{csteps} applies of the n={sample_n} p={args.p} mesh "
-                                              f"({sn} DOFs), {dt:.1f} s; 1 thread: 2 applies",
-                                    "value_1_thread": rate1}
+                sample_n, args.p, args.kind, 3, single_thread=True, seconds=args.cpu_seconds, keep_y=ys)
+            port = {"value": rate, "unit": "GDOF/s", "cores": threads, "kind": "port",
+                    "sample": f"{csteps} applies of the oracle (plain-C restatement of the reference's PA "
+                              f"path) on the n={sample_n} p={args.p} mesh ({sn} DOFs), {dt:.1f} s; "
+                              f"1 thread: 2 applies", "value_1_thread": rate1}
+            if sample_n == args.n:
+                yo = ys[0]
+                yg = y_check.cpu().double().numpy()
+                rel = float(np.linalg.norm(yg - yo) / np.linalg.norm(yo))
+                tol = 1e-5 if prec == 1 else 1e-12
+                parity_ok = rel <= tol
+                line["parity"] = {"rel_l2_vs_oracle": rel, "tol": tol, "ok": parity_ok, "ndofs": sn,
+                                  "oracle": "oracle/gbpa_oracle.c (pinned to reference-generated golden "
+                                            "vectors), same mesh and x, oracle-side maps, geometry and qdata"}
         except Exception as e:  # the baseline is reported, never required
-            line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+            port = {"value": None, "error": str(e)[:200]}
+        res, why = (mfem_cpu_apply(sample_n, args.p, 10, 1) if args.kind == "diffusion"
+                    else (None, "the MFEM bench driver times the diffusion operator only"))
+        if res is not None:
+            line["cpu_baseline"] = {"value": res["ndofs"] * res["steps"] / res["total_s"] / 1e9,
+                                    "unit": "GDOF/s", "cores": res["threads"], "kind": "reference",
+                                    "sample": mfem_sample_text(res)}
+            line["port_baseline"] = port
+        else:
+            line["cpu_baseline"] = dict(port or {}, note=why)
         line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-    return 0
+    return 0 if parity_ok else 1
 
 
 def run_extras(args, fes, integ, op, x, y):
@@ -577,6 +664,37 @@ def run_pcg_form(n, p, max_it=2000):
     out["mixed_reliable"] = {"status": st, "seconds": info.seconds, "replacements": info.outer_iterations,
                              "f32_iterations": info.iterations, "true_rel_residual": info.true_rel_residual,
                              "rel_l2_vs_fp64": float(torch.linalg.norm(Xr - X64) / torch.linalg.norm(X64))}
+    # the FP64 reference solution: FP64 Jacobi-PCG to 1e-12; every solution's
+    # error against it, and every solution's true residual computed by the
+    # oracle on the host (plain-C apply, FP64) from the same qdata and maps
+    Xref = torch.zeros_like(b)
+    st = dev.lib.gbpa_pcg_solve(A64.handle, P(M.dinv), P(b), P(Xref), 1e-12, 0.0, 2 * max_it, 0,
+                                ctypes.byref(info))
+    out["fp64_reference_solution"] = {"status": st, "rel_tol": 1e-12, "seconds": info.seconds,
+                                      "iterations": info.iterations, "true_rel_residual": info.true_rel_residual}
+    sols = {"fp64_pcg": X64, "mixed_f32_in_f64": Xm, "mixed_reliable": Xr}
+    for name, X in sols.items():
+        out[name]["rel_l2_vs_fp64_reference"] = float(torch.linalg.norm(X - Xref) / torch.linalg.norm(Xref))
+    try:
+        from tests import oracle_lib
+        o = oracle_lib.load()
+        R = fes.GetElementRestriction()
+        gm, off, ind = R.gather_map.cpu().numpy(), R.offsets.cpu().numpy(), R.indices.cpu().numpy()
+        Bh, Gh, qh = integ.B.cpu().numpy(), integ.G.cpu().numpy(), integ.qdata.cpu().numpy()
+        bh = b.cpu().numpy()
+        ess_l = torch.from_numpy(ess).long()
+        for name, X in list(sols.items()) + [("fp64_reference_solution", Xref)]:
+            xh = X.cpu().clone()
+            xh[ess_l] = 0.0
+            r = bh - o.pa_mult(0, fes.ne, nd, True, integ.D, integ.Q, gm, off, ind, Bh, Gh, qh, xh.numpy())
+            r[ess] = 0.0
+            out[name]["oracle_true_rel_residual"] = float(np.linalg.norm(r) / np.linalg.norm(bh))
+        del qh
+    except Exception as e:  # reported, never required
+        out["oracle_check_error"] = str(e)[:200]
+    out["error_target"] = "solution rel. L2 error vs the FP64 reference solution <= 1e-9"
+    out["mixed_meets_target"] = bool(out["mixed_reliable"]["rel_l2_vs_fp64_reference"] <= 1e-9 and
+                                     out["mixed_f32_in_f64"]["rel_l2_vs_fp64_reference"] <= 1e-9)
     t64 = out["fp64_pcg"]["seconds"]
     out["speedup_mixed_vs_fp64"] = t64 / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)
     out["speedup_mixed_vs_f64x2_pcg"] = out["f64x2_pcg"]["seconds"] / max(out["mixed_f32_in_f64"]["seconds"], 1e-30)

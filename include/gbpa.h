@@ -247,6 +247,18 @@ int gbpa_operator_mult_host(gbpa_operator_t op, const void *x, void *y);
  * AddMultPA on a zeroed E-vector, fem/bilinearform_ext.cpp:530-546). yE is
  * an E-vector (D, D, D, NE) in the descriptor's precision. */
 int gbpa_operator_apply_element(gbpa_operator_t op, const void *x, void *yE);
+/* Domain-integrator element markers: PABilinearFormExtension::
+ * AddMultWithMarkers with AddWithMarkers_ (fem/bilinearform_ext.cpp:530-550,
+ * 753-774, 807-847) and the marked diagonal (:405-440). Element e contributes
+ * to Mult, the PCG solves and AssembleDiagonal iff attributes[e] > 0 and
+ * markers[attributes[e] - 1] != 0 (BilinearForm::AddDomainIntegrator(integ,
+ * elem_marker) with the mesh's element attributes). attributes: device
+ * int[ne]; markers: device int[n_markers], one per attribute. An attribute
+ * above n_markers returns GBPA_ERR_INDEX and leaves every element active.
+ * attributes == NULL removes the markers (every element contributes). The
+ * arrays are read during the call only. */
+int gbpa_operator_set_element_markers(gbpa_operator_t op, const int *attributes,
+                                      const int *markers, int n_markers);
 /* BilinearForm::AssembleDiagonal (PA), fem/bilinearform_ext.cpp:370-454,
  * with ConstrainedOperator::AssembleDiagonal DIAG_ONE when ess is set.
  * diag is always FP64. */
@@ -264,7 +276,9 @@ int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag);
  * GBPA_ERR_UNSUPPORTED. Work goes on `stream` (NULL: the legacy default
  * stream). All calls share the scratch, so calls that overlap on the GPU race:
  * serialise them. The first call on each device looks up the scratch's device
- * address; make it before any stream capture. */
+ * address and keeps it; make it before any stream capture, and do not use this
+ * entry point after a cudaDeviceReset of that device (the kept address belonged
+ * to the old context). (D, Q) beyond 16 returns GBPA_ERR_UNSUPPORTED. */
 #define GBPA_NOALLOC_MAX_EVEC (1 << 21)
 int gbpa_diffusion_mult_noalloc(void *stream, int ne, int ndofs, int d1d, int q1d,
                                 int symm, const double *B, const double *G,

@@ -2,11 +2,17 @@
 
 The compute path is libgbpa.so (CUDA, sm_103a), bound through its C ABI in
 _lib.py; pa.py mirrors the reference's PA interface on top of it; fem.py holds
-the host-side discretisation data. Importing the package loads the CUDA
-library and raises if it has not been built.
+the host-side discretisation data (meshes, spaces, basis tables) and loads no
+native code. The CUDA library is loaded on first use -- `mfem_gb300.lib`, or
+`pa.Device()` -- and that first use raises if the library has not been built:
+there is no CPU fallback.
 """
-from . import _lib
-
-lib = _lib.load()
 
 __all__ = ["lib"]
+
+
+def __getattr__(name):
+    if name == "lib":
+        from . import _lib
+        return _lib.load()
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gbpa_operator_mult_host": (I, [P, P, P]),
     "gbpa_operator_apply_element": (I, [P, P, P]),
     "gbpa_operator_assemble_diagonal": (I, [P, P]),
+    "gbpa_operator_set_element_markers": (I, [P, P, P, I]),
     "gbpa_diffusion_mult_noalloc": (I, [P, I, I, I, I, I, P, P, P, P, P, P, P, P]),
     "gbpa_vec_dot": (I, [P, I64, P, P, ctypes.POINTER(D)]),
     "gbpa_vec_add": (I, [P, I64, P, D, P, P]),

@@ -29,14 +29,32 @@ def key(kind, prec, D, Q):
     return f"{kind}:{prec}:{D}:{Q}"
 
 
+def _parse_entry(k, v):
+    """(kind id, precision id, D, Q, nbz) of one table entry; raises
+    KeyError/ValueError/TypeError/AttributeError on a malformed entry."""
+    kind, prec, D, Q = k.split(":")
+    return KINDS[kind], PRECS[prec], int(D), int(Q), int(v)
+
+
+def _parse_table(table, what, skipped):
+    """Valid entries of one table section; malformed ones are listed in
+    `skipped` and left out."""
+    out = []
+    for k, v in dict(table).items():
+        try:
+            out.append(_parse_entry(k, v))
+        except (KeyError, ValueError, TypeError, AttributeError):
+            skipped.append(f"{what}[{k!r}]")
+    return out
+
+
 def apply_table(lib, table):
-    """Install a tuning table into the library (kind/prec names as in KINDS, PRECS)."""
-    n = 0
-    for k, nbz in table.items():
-        kind, prec, D, Q = k.split(":")
-        if lib.gbpa_set_elements_per_block(KINDS[kind], PRECS[prec], int(D), int(Q), int(nbz)) == 0:
-            n += 1
-    return n
+    """Install a tuning table into the library (kind/prec names as in KINDS,
+    PRECS). Every entry is parsed before any is installed; malformed entries
+    are skipped. Returns the number of entries the library accepted."""
+    entries = _parse_table(table, "nbz", [])
+    return sum(1 for kd, pr, D, Q, nbz in entries
+               if lib.gbpa_set_elements_per_block(kd, pr, D, Q, nbz) == 0)
 
 
 # (D, Q) pairs with a compile-time 3D-layout diffusion kernel (GBPA_DQ3_LIST)
@@ -45,29 +63,38 @@ DQ3 = {(2, 2), (2, 3), (3, 3), (3, 4), (4, 4), (4, 5), (5, 5), (5, 6), (6, 6), (
 
 
 def apply_layouts(lib, layout3d):
-    """Install the 3D-layout entries {key: nbz}."""
-    n = 0
-    for k, nbz in layout3d.items():
-        kind, prec, D, Q = k.split(":")
-        if lib.gbpa_set_apply_layout(KINDS[kind], PRECS[prec], int(D), int(Q), 1, int(nbz)) == 0:
-            n += 1
-    return n
+    """Install the 3D-layout entries {key: nbz} (parsed first, malformed
+    entries skipped)."""
+    entries = _parse_table(layout3d, "layout3d", [])
+    return sum(1 for kd, pr, D, Q, nbz in entries
+               if lib.gbpa_set_apply_layout(kd, pr, D, Q, 1, nbz) == 0)
 
 
 def load_default(lib, path=TUNING):
-    """Install a saved table; a missing, unreadable or malformed file leaves the
-    library's defaults in place (with a warning), and entries the library
-    rejects are skipped. Returns the number of entries installed."""
+    """Install a saved table. The whole file is read and every entry parsed
+    before anything is installed: a missing, unreadable or non-object file
+    leaves the library's defaults in place, and malformed entries are skipped
+    one by one, each named in a warning. Returns the number of entries
+    installed."""
+    import warnings
     if not os.path.exists(path):
         return 0
     try:
         with open(path) as f:
             t = json.load(f)
-        return apply_table(lib, dict(t.get("nbz", {}))) + apply_layouts(lib, dict(t.get("layout3d", {})))
-    except (OSError, ValueError, TypeError, AttributeError, KeyError) as e:
-        import warnings
+        if not isinstance(t, dict):
+            raise TypeError("the table is not a JSON object")
+        skipped = []
+        nbz = _parse_table(t.get("nbz", {}), "nbz", skipped)
+        lay = _parse_table(t.get("layout3d", {}), "layout3d", skipped)
+    except (OSError, ValueError, TypeError, AttributeError) as e:
         warnings.warn(f"tuning table {path} not applied ({type(e).__name__}: {e}); using the defaults")
         return 0
+    if skipped:
+        warnings.warn(f"tuning table {path}: skipped malformed entries {', '.join(skipped)}")
+    n = sum(1 for kd, pr, D, Q, v in nbz if lib.gbpa_set_elements_per_block(kd, pr, D, Q, v) == 0)
+    n += sum(1 for kd, pr, D, Q, v in lay if lib.gbpa_set_apply_layout(kd, pr, D, Q, 1, v) == 0)
+    return n
 
 
 def candidates_3d(prec, D, Q, kind="diffusion"):

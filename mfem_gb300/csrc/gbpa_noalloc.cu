@@ -18,7 +18,10 @@
 //  - The array keeps the last call's contents. Nothing needs clearing: the
 //    element kernel overwrites every scratch entry it later reads.
 //  - The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress; make that first call before any stream capture.
+//    cudaGetSymbolAddress and keeps it for the life of the process; make that
+//    first call before any stream capture. The kept address belongs to the
+//    device's primary context: do not call this entry point again after a
+//    cudaDeviceReset (or any other teardown of that context).
 #include "gbpa_dispatch.cuh"
 #include <mutex>
 
@@ -37,10 +40,9 @@ extern "C" int gbpa_diffusion_mult_noalloc(void *stream, int ne, int ndofs, int 
                                            const int *offsets, const int *indices,
                                            const double *x, double *y)
 {
-   if (ne < 0 || ndofs < 0 || d1d < 1 || q1d < 1 || d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D)
-   {
-      return GBPA_ERR_INVALID_ARGUMENT;
-   }
+   if (ne < 0 || ndofs < 0 || d1d < 1 || q1d < 1) { return GBPA_ERR_INVALID_ARGUMENT; }
+   // sizes beyond the kernels' range: the same code as the rest of the ABI
+   if (d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D) { return GBPA_ERR_UNSUPPORTED; }
    const long long nE = (long long)ne * d1d * d1d * d1d;
    if (nE > GBPA_NOALLOC_MAX_EVEC)
    {

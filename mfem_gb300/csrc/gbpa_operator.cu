@@ -214,6 +214,51 @@ __global__ void copy_masked_kernel(int64_t n, const unsigned char *__restrict__ 
    }
 }
 
+// Element markers (PABilinearFormExtension::AddMultWithMarkers /
+// AddWithMarkers_, fem/bilinearform_ext.cpp:753-774,807-847): element e
+// contributes iff its attribute a > 0 and markers[a - 1] != 0. An attribute
+// past the marker array is an index error here (the reference reads past it).
+__global__ void element_markers_kernel(int ne, const int *__restrict__ attributes,
+                                       const int *__restrict__ markers, int n_markers,
+                                       unsigned char *__restrict__ active, int *flags)
+{
+   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x)
+   {
+      const int a = attributes[e];
+      if (a > n_markers) { atomicOr(flags, GBPA_FLAG_INDEX); active[e] = 0; continue; }
+      active[e] = (a > 0 && markers[a - 1] != 0) ? 1 : 0;
+   }
+}
+
+// The element kernels' gather map: GBPA_GATHER_SKIP on every slot whose dof is
+// essential (mask) or whose element is unmarked (active); an unmarked element
+// then gathers zeros, and its apply contributes exactly zero to the scatter.
+__global__ void operator_gather_map_kernel(int64_t n, int nd, const int *__restrict__ gmap,
+                                           const unsigned char *__restrict__ mask,
+                                           const unsigned char *__restrict__ active,
+                                           int *__restrict__ out)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int g = gmap[i];
+      const int j = g >= 0 ? g : -1 - g;
+      const bool off = (active && !active[i / nd]) || (mask && mask[j]);
+      out[i] = off ? GBPA_GATHER_SKIP : g;
+   }
+}
+
+// zero the E-vector entries of unmarked elements (diagonal with markers)
+__global__ void zero_unmarked_kernel(int64_t n, int nd, const unsigned char *__restrict__ active,
+                                     double *__restrict__ yE)
+{
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      if (!active[i / nd]) { yE[i] = 0.0; }
+   }
+}
+
 __global__ void set_mask_one_kernel(int ndofs, const unsigned char *mask, double *y)
 {
    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndofs; i += gridDim.x * blockDim.x)
@@ -354,12 +399,65 @@ extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *de
    return GBPA_SUCCESS;
 }
 
+extern "C" int gbpa_operator_set_element_markers(gbpa_operator_t op, const int *attributes,
+                                                 const int *markers, int n_markers)
+{
+   if (!op || n_markers < 0 || (attributes && n_markers > 0 && !markers)) { return GBPA_ERR_INVALID_ARGUMENT; }
+   const gbpa_operator_desc &d = op->d;
+   gbpa_ctx *ctx = op->ctx;
+   const int64_t nE = evec_size(d);
+   const int nd = d.d1d * d.d1d * d.d1d;
+   // the element kernels' map changes: a captured PCG iteration is stale
+   if (op->graph) { cudaStreamSynchronize(ctx->stream); cudaGraphExecDestroy(op->graph); op->graph = nullptr; }
+   int rc = GBPA_SUCCESS;
+   if (!attributes)
+   {
+      // back to every element
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(op->emask);
+      op->emask = nullptr;
+      if (!op->mask) { cudaFree(op->gmap_m); op->gmap_m = nullptr; return GBPA_SUCCESS; }
+   }
+   else if (d.ne > 0)
+   {
+      int flags = 0;
+      rc = gbpa_get_error_flags(ctx, &flags);   // clear stale flags
+      if (!rc && !op->emask) { rc = check_cuda(cudaMalloc(&op->emask, d.ne), "cudaMalloc(element markers)"); }
+      if (!rc)
+      {
+         element_markers_kernel<<<grid_for(d.ne, 256), 256, 0, ctx->stream>>>(d.ne, attributes, markers, n_markers,
+                                                                            op->emask, ctx->d_flags);
+         rc = last_launch(ctx, "element_markers");
+      }
+      if (!rc) { rc = gbpa_get_error_flags(ctx, &flags); }
+      if (!rc && (flags & GBPA_FLAG_INDEX)) { rc = GBPA_ERR_INDEX; }
+      if (rc)
+      {
+         // refused: every element active again
+         cudaStreamSynchronize(ctx->stream);
+         cudaFree(op->emask);
+         op->emask = nullptr;
+         if (!op->mask) { cudaFree(op->gmap_m); op->gmap_m = nullptr; return rc; }
+      }
+   }
+   if (nE == 0) { return rc; }
+   if (!op->gmap_m)
+   {
+      const int ra = check_cuda(cudaMalloc(&op->gmap_m, sizeof(int) * nE), "cudaMalloc(masked map)");
+      if (ra) { op->gmap_m = nullptr; return ra; }
+   }
+   operator_gather_map_kernel<<<grid_for(nE, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(
+      nE, nd, d.gather_map, op->mask, op->emask, op->gmap_m);
+   const int rl = last_launch(ctx, "operator_gather_map");
+   return rc ? rc : rl;
+}
+
 extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
 {
    if (!op) { return GBPA_SUCCESS; }
    cudaStreamSynchronize(op->ctx->stream);
    if (op->graph) { cudaGraphExecDestroy(op->graph); }
-   cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->gmap_m); cudaFree(op->qd2);
+   cudaFree(op->yE); cudaFree(op->mask); cudaFree(op->emask); cudaFree(op->gmap_m); cudaFree(op->qd2);
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
    cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb); cudaFree(op->stage);
@@ -514,6 +612,14 @@ extern "C" int gbpa_operator_assemble_diagonal(gbpa_operator_t op, double *diag)
                                 (const double *)d.qdata, (double *)op->yE);
    }
    if (rc) { return rc; }
+   if (op->emask)
+   {
+      // assemble_diagonal_with_markers (fem/bilinearform_ext.cpp:405-440)
+      zero_unmarked_kernel<<<grid_for(nE, 256, 8 * ctx->num_sms), 256, 0, ctx->stream>>>(
+         nE, d.d1d * d.d1d * d.d1d, op->emask, (double *)op->yE);
+      rc = last_launch(ctx, "zero_unmarked");
+      if (rc) { return rc; }
+   }
    rc = launch_csr_scatter<double>(ctx, d.ndofs, d.offsets, d.indices, (const double *)op->yE,
                                    diag, nullptr, nullptr, false, true);
    if (rc || !op->mask) { return rc; }

@@ -21,7 +21,9 @@ struct gbpa_operator
    gbpa_ctx *ctx = nullptr;
    gbpa_operator_desc d{};
    unsigned char *mask = nullptr;   // ess mask (ndofs) or null
-   int *gmap_m = nullptr;           // with ess: gather map with the ess slots set to GBPA_GATHER_SKIP
+   unsigned char *emask = nullptr;  // element markers: 1 = the element contributes (null: all do)
+   int *gmap_m = nullptr;           // with ess or element markers: gather map with the ess slots and
+                                    // every slot of an unmarked element set to GBPA_GATHER_SKIP
    void *yE = nullptr;              // E-vector scratch in the operator's precision
    float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
    // PCG workspace (vectors in the operator's precision)

@@ -167,6 +167,9 @@ class CartesianMesh:
             v[interior] += (2.0 * u[interior] - 1.0) * jitter * h
         self.vertices = v
         self.curved = curved
+        # element attributes (1-based, as Mesh::GetAttribute): all 1, as
+        # MakeCartesian3D sets them; a caller may assign its own
+        self.attributes = np.ones(self.ne, np.int32)
 
     def element_corners(self):
         """(NE, 8) vertex ids in lexicographic corner order (ax fastest)."""

@@ -374,6 +374,19 @@ class PAOperator:
     def AssembleDiagonal(self, diag):
         check(_dev().lib.gbpa_operator_assemble_diagonal(self.handle, _p(diag)), "operator_assemble_diagonal")
 
+    def SetElementMarkers(self, attributes, markers):
+        """Only elements whose attribute a has markers[a - 1] != 0 contribute
+        (AddMultWithMarkers, fem/bilinearform_ext.cpp:807-847); None removes
+        the markers."""
+        lib = _dev().lib
+        if attributes is None:
+            check(lib.gbpa_operator_set_element_markers(self.handle, None, None, 0), "set_element_markers")
+            return
+        a = to_dev(np.asarray(attributes, np.int32))
+        m = to_dev(np.asarray(markers, np.int32))
+        check(lib.gbpa_operator_set_element_markers(self.handle, _p(a), _p(m), m.numel()),
+              "set_element_markers")
+
     def __del__(self):
         try:
             _dev().lib.gbpa_operator_destroy(self.handle)
@@ -396,18 +409,26 @@ class BilinearForm:
             raise NotImplementedError("only AssemblyLevel.PARTIAL is provided")
         self.level = level
 
-    def AddDomainIntegrator(self, integ):
+    def AddDomainIntegrator(self, integ, elem_marker=None):
+        """elem_marker: one entry per element attribute (the mesh's
+        `attributes`); only elements of marked attributes contribute."""
         if self.integs:
             raise NotImplementedError("one domain integrator per form")
         self.integs.append(integ)
+        self.elem_marker = None if elem_marker is None else np.asarray(elem_marker, np.int32)
+
+    def _markers(self, op):
+        if getattr(self, "elem_marker", None) is not None:
+            op.SetElementMarkers(self.fes.mesh.attributes, self.elem_marker)
+        return op
 
     def Assemble(self, modes=None, precision=_lib.GBPA_F64):
         if self.level != AssemblyLevel.PARTIAL:
             raise RuntimeError("call SetAssemblyLevel(AssemblyLevel.PARTIAL) first")
         integ = self.integs[0]
         integ.AssemblePA(self.fes, modes)
-        self.op = PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
-                             precision=precision)
+        self.op = self._markers(PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
+                                           precision=precision))
 
     def Height(self):
         return self.fes.ndofs
@@ -420,8 +441,8 @@ class BilinearForm:
 
     def ConstrainedOperator(self, ess, precision=_lib.GBPA_F64):
         integ = self.integs[0]
-        return PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
-                          ess=ess, precision=precision)
+        return self._markers(PAOperator(integ.kind, self.fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata,
+                                        ess=ess, precision=precision))
 
     def FormLinearSystem(self, ess_tdof_list, x, b):
         """Operator::FormLinearSystem (linalg/operator.cpp:129-143) with the

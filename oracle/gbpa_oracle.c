@@ -720,6 +720,32 @@ void or_pa_mult(int kind, int ne, int ndofs, int symm, int d1d, int q1d,
    or_restriction_mult_transpose(d1d * d1d * d1d, ndofs, offsets, indices, yE, y, 0);
 }
 
+/* fem/bilinearform_ext.cpp:807-847: the integrator's apply into a zeroed
+ * temporary E-vector, then AddWithMarkers_ (:753-774) adds the marked
+ * elements' blocks to localY, which MultTranspose scatters (:548-556). */
+void or_pa_mult_markers(int kind, int ne, int ndofs, int symm, int d1d, int q1d,
+                        const int *gather_map, const int *offsets, const int *indices,
+                        const double *B, const double *G, const double *Dq,
+                        const int *attributes, const int *markers,
+                        const double *x, double *y, double *work)
+{
+   const int nd = d1d * d1d * d1d;
+   const long nE = (long)ne * nd;
+   double *xE = work, *tE = work + nE, *yE = work + 2 * nE;
+   or_restriction_mult(ne, nd, gather_map, x, xE);
+   memset(tE, 0, sizeof(double) * nE);
+   memset(yE, 0, sizeof(double) * nE);
+   if (kind == 0) { or_diffusion_apply3d(ne, symm, d1d, q1d, B, G, Dq, xE, tE); }
+   else { or_mass_apply3d(ne, d1d, q1d, B, Dq, xE, tE); }
+   for (int e = 0; e < ne; ++e)
+   {
+      const int a = attributes[e];
+      if (a <= 0 || markers[a - 1] == 0) { continue; }
+      for (int i = 0; i < nd; ++i) { yE[(long)e * nd + i] += tE[(long)e * nd + i]; }
+   }
+   or_restriction_mult_transpose(nd, ndofs, offsets, indices, yE, y, 0);
+}
+
 /* ----------------------------------------------------------------- PCG */
 static double dot(int n, const double *a, const double *b)
 {

@@ -81,6 +81,17 @@ void or_pa_mult(int kind, int ne, int ndofs, int symm, int d1d, int q1d,
                 const double *B, const double *G, const double *D,
                 const double *x, double *y, double *work);
 
+/* PABilinearFormExtension::AddMultWithMarkers, fem/bilinearform_ext.cpp:
+ * 530-550 and 807-847: y = R^T sum_e [marked e] A_e R x, where element e is
+ * marked iff attributes[e] > 0 and markers[attributes[e] - 1] != 0
+ * (AddWithMarkers_, :753-774). kind 0 = diffusion, 1 = mass. work: 3*ne*D^3
+ * doubles. */
+void or_pa_mult_markers(int kind, int ne, int ndofs, int symm, int d1d, int q1d,
+                        const int *gather_map, const int *offsets, const int *indices,
+                        const double *B, const double *G, const double *D,
+                        const int *attributes, const int *markers,
+                        const double *x, double *y, double *work);
+
 /* CGSolver::Mult (linalg/solvers.cpp:869-1050) with OperatorJacobiSmoother
  * (linalg/solvers.cpp:401-452) on ConstrainedOperator (linalg/operator.cpp:
  * 601-661, DIAG_ONE) around the PA diffusion operator. dinv is the smoother's

@@ -350,6 +350,54 @@ static void run_case(const Case &c, const std::string &root)
       mint->AddMultPA(xE, yE); save(dir, "yE_mass", yE);
    }
 
+   if (!c.solve && c.coeff == C_NONSYM)
+   {
+      // VectorDiffusionIntegrator / VectorMassIntegrator PA with the case's
+      // (nonsymmetric) matrix coefficient on the vdim = 3 space (byNODES):
+      // components coupled through the coefficient
+      // (fem/integ/bilininteg_vecdiffusion_pa.cpp:64-68,119-130,213-272;
+      // fem/integ/bilininteg_vecmass_pa.cpp:73-78,119-160), and the
+      // coefficient as both setups project it (ProjectTranspose)
+      FiniteElementSpace vfes(&mesh, &fec, 3);
+      const Operator *vR = vfes.GetElementRestriction(ElementDofOrdering::LEXICOGRAPHIC);
+      Vector vx(vfes.GetVSize());
+      uint64_t sv = 5;
+      for (int i = 0; i < vx.Size(); i++) { vx(i) = 2.0 * u01(sv) - 1.0; }
+      Vector vxE(vR->Height());
+      vR->Mult(vx, vxE);
+      VectorDiffusionIntegrator *vdi = new VectorDiffusionIntegrator(knon);
+      vdi->SetIntRule(&ir);
+      BilinearForm va(&vfes);
+      va.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      va.AddDomainIntegrator(vdi);
+      va.Assemble();
+      Vector vy(vfes.GetVSize());
+      va.Mult(vx, vy);
+      Vector vyE(vR->Height());
+      vyE = 0.0;
+      vdi->AddMultPA(vxE, vyE);
+      save(dir, "vec_x", vx);
+      save(dir, "vec_xE", vxE);
+      save(dir, "vmat_y", vy);
+      save(dir, "vmat_yE", vyE);
+      VectorMassIntegrator *vmi = new VectorMassIntegrator(knon);
+      vmi->SetIntRule(&ir);
+      BilinearForm vm(&vfes);
+      vm.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      vm.AddDomainIntegrator(vmi);
+      vm.Assemble();
+      Vector vmy(vfes.GetVSize());
+      vm.Mult(vx, vmy);
+      Vector vmyE(vR->Height());
+      vmyE = 0.0;
+      vmi->AddMultPA(vxE, vmyE);
+      save(dir, "vmatmass_y", vmy);
+      save(dir, "vmatmass_yE", vmyE);
+      CoefficientVector mc(qs, CoefficientStorage::FULL);
+      mc.ProjectTranspose(knon);
+      save(dir, "vmat_coeff", mc);
+   }
+
    if (!c.solve && (c.coeff == C_FN || c.coeff == C_VEC))
    {
       // VectorDiffusionIntegrator PA on the vdim = 3 space (byNODES) with the
@@ -658,6 +706,8 @@ int main(int argc, char **argv)
       {"jit2_p6_fn",      2, 6, 8, 0.1, C_FN,     false, false},
       {"cart1_p8_one",    1, 8, 10, 0.0, C_ONE,   false, false},
       {"jit1_p7_fn",      1, 7, 9, 0.1, C_FN,     false, false},
+      {"jit2_p5_fn",      2, 5, 7, 0.1, C_FN,     false, false},
+      {"curv2_p5_fn",     2, 5, 7, 0.0, C_FN,     true,  false},
       {"curv2_p3_fn",     2, 3, 5, 0.0, C_FN,     true,  false},
       {"cfg1_solve",      8, 3, 4, 0.0, C_ONE,    false, true},
    };

@@ -33,6 +33,7 @@ _SIGS = {
     "or_mass_apply3d": [_I, _I, _I, _P, _P, _P, _P],
     "or_mass_diagonal3d": [_I, _I, _I, _P, _P, _P],
     "or_pa_mult": [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "or_pa_mult_markers": [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "or_pcg_diffusion": [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _I,
                          _P, _P, _P, _D, _D, _I, _I, _P, _P],
     "or_num_threads": [],
@@ -174,6 +175,15 @@ class Oracle:
         work = np.zeros(2 * ne * d1d ** 3)
         self.lib.or_pa_mult(kind, ne, ndofs, int(symm), d1d, q1d, _ptr(gm), _ptr(off), _ptr(ind),
                             _ptr(B), _ptr(G), _ptr(D), _ptr(x), _ptr(y), _ptr(work))
+        return y
+
+    def pa_mult_markers(self, kind, ne, ndofs, symm, d1d, q1d, gm, off, ind, B, G, D, attributes, markers, x):
+        y = np.zeros(ndofs)
+        work = np.zeros(3 * ne * d1d ** 3)
+        a = np.ascontiguousarray(attributes, np.int32)
+        m = np.ascontiguousarray(markers, np.int32)
+        self.lib.or_pa_mult_markers(kind, ne, ndofs, int(symm), d1d, q1d, _ptr(gm), _ptr(off), _ptr(ind),
+                                    _ptr(B), _ptr(G), _ptr(D), _ptr(a), _ptr(m), _ptr(x), _ptr(y), _ptr(work))
         return y
 
     def pcg_diffusion(self, ne, ndofs, symm, d1d, q1d, gm, off, ind, B, G, D, ess, dinv, b,

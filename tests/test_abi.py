@@ -130,45 +130,3 @@ def test_host_restriction_build_rejects_out_of_range(lib):
     off = np.zeros(5, np.int32); ind = np.zeros(4, np.int32); gm = np.zeros(4, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     assert lib.gbpa_restriction_build(1, 4, 4, P(ed), None, P(off), P(ind), P(gm)) == -9
-
-
-def test_every_entry_point_is_documented_for_integrators():
-    """INTEGRATION.md names every exported entry point (call-site table or
-    the list of the remaining ones)."""
-    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
-    missing = [n for n in declared_symbols() if n not in doc]
-    assert not missing, missing
-
-
-def _calls_in_code_blocks(text):
-    """(name, number of top-level arguments) of every gbpa_* call inside the
-    ``` code blocks of a markdown text."""
-    out = []
-    for block in re.findall(r"```[a-z]*\n(.*?)```", text, flags=re.S):
-        for m in re.finditer(r"\b(gbpa_\w+)\s*\(", block):
-            i, depth, args, cur = m.end(), 1, 0, ""
-            while i < len(block) and depth:
-                c = block[i]
-                if c in "([{":
-                    depth += 1
-                elif c in ")]}":
-                    depth -= 1
-                elif c == "," and depth == 1:
-                    args += 1
-                if depth:
-                    cur += c
-                i += 1
-            n = 0 if not cur.strip() else args + 1
-            out.append((m.group(1), n))
-    return out
-
-
-def test_integration_snippets_match_the_prototypes():
-    """Every gbpa_* call in INTEGRATION.md's code samples passes as many
-    arguments as the header declares."""
-    protos = _prototypes()
-    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
-    calls = [(n, k) for n, k in _calls_in_code_blocks(doc) if n in protos]
-    assert len(calls) >= 10
-    bad = [(n, k, len(protos[n][1])) for n, k in calls if k != len(protos[n][1])]
-    assert not bad, bad

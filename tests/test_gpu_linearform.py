@@ -16,7 +16,8 @@ CASES = [c for c in golden_cases() if c != "cfg1_solve"]
 MESHES = {"cart2_p2_one": (2, 2, 0.0, False), "cart2_p1_const": (2, 1, 0.0, False),
           "jit3_p3_fn": (3, 3, 0.1, False), "jit2_p4_vec": (2, 4, 0.1, False), "jit2_p4_sym": (2, 4, 0.1, False),
           "jit2_p2_nonsym": (2, 2, 0.1, False), "jit2_p6_fn": (2, 6, 0.1, False), "cart1_p8_one": (1, 8, 0.0, False),
-          "jit1_p7_fn": (1, 7, 0.1, False), "curv2_p3_fn": (2, 3, 0.0, True)}
+          "jit1_p7_fn": (1, 7, 0.1, False), "curv2_p3_fn": (2, 3, 0.0, True),
+          "jit2_p5_fn": (2, 5, 0.1, False), "curv2_p5_fn": (2, 5, 0.0, True)}
 
 
 def rel(a, b):
@@ -34,14 +35,35 @@ def test_domain_lf_from_reference_inputs(case):
     assert rel(H(b), g["lf_fn"]) < 1e-13
 
 
-@pytest.mark.parametrize("case", ["jit3_p3_fn", "jit2_p6_fn", "curv2_p3_fn", "cart1_p8_one"])
+def reference_dof_of(g, n, nd, our_gather_map):
+    """For each of the package's dofs, the reference dof at the same place.
+    The reference's MakeCartesian3D numbers vertices lexicographically (as the
+    package does) but orders elements along a space-filling curve, and numbers
+    dofs by vertices, edges, faces and interiors; both gather maps list an
+    element's dofs in the same lexicographic order. So element e of the
+    reference is the package's element at the lattice position of its first
+    corner vertex, and slot l of the two elements holds the same dof."""
+    ev = np.asarray(g["elem_vertices"]).reshape(-1, 8)
+    v0 = ev[:, 0]
+    i, j, k = v0 % (n + 1), (v0 // (n + 1)) % (n + 1), v0 // (n + 1) ** 2
+    ours = i + n * (j + n * k)                      # package element of each reference element
+    ref_gm = np.asarray(g["gather_map"]).reshape(-1, nd)
+    our_gm = np.asarray(our_gather_map).reshape(-1, nd)[ours]
+    assert (ref_gm >= 0).all() and (our_gm >= 0).all()
+    perm = np.full(our_gm.max() + 1, -1, np.int64)
+    perm[our_gm.reshape(-1)] = ref_gm.reshape(-1)
+    # a consistent bijection: every package dof gets exactly one reference dof
+    assert (perm >= 0).all()
+    pairs = np.unique(np.stack([our_gm.reshape(-1), ref_gm.reshape(-1)]), axis=1)
+    assert pairs.shape[1] == perm.size and np.unique(perm).size == perm.size
+    return perm
+
+
+@pytest.mark.parametrize("case", ["jit3_p3_fn", "jit2_p6_fn", "curv2_p3_fn", "cart1_p8_one", "curv2_p5_fn"])
 def test_linear_form_end_to_end(case):
     """Geometry, kappa at the rule's points and the assembly all on the
-    device from the package's own mesh. The package numbers dofs
-    lexicographically on the (p n + 1)^3 grid and elements lexicographically;
-    the reference numbers elements along a space-filling curve and dofs by
-    vertices, edges, faces, interiors, so the two vectors agree up to a
-    permutation: compared sorted."""
+    device from the package's own mesh, compared entry by entry with the
+    reference's vector through the dof correspondence (reference_dof_of)."""
     from mfem_gb300 import fem
     from mfem_gb300.pa import DomainLFIntegrator, FiniteElementSpace, LinearForm
     from tests.gpu_util import dev
@@ -53,7 +75,8 @@ def test_linear_form_end_to_end(case):
     lf = LinearForm(fes)
     lf.AddDomainIntegrator(DomainLFIntegrator("kappa"))
     b = lf.Assemble(modes=fem.kappa_modes(3))
-    assert rel(np.sort(b.cpu().numpy()), np.sort(g["lf_fn"])) < 1e-13
+    perm = reference_dof_of(g, n, (pdeg + 1) ** 3, fes.GetElementRestriction().gather_map.cpu().numpy())
+    assert rel(b.cpu().numpy(), np.asarray(g["lf_fn"])[perm]) < 1e-13
 
 
 def test_linear_form_of_one_integrates_the_volume():

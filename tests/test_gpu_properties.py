@@ -245,3 +245,60 @@ def test_indefinite_operator_stops():
     info = _lib.SolveInfo()
     st = d.lib.gbpa_pcg_solve(A.handle, p(dinv), p(b), p(x), 1e-10, 0.0, 100, 0, ctypes.byref(info))
     assert st == 0 and info.converged == 0 and info.iterations == 0
+
+
+@pytest.mark.parametrize("n", [1, 255, 256 * 8 * 152 + 17, 29_503_629])
+def test_vec_dot_values_and_reproducibility(n):
+    """Vector::operator* (linalg/vector.cpp:1079-1106, reduce in
+    general/reducers.hpp:531-594) through gbpa_vec_dot: within a worst-case
+    rounding bound of math.fsum of the products (the correctly rounded sum),
+    and bit-identical across repeated calls (fixed summation order)."""
+    from tests.gpu_util import dev
+    d = dev()
+    rng = np.random.default_rng(n)
+    xh = rng.uniform(-1, 1, n)
+    yh = rng.uniform(-1, 1, n)
+    x, y = torch.from_numpy(xh).cuda(), torch.from_numpy(yh).cuda()
+    r = ctypes.c_double(0.0)
+    assert d.lib.gbpa_vec_dot(d.ctx, n, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                              ctypes.byref(r)) == 0
+    exact = math.fsum((xh * yh).tolist())
+    # worst case: each thread's grid-stride chain (at most n / 1e4 terms for
+    # the >= 1e4 threads the kernel runs at these sizes), then two tree levels
+    # of depth <= 32 each, every step rounding once (2^-53 relative) with
+    # partial sums bounded by sum |x_i y_i|
+    k = n / 1e4 + 64
+    bound = k * 2.0 ** -53 * float(np.sum(np.abs(xh * yh)))
+    assert abs(r.value - exact) <= bound
+    vals = set()
+    for _ in range(3):
+        r2 = ctypes.c_double(0.0)
+        assert d.lib.gbpa_vec_dot(d.ctx, n, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()),
+                                  ctypes.byref(r2)) == 0
+        vals.add(r2.value)
+    assert vals == {r.value}
+
+
+@pytest.mark.parametrize("n", [1, 255, 256 * 8 * 152 + 17, 29_503_629])
+def test_vec_add_values(n):
+    """add(x, a, y, z): z = x + a*y (linalg/vector.cpp:414-600) through
+    gbpa_vec_add, against numpy in float64: equal up to the one rounding a
+    fused multiply-add saves (at most one ulp of |x| + |a y|); z may alias x."""
+    from tests.gpu_util import dev
+    d = dev()
+    rng = np.random.default_rng(n + 1)
+    xh = rng.uniform(-1, 1, n)
+    yh = rng.uniform(-1, 1, n)
+    a = -0.7310581
+    x, y = torch.from_numpy(xh).cuda(), torch.from_numpy(yh).cuda()
+    z = torch.full_like(x, float("nan"))
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert d.lib.gbpa_vec_add(d.ctx, n, P(x), a, P(y), P(z)) == 0
+    torch.cuda.synchronize()
+    ref = xh + a * yh
+    tol = 2.0 ** -52 * (np.abs(xh) + np.abs(a * yh))
+    assert np.all(np.abs(z.cpu().numpy() - ref) <= tol)
+    # in place: x = x + a*y
+    assert d.lib.gbpa_vec_add(d.ctx, n, P(x), a, P(y), P(x)) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), z.cpu().numpy())

@@ -193,3 +193,21 @@ def test_vector_mass_componentwise(oracle, case):
         yE[:, i, :] = oracle.mass_apply3d(ne, D, Q, g["B"], Di, xE[:, i, :].copy()).reshape(ne, D3)
     ref = g["vmass_yE"].reshape(ne, 3, D3)
     assert np.linalg.norm(yE - ref) / np.linalg.norm(ref) < 1e-13
+
+
+def test_markers_oracle_all_and_none_marked(oracle):
+    """The element-marker restatement (AddMultWithMarkers) reduces to the
+    plain L->L apply when every attribute is marked, gives zero when none
+    is, and is additive over a partition of the attributes."""
+    g = load_golden("jit3_p3_fn")
+    ne, ndofs, D, Q = (int(v) for v in g["meta"][:4])
+    args = (0, ne, ndofs, True, D, Q, g["gather_map"], g["offsets"], g["indices"], g["B"], g["G"],
+            g["qdata_diff"])
+    rng = np.random.default_rng(3)
+    attr = rng.integers(1, 4, ne).astype(np.int32)
+    full = oracle.pa_mult(*args, g["x"])
+    assert np.allclose(oracle.pa_mult_markers(*args, attr, [1, 1, 1], g["x"]), full, rtol=0, atol=1e-13)
+    assert np.abs(oracle.pa_mult_markers(*args, attr, [0, 0, 0], g["x"])).max() == 0.0
+    part = sum(oracle.pa_mult_markers(*args, attr, m, g["x"]) for m in ([1, 0, 0], [0, 1, 0], [0, 0, 1]))
+    assert np.linalg.norm(part - full) / np.linalg.norm(full) < 1e-14
+    assert np.allclose(full, g["y_diff"], rtol=0, atol=1e-12 * np.abs(g["y_diff"]).max())

@@ -121,3 +121,25 @@ def test_load_default_tolerates_bad_files(tmp_path):
     rejected = tmp_path / "rejected.json"
     rejected.write_text(json.dumps({"nbz": {"diffusion:f64:5:6": 500}, "layout3d": {"diffusion:f64:9:10": 2}}))
     assert at.load_default(lib, str(rejected)) == 0   # both entries refused by the library, none installed
+
+
+def test_load_default_skips_only_malformed_entries(tmp_path):
+    """A malformed entry is named in the warning and skipped; the valid
+    entries before and after it are installed, and the count says so."""
+    from mfem_gb300 import autotune as at
+    lib = _FakeLib()
+    mixed = tmp_path / "mixed.json"
+    mixed.write_text(json.dumps({"nbz": {"diffusion:f64:5:6": 7, "diffusion:f64:bad:6": 2, "mass:f32:5:6": 3},
+                                 "layout3d": {"diffusion:f64x2:5:6": 1, "nope": 1}}))
+    with pytest.warns(UserWarning, match="skipped malformed entries"):
+        n = at.load_default(lib, str(mixed))
+    assert n == 3
+    assert lib.nbz == {(0, 0, 5, 6): 7, (1, 1, 5, 6): 3}
+    assert lib.layout == {(0, 2, 5, 6): (1, 1)}
+    # a table that is not a JSON object installs nothing
+    arr = tmp_path / "arr.json"
+    arr.write_text("[1, 2]")
+    lib2 = _FakeLib()
+    with pytest.warns(UserWarning):
+        assert at.load_default(lib2, str(arr)) == 0
+    assert not lib2.nbz and not lib2.layout
