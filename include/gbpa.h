@@ -437,8 +437,11 @@ int gbpa_batched_pcg_solve_ex(gbpa_ctx_t ctx, int nprob,
  * coefficient component (coeff_vdim 1: the same scalar for every
  * component; coeff_vdim = vdim: C_c). C laid out (coeff_vdim, Q^3, NE),
  * c_size coeff_vdim (constant) or coeff_vdim Q^3 NE. D: (Q^3, 6, vdim, NE),
- * which fits in the reference's pa_data (Q^3 9 vdim NE). Matrix
- * coefficients (component coupling) are not supported. */
+ * which fits in the reference's pa_data (Q^3 9 vdim NE). coeff_vdim 9 (vdim
+ * 3) is a matrix coefficient, C (9, Q^3, NE) as CoefficientVector::
+ * ProjectTranspose stores it: block b of D (layout (Q^3, 6, NE, 9)) is the
+ * geometric factor times C(map[b]), map = {0,3,6,1,4,7,2,5,8} (:119-130,
+ * 213-272); apply it with gbpa_vector_diffusion_apply3d_coeff. */
 int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim,
                                   int coeff_vdim, const double *W,
                                   const double *J, const double *C,
@@ -449,12 +452,27 @@ int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim,
 int gbpa_vector_diffusion_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int d1d,
                                   int q1d, const double *B, const double *G,
                                   const double *D, const double *x, double *y);
+/* The same with the coefficient's vdim, as ApplyPAKernels::Run receives it
+ * (fem/integ/bilininteg_vecdiffusion_pa.cpp:276-330): coeff_vdim 1 or vdim as
+ * above; coeff_vdim 9 with vdim 3 is the matrix coefficient
+ * (VectorDiffusionIntegrator(MatrixCoefficient&), :64-68,119-130), whose
+ * components couple: y_j += G^T D_(j+3i) G x_i, with D written by
+ * gbpa_vector_diffusion_setup3d(coeff_vdim 9) in the block-major layout
+ * (Q^3, 6, NE, 9) (it fits the reference's pa_data, Q^3 * 9 * 9 * NE). */
+int gbpa_vector_diffusion_apply3d_coeff(gbpa_ctx_t ctx, int ne, int vdim, int coeff_vdim,
+                                        int d1d, int q1d, const double *B,
+                                        const double *G, const double *D,
+                                        const double *x, double *y);
 
 /* VectorMassIntegrator::AssemblePA / AddMultPA, 3D, scalar or vector
  * coefficient (fem/integ/bilininteg_vecmass_pa.cpp:21-210): D (Q^3,
  * coeff_vdim, NE) = C_k W detJ, the reference's own layout; the apply runs
  * the scalar mass operator per component on the (D^3, vdim, NE) E-vectors.
- * Matrix coefficients are not supported. */
+ * A matrix coefficient (vdim 3, coeff_vdim 9, C (9, Q^3, NE) as
+ * CoefficientVector::ProjectTranspose stores it) couples the components:
+ * D is then block-major (Q^3, NE, 9), block 3c+d = C(3c+d) W detJ, and the
+ * apply adds y_c += B^T D_(3c+d) B x_d (fem/integ/bilininteg_vecmass_pa.hpp:
+ * 157-170). */
 int gbpa_vector_mass_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim,
                              int coeff_vdim, const double *W, const double *J,
                              const double *C, int64_t c_size, double *D);
@@ -565,9 +583,14 @@ int gbpa_get_elements_per_block(int kind, int precision, int d1d, int q1d);
  * thread per (qx, qy) column, z in registers) or GBPA_LAYOUT_3D (block
  * (Q, Q, Q*nbz), one thread per quadrature point, every contraction through
  * shared memory; compile-time kernels for the (D, Q) pairs the 2D slab
- * specialises, others stay 2D; nbz * q1d <= 64 and nbz * q1d^3 <= 1024). The
- * autotuner chooses per order. get returns the layout and its nbz. */
-enum gbpa_layout { GBPA_LAYOUT_SLAB2D = 0, GBPA_LAYOUT_3D = 1 };
+ * specialises, others stay 2D; nbz * q1d <= 64 and nbz * q1d^3 <= 1024), or
+ * GBPA_LAYOUT_TC (FP32 diffusion operators only, (d1d, q1d) in (3,4), (4,5),
+ * (5,6); nbz ignored): the element contraction as two dense GEMMs per tile of
+ * 128 elements on the tcgen05 tensor cores (fp16 hi/lo operand limbs, FP32
+ * accumulation). An operator picks up the tensor-core layout when it is
+ * selected at operator creation. The autotuner chooses per order. get
+ * returns the layout and its nbz. */
+enum gbpa_layout { GBPA_LAYOUT_SLAB2D = 0, GBPA_LAYOUT_3D = 1, GBPA_LAYOUT_TC = 2 };
 int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, int layout,
                           int nbz);
 int gbpa_get_apply_layout(int kind, int precision, int d1d, int q1d, int *nbz);

@@ -111,6 +111,7 @@ SIGNATURES = {
                                       ctypes.POINTER(D)]),
     "gbpa_vector_diffusion_setup3d": (I, [P, I, I, I, I, P, P, P, I64, P]),
     "gbpa_vector_diffusion_apply3d": (I, [P, I, I, I, I, P, P, P, P, P]),
+    "gbpa_vector_diffusion_apply3d_coeff": (I, [P, I, I, I, I, I, P, P, P, P, P]),
     "gbpa_vector_mass_setup3d": (I, [P, I, I, I, I, P, P, P, I64, P]),
     "gbpa_vector_mass_apply3d": (I, [P, I, I, I, I, I, P, P, P, P]),
     "gbpa_domain_lf3d": (I, [P, I, I, I, P, P, P, P, I64, I, P, P, P]),

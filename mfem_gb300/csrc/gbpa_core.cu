@@ -7,6 +7,7 @@
 //   Jacobi setup       linalg/solvers.cpp:401-425
 #include "gbpa_csr.cuh"
 #include "gbpa_dispatch.cuh"
+#include "gbpa_tc.cuh"
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -718,28 +719,35 @@ extern "C" int gbpa_get_elements_per_block(int kind, int precision, int d1d, int
 }
 
 // ------------------------------------------------------ apply layout table
-static std::unordered_map<int, int> g_layout;   // key -> nbz of the 3D layout
+// key -> (layout, nbz of the 3D layout); absent = the 2D slab
+static std::unordered_map<int, std::pair<int, int>> g_layout;
 
 int gbpa::apply_layout(int kind, int precision, int D, int Q, int *nbz)
 {
    std::lock_guard<std::mutex> lock(g_nbz_mu);
    auto it = g_layout.find(nbz_key(kind, precision, D, Q));
    if (it == g_layout.end()) { return GBPA_LAYOUT_SLAB2D; }
-   if (nbz) { *nbz = it->second; }
-   return GBPA_LAYOUT_3D;
+   if (nbz) { *nbz = it->second.second; }
+   return it->second.first;
 }
 
 extern "C" int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, int layout, int nbz)
 {
    if (kind < 0 || kind > 1 || precision < 0 || precision > 2 || d1d < 1 || q1d < 1 ||
-       d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || (layout != GBPA_LAYOUT_SLAB2D && layout != GBPA_LAYOUT_3D) ||
+       d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D ||
+       (layout != GBPA_LAYOUT_SLAB2D && layout != GBPA_LAYOUT_3D && layout != GBPA_LAYOUT_TC) ||
        (layout == GBPA_LAYOUT_3D && (nbz < 1 || nbz * q1d * q1d * q1d > 1024 || nbz * q1d > 64)))
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
+   if (layout == GBPA_LAYOUT_TC &&
+       (kind != GBPA_DIFFUSION || precision != GBPA_F32 || !gbpa::tc::supported(d1d, q1d)))
+   {
+      return GBPA_ERR_UNSUPPORTED;
+   }
    std::lock_guard<std::mutex> lock(g_nbz_mu);
    if (layout == GBPA_LAYOUT_SLAB2D) { g_layout.erase(nbz_key(kind, precision, d1d, q1d)); }
-   else { g_layout[nbz_key(kind, precision, d1d, q1d)] = nbz; }
+   else { g_layout[nbz_key(kind, precision, d1d, q1d)] = {layout, layout == GBPA_LAYOUT_3D ? nbz : 0}; }
    return GBPA_SUCCESS;
 }
 

@@ -179,6 +179,11 @@ int elements_per_block(int kind, int precision, int D, int Q);
 // elements per block.
 int apply_layout(int kind, int precision, int D, int Q, int *nbz);
 
+// Vector mass with a matrix coefficient (vdim 3): block-major qdata
+// (Q^3, NE, 9), y_E += sum over the coupled blocks (gbpa_vector_coupled.cu).
+int vector_mass_apply_matrix(gbpa_ctx *ctx, int ne, int d1d, int q1d, const double *B, const double *D,
+                             const double *x, double *y);
+
 // Deterministic two-level dot product into a device scalar (double).
 template <typename T>
 int launch_dot(gbpa_ctx *ctx, int64_t n, const T *x, const T *y,

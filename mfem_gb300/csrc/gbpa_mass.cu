@@ -251,11 +251,13 @@ extern "C" int gbpa_domain_lf3d(gbpa_ctx_t ctx, int ne, int d1d, int q1d, const 
 extern "C" int gbpa_vector_mass_apply3d(gbpa_ctx_t ctx, int ne, int vdim, int coeff_vdim, int d1d, int q1d,
                                         const double *B, const double *D, const double *x, double *y)
 {
-   if (!ctx || ne < 0 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim) ||
+   const bool matrix = vdim == 3 && coeff_vdim == 9;
+   if (!ctx || ne < 0 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim && !matrix) ||
        (ne > 0 && (!B || !D || !x || !y)))
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
    if (!dq_ok(d1d, q1d)) { return GBPA_ERR_UNSUPPORTED; }
+   if (matrix) { return vector_mass_apply_matrix(ctx, ne, d1d, q1d, B, D, x, y); }
    return launch_mass_apply_qdiv(ctx, ne * vdim, d1d, q1d, B, D, x, y, coeff_vdim == 1 ? vdim : 1);
 }

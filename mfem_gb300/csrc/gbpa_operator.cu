@@ -7,6 +7,8 @@
 //   OperatorJacobiSmoother::Mult      linalg/solvers.cpp:427-452
 #include "gbpa_csr.cuh"
 #include "gbpa_operator.cuh"
+#include <type_traits>
+#include <vector>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -343,6 +345,28 @@ static int64_t qdata_size(const gbpa_operator_desc &d)
    return (int64_t)d.ne * q3 * (d.kind == GBPA_DIFFUSION ? (d.symm ? 6 : 9) : 1);
 }
 
+// Tensor-core layout of an FP32 diffusion operator: the Kronecker tables of
+// its (FP32) basis tables and the per-element output scales.
+static int setup_tensor_core(gbpa_operator *op)
+{
+   const gbpa_operator_desc &d = op->d;
+   const int n = d.q1d * d.d1d;
+   std::vector<float> bf(n), gf(n);
+   int rc = check_cuda(cudaMemcpy(bf.data(), d.B, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy B");
+   if (!rc) { rc = check_cuda(cudaMemcpy(gf.data(), d.G, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy G"); }
+   if (rc) { return rc; }
+   std::vector<double> bd(bf.begin(), bf.end()), gd(gf.begin(), gf.end());
+   op->tct = new (std::nothrow) tc::Tables;
+   if (!op->tct) { return GBPA_ERR_OUT_OF_MEMORY; }
+   rc = tc::build_tables(d.d1d, d.q1d, bd.data(), gd.data(), op->tct);
+   if (!rc) { rc = check_cuda(cudaMalloc(&op->tc_qscale, sizeof(float) * d.ne), "cudaMalloc(tc scale)"); }
+   if (!rc)
+   {
+      rc = tc::launch_qscale(op->ctx, d.ne, d.q1d, (const float *)d.qdata, (float)op->tct->R, op->tc_qscale);
+   }
+   return rc;
+}
+
 extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
                                     gbpa_operator_t *out)
 {
@@ -393,6 +417,11 @@ extern "C" int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *de
          rc = check_cuda(cudaMalloc(&op->gmap_m, sizeof(int) * nE), "cudaMalloc(masked map)");
          if (!rc) { rc = launch_masked_gather_map(ctx, nE, d.gather_map, op->mask, op->gmap_m); }
       }
+   }
+   if (!rc && d.kind == GBPA_DIFFUSION && d.precision == GBPA_F32 && d.symm && d.ne > 0 &&
+       tc::supported(d.d1d, d.q1d) && apply_layout(GBPA_DIFFUSION, GBPA_F32, d.d1d, d.q1d, nullptr) == GBPA_LAYOUT_TC)
+   {
+      rc = setup_tensor_core(op);
    }
    if (rc) { gbpa_operator_destroy(op); return rc; }
    *out = op;
@@ -461,6 +490,8 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    cudaFree(op->r); cudaFree(op->dv); cudaFree(op->z);
    cudaFree(op->partials); cudaFree(op->state);
    cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb); cudaFree(op->stage);
+   if (op->tct) { tc::free_tables(op->tct); delete op->tct; }
+   cudaFree(op->tc_qscale);
    delete op;
    return GBPA_SUCCESS;
 }
@@ -483,6 +514,15 @@ static int apply_to(gbpa_operator *op, const T *x, T *out, int mode, const int *
       }
       return launch_mass_apply_x2(op->ctx, d.ne, d.d1d, d.q1d, (const double *)d.B, op->qd2, xd,
                                   op->gather(), op->gather_mask(), (double *)out, mode, skip);
+   }
+   if constexpr (std::is_same<T, float>::value)
+   {
+      // the tensor-core layout, while it stays selected for this order
+      if (op->tct && apply_layout(GBPA_DIFFUSION, GBPA_F32, d.d1d, d.q1d, nullptr) == GBPA_LAYOUT_TC)
+      {
+         return tc::launch_diffusion_f32(op->ctx, d.ne, d.d1d, d.q1d, *op->tct, (const float *)d.qdata,
+                                         op->tc_qscale, x, op->gather(), op->gather_mask(), out, mode, skip);
+      }
    }
    if (d.kind == GBPA_DIFFUSION)
    {

@@ -1,6 +1,7 @@
 // Operator object shared by the operator and block-solver translation units.
 #pragma once
 #include "gbpa_dispatch.cuh"
+#include "gbpa_tc.cuh"
 
 struct PcgState
 {
@@ -26,6 +27,10 @@ struct gbpa_operator
                                     // every slot of an unmarked element set to GBPA_GATHER_SKIP
    void *yE = nullptr;              // E-vector scratch in the operator's precision
    float2 *qd2 = nullptr;           // GBPA_F64X2: qdata split into (hi, lo) floats
+   // tensor-core layout (FP32 diffusion): split Kronecker tables and the
+   // per-element output scale; null when the operator was created without it
+   gbpa::tc::Tables *tct = nullptr;
+   float *tc_qscale = nullptr;
    // PCG workspace (vectors in the operator's precision)
    void *r = nullptr, *dv = nullptr, *z = nullptr;
    double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)

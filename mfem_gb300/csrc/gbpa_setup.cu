@@ -225,6 +225,66 @@ __global__ void vector_diffusion_setup_kernel(int ne, int Q3, int vdim, int coef
    }
 }
 
+// VectorDiffusionIntegrator::AssemblePA with a matrix coefficient (vdim = 3,
+// fem/integ/bilininteg_vecdiffusion_pa.cpp:119-130,213-272): block b (0..8)
+// holds the geometric 3x3 symmetric factor times the coefficient entry
+// C(map[b]), map = {0,3,6,1,4,7,2,5,8}; block b = j + 3 i couples source
+// component i into component j. Layout block-major (Q^3, 6, NE, 9), so each
+// block is one scalar-diffusion qdata array (Q^3, 6, NE).
+__global__ void vector_diffusion_setup_matrix_kernel(int ne, int Q3, const double *__restrict__ W,
+                                                     const double *__restrict__ Jg,
+                                                     const double *__restrict__ C, int const_c,
+                                                     double *__restrict__ D)
+{
+   const int map[9] = {0, 3, 6, 1, 4, 7, 2, 5, 8};
+   const int64_t n = (int64_t)ne * Q3;
+   const double one = 1.0;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int q = (int)(i % Q3);
+      const int64_t e = i / Q3;
+      double J[3][3];
+      for (int c = 0; c < 3; ++c)
+         for (int d = 0; d < 3; ++d) { J[c][d] = Jg[q + (int64_t)Q3 * (c + 3 * (d + 3 * e))]; }
+      double d0[6];
+      diffusion_point(J, W[q], 1, &one, 1, d0, 1);
+      for (int b = 0; b < 9; ++b)
+      {
+         const int k = map[b];
+         const double ck = const_c ? C[k] : C[k + 9 * i];
+         double *out = D + q + (int64_t)Q3 * 6 * (e + (int64_t)ne * b);
+         for (int s = 0; s < 6; ++s) { out[(int64_t)s * Q3] = d0[s] * ck; }
+      }
+   }
+}
+
+// VectorMassIntegrator::AssemblePA with a matrix coefficient (vdim = 3,
+// fem/integ/bilininteg_vecmass_pa.cpp:73-78,119-160): block b = 3 c + d holds
+// C(b, q, e) W(q) detJ, coupling component d into component c. Layout
+// block-major (Q^3, NE, 9): each block is one scalar-mass qdata array.
+__global__ void vector_mass_setup_matrix_kernel(int ne, int Q3, const double *__restrict__ W,
+                                                const double *__restrict__ Jg, const double *__restrict__ C,
+                                                int const_c, double *__restrict__ D)
+{
+   const int64_t n = (int64_t)ne * Q3;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int q = (int)(i % Q3);
+      const int64_t e = i / Q3;
+      double J[3][3];
+      for (int c = 0; c < 3; ++c)
+         for (int d = 0; d < 3; ++d) { J[c][d] = Jg[q + (int64_t)Q3 * (c + 3 * (d + 3 * e))]; }
+      const double w_det = W[q] * det3(J);
+      for (int b = 0; b < 9; ++b)
+      {
+         const double cb = const_c ? C[b] : C[b + 9 * i];
+         D[q + (int64_t)Q3 * (e + (int64_t)ne * b)] = cb * w_det;
+      }
+   }
+}
+
 // VectorMassIntegrator::AssemblePA, 3D (fem/integ/bilininteg_vecmass_pa.cpp:
 // 119-160), scalar or vector coefficient: D(q, k, e) = C(k, q, e) W(q) detJ,
 // layout (Q^3, coeff_vdim, NE).
@@ -439,7 +499,8 @@ extern "C" int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, in
                                              const double *W, const double *J, const double *C, int64_t c_size,
                                              double *D)
 {
-   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim))
+   const bool matrix = vdim == 3 && coeff_vdim == 9;
+   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim && !matrix))
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
@@ -448,6 +509,12 @@ extern "C" int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, in
    if (ne == 0) { return GBPA_SUCCESS; }
    if (!W || !J || !C || !D) { return GBPA_ERR_INVALID_ARGUMENT; }
    const int64_t n = (int64_t)ne * Q3;
+   if (matrix)
+   {
+      vector_diffusion_setup_matrix_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, W, J, C,
+                                                                                     c_size == 9 ? 1 : 0, D);
+      return last_launch(ctx, "vector_diffusion_setup_matrix");
+   }
    vector_diffusion_setup_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, vdim, coeff_vdim, W, J, C,
                                                                             c_size == coeff_vdim ? 1 : 0, D);
    return last_launch(ctx, "vector_diffusion_setup");
@@ -456,7 +523,8 @@ extern "C" int gbpa_vector_diffusion_setup3d(gbpa_ctx_t ctx, int ne, int q1d, in
 extern "C" int gbpa_vector_mass_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdim, int coeff_vdim, const double *W,
                                         const double *J, const double *C, int64_t c_size, double *D)
 {
-   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim))
+   const bool matrix = vdim == 3 && coeff_vdim == 9;
+   if (!ctx || ne < 0 || q1d < 1 || vdim < 1 || vdim > 3 || (coeff_vdim != 1 && coeff_vdim != vdim && !matrix))
    {
       return GBPA_ERR_INVALID_ARGUMENT;
    }
@@ -465,6 +533,12 @@ extern "C" int gbpa_vector_mass_setup3d(gbpa_ctx_t ctx, int ne, int q1d, int vdi
    if (ne == 0) { return GBPA_SUCCESS; }
    if (!W || !J || !C || !D) { return GBPA_ERR_INVALID_ARGUMENT; }
    const int64_t n = (int64_t)ne * Q3;
+   if (matrix)
+   {
+      vector_mass_setup_matrix_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, W, J, C,
+                                                                                c_size == 9 ? 1 : 0, D);
+      return last_launch(ctx, "vector_mass_setup_matrix");
+   }
    vector_mass_setup_kernel<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ne, Q3, coeff_vdim, W, J, C,
                                                                        c_size == coeff_vdim ? 1 : 0, D);
    return last_launch(ctx, "vector_mass_setup");

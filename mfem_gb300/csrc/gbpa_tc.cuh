@@ -1,0 +1,35 @@
+// Tensor-core (tcgen05) FP32 diffusion apply: tables and launcher
+// (gbpa_apply_tc.cu).
+#pragma once
+#include "gbpa_internal.cuh"
+
+namespace gbpa
+{
+namespace tc
+{
+// The Kronecker matrix of one (D, Q) pair, split into fp16 limbs and laid out
+// per chunk for the tensor cores (forward and backward operands), in device
+// memory; R is the largest absolute row sum of the matrix (the bound behind
+// the per-element output scale).
+struct Tables
+{
+   unsigned char *fwd = nullptr, *bwd = nullptr;
+   double R = 0.0;
+   int D = 0, Q = 0;
+};
+// (D, Q) pairs with a tensor-core kernel.
+bool supported(int D, int Q);
+// B, G: host (Q, D) column-major tables in FP64.
+int build_tables(int D, int Q, const double *B, const double *G, Tables *t);
+void free_tables(Tables *t);
+// Per-element power-of-two scale of the pointwise output (one float each).
+int launch_qscale(gbpa_ctx *ctx, int ne, int Q, const float *qd, float R, float *qscale);
+// y = A_e R x with the gather fused (mode as for the other element kernels:
+// 0 E-vector out, 1 accumulate, GBPA_OUT_ATOMIC L-vector). Symmetric qdata
+// (Q^3, 6, NE) in FP32. skip: optional device flag; nonzero skips the launch
+// (a solver that has converged inside a captured graph).
+int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, const float *qd,
+                         const float *qscale, const float *x, const int *gmap, const unsigned char *mask,
+                         float *y, int mode, const int *skip = nullptr);
+} // namespace tc
+} // namespace gbpa

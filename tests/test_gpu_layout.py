@@ -129,7 +129,8 @@ def test_layout_arguments_validated():
     from tests.gpu_util import dev
     d = dev()
     assert d.lib.gbpa_set_apply_layout(2, 0, 4, 5, 1, 1) == -1      # unknown kind
-    assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 2, 1) == -1      # unknown layout
+    assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 3, 1) == -1      # unknown layout
+    assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 2, 1) == -2      # tensor-core layout: FP32 only
     assert d.lib.gbpa_set_apply_layout(0, 0, 4, 5, 1, 0) == -1      # nbz < 1
     assert d.lib.gbpa_set_apply_layout(0, 0, 9, 10, 1, 2) == -1     # 2000 threads
     assert d.lib.gbpa_set_apply_layout(0, 0, 2, 3, 1, 30) == -1     # blockDim.z = 90 > 64

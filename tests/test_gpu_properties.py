@@ -3,6 +3,7 @@ cases the reference handles, and failure reporting without any GPU fault
 (poisoned inputs on the host; the library must return a status and the
 context must stay usable)."""
 import ctypes
+import math
 
 import numpy as np
 import pytest

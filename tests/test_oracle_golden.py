@@ -211,3 +211,37 @@ def test_markers_oracle_all_and_none_marked(oracle):
     part = sum(oracle.pa_mult_markers(*args, attr, m, g["x"]) for m in ([1, 0, 0], [0, 1, 0], [0, 0, 1]))
     assert np.linalg.norm(part - full) / np.linalg.norm(full) < 1e-14
     assert np.allclose(full, g["y_diff"], rtol=0, atol=1e-12 * np.abs(g["y_diff"]).max())
+
+
+MATRIX_MAP = [0, 3, 6, 1, 4, 7, 2, 5, 8]
+
+
+def test_vector_matrix_coefficient_componentwise(oracle):
+    """VectorDiffusionIntegrator / VectorMassIntegrator PA with a matrix
+    coefficient (components coupled through it) is the sum of scalar
+    operators, one per coefficient entry: diffusion block b = j + 3 i (source
+    i, destination j) with coefficient entry map[b]
+    (fem/integ/bilininteg_vecdiffusion_pa.cpp:213-272, .hpp:96-163); mass
+    block 3 c + d (source d, destination c) with entry 3 c + d
+    (fem/integ/bilininteg_vecmass_pa.cpp:119-160, .hpp:157-170). The scalar
+    oracle composed this way reproduces the reference's vector E-vectors."""
+    g = load_golden("jit2_p2_nonsym")
+    ne, ndofs, D, Q = (int(v) for v in g["meta"][:4])
+    Q3, D3 = Q ** 3, D ** 3
+    C = np.asarray(g["vmat_coeff"]).reshape(ne * Q3, 9)
+    xE = np.asarray(g["vec_xE"]).reshape(ne, 3, D3)
+    y = np.zeros((ne, 3, D3))
+    ym = np.zeros((ne, 3, D3))
+    for i in range(3):
+        xi = np.ascontiguousarray(xE[:, i, :]).reshape(-1)
+        for j in range(3):
+            b = j + 3 * i
+            qd = oracle.diffusion_setup3d(ne, Q, 1, g["W"], g["J"], np.ascontiguousarray(C[:, MATRIX_MAP[b]]))
+            y[:, j, :] += oracle.diffusion_apply3d(ne, True, D, Q, g["B"], g["G"], qd, xi).reshape(ne, D3)
+            bm = 3 * j + i
+            qm = oracle.mass_setup3d(ne, Q3, g["W"], g["detJ"], np.ascontiguousarray(C[:, bm]))
+            ym[:, j, :] += oracle.mass_apply3d(ne, D, Q, g["B"], qm, xi).reshape(ne, D3)
+    ref = np.asarray(g["vmat_yE"])
+    assert np.linalg.norm(y.reshape(-1) - ref) / np.linalg.norm(ref) < 1e-13
+    refm = np.asarray(g["vmatmass_yE"])
+    assert np.linalg.norm(ym.reshape(-1) - refm) / np.linalg.norm(refm) < 1e-13
