@@ -26,10 +26,13 @@
 // float per element, computed at operator creation). Both scales are undone
 // exactly in the output.
 //
-// Shared-memory operands use the K-major, no-swizzle canonical layout:
-// 8 x 8 fp16 core matrices of 128 contiguous bytes, core (row group rg,
-// k group kg) at byte (kg * rows/8 + rg) * 128 (LBO = rows/8 * 128 between
-// K-adjacent cores, SBO = 128 between row groups).
+// Shared-memory operands use the no-swizzle canonical layouts: 8 x 8 fp16
+// core matrices of 128 contiguous bytes. K-major (x, O, the forward table):
+// core (row group rg, k group kg) at byte (kg * rows/8 + rg) * 128, LBO =
+// rows/8 * 128 between K-adjacent cores, SBO = 128 between row groups. The
+// backward GEMM reads the forward table chunk as MN-major (N = dofs
+// contiguous in each 16-byte row): LBO = 128 between K-adjacent cores (chunk
+// columns), SBO = NC/8 * 128 between N-adjacent cores.
 #include "gbpa_apply_kernels.cuh"
 #include "gbpa_dispatch.cuh"
 #include "gbpa_tc.cuh"
@@ -42,30 +45,67 @@ namespace gbpa
 namespace tc
 {
 
+// Timeline probes for kernel development: compiled in only with
+// -DGBPA_TC_TRACE (SM clock of CTA 0's first tiles into a device table).
+#ifdef GBPA_TC_TRACE
+__device__ unsigned long long g_tc_trace[2048];
+#define TC_TRACE(it, i)                                                           \
+   do                                                                             \
+   {                                                                              \
+      if (blockIdx.x == 0 && (it) < 2) { g_tc_trace[(it) * 1024 + (i)] = clock64(); } \
+   } while (0)
+#else
+#define TC_TRACE(it, i) do { } while (0)
+#endif
+
 template <int D, int Q, int PC>
 struct Shape
 {
    static constexpr int D3 = D * D * D;
    static constexpr int KF = (D3 + 15) / 16 * 16;   // dofs, padded to the MMA K step
+   static constexpr int KH = KF / 2;                // dofs per half row
    static constexpr int Q3 = Q * Q * Q;
    static constexpr int NC = 3 * PC;                // chunk columns (points x 3 components)
    static constexpr int NCH = (Q3 + PC - 1) / PC;   // chunks
+   static constexpr int NP = PC / 2;                // points of a chunk per thread (two halves per row)
+   static constexpr int NV = 3 * NP;                // chunk columns per thread
+   static constexpr int NQ = 6 * NP;                // qdata values per thread and chunk
    static constexpr int M = 128;                    // elements per tile
    static constexpr int A_LIMB = M * KF * 2;        // bytes of one fp16 limb of the x tile
    static constexpr int BF_LIMB = NC * KF * 2;      // one limb of a forward table chunk
-   static constexpr int BB_LIMB = KF * NC * 2;      // one limb of a backward table chunk
    static constexpr int AB_LIMB = M * NC * 2;       // one limb of the chunk's O columns
+   static constexpr int MAP_BYTES = M * D3 * 4;     // the tile's gather map
+   // a ring of NT table-chunk buffers (chunk c in buffer c % NT; the forward
+   // GEMM reads a chunk K-major, the backward GEMM reads the same bytes as an
+   // MN-major operand), the chunk's O columns and the chunk's qdata
+   // (bulk-copied one chunk ahead). The tile's gather map is staged over the
+   // second and third table buffers and the O columns, which are free while
+   // the map is read (before the tile's first MMA).
+   static constexpr int NT = 3;
+   static constexpr int QD_BYTES = 2 * NQ * M * 4;  // one tile-chunk of transposed qdata
    static constexpr int OFF_AF = 0;
-   static constexpr int OFF_BF = OFF_AF + 2 * A_LIMB;
-   static constexpr int OFF_BB = OFF_BF + 2 * BF_LIMB;
-   static constexpr int OFF_AB = OFF_BB + 2 * BB_LIMB;
-   static constexpr int SMEM = OFF_AB + 2 * AB_LIMB;
-   static constexpr int STG = D3 | 1;               // staging row stride (odd: no bank conflicts)
-   static constexpr int OFF_STG = OFF_BB;           // staging reuses the chunk buffers
-   static constexpr int TF = 0, TB = 128;           // TMEM columns of the two accumulators
-   static_assert(KF <= 128 && NC <= 128 && NC % 16 == 0, "accumulators must fit 128 TMEM columns");
-   static_assert(OFF_STG + M * STG * 4 <= SMEM, "staging must fit in the chunk buffers");
+   static constexpr int OFF_T = OFF_AF + 2 * A_LIMB;
+   static constexpr int OFF_AB = OFF_T + NT * 2 * BF_LIMB;
+   static constexpr int OFF_QD = OFF_AB + 2 * AB_LIMB;
+   static constexpr int OFF_MAP = OFF_T + 2 * BF_LIMB;
+   static constexpr int SMEM = OFF_QD + QD_BYTES;
+   static __device__ __forceinline__ int off_t(int c) { return OFF_T + (c % NT) * 2 * BF_LIMB; }
+   // output staging in the x tile's buffer: row stride D3; an even stride is
+   // XOR-swizzled by the row (bank-conflict-free either way)
+   static constexpr int STG = D3;
+   static_assert(D3 % 2 == 1 || D3 % 32 == 0, "staging swizzle");
+   static __device__ __forceinline__ int stg(int row, int i)
+   {
+      return row * STG + (D3 % 2 ? i : (i ^ (row & 31)));
+   }
+   static constexpr int TF0 = 0, TF1 = 64, TB = 128;   // TMEM columns: two forward buffers, the result
+   static constexpr int QT_CHUNK = 2 * NQ * M;      // floats of one tile-chunk of transposed qdata
+   static_assert(KF <= 128 && NC <= 64 && NC % 16 == 0 && NV % 8 == 0, "TMEM and MMA shapes");
+   static_assert(M * STG * 4 <= 2 * A_LIMB, "output staging must fit in the x tile");
    static_assert(SMEM <= 220 * 1024, "shared memory");
+   static_assert(MAP_BYTES % 16 == 0, "bulk copy size");
+   static_assert(OFF_MAP + MAP_BYTES <= OFF_QD, "map staging must fit over the chunk buffers");
+   static_assert(NCH >= NT, "the table ring is filled at the tile start");
 };
 
 __device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsigned sbo)
@@ -77,10 +117,11 @@ __device__ __forceinline__ uint64_t smem_desc(unsigned saddr, unsigned lbo, unsi
    return d;                 // base offset 0, no swizzle
 }
 
-// instruction descriptor, kind::f16: fp16 A and B (K-major), FP32 accumulate
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N)
+// instruction descriptor, kind::f16: fp16 A (K-major) and B (K-major, or
+// MN-major with b_mn), FP32 accumulate
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N, bool b_mn = false)
 {
-   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+   return (1u << 4) | (b_mn ? (1u << 16) : 0u) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_f16(unsigned dtmem, uint64_t da, uint64_t db, uint32_t idesc, bool acc)
@@ -93,6 +134,14 @@ __device__ __forceinline__ void mma_commit(unsigned long long *bar)
 {
    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                 ::"r"(smem_u32(bar)) : "memory");
+}
+// one lane of a converged warp (the lane that issues single-thread
+// tcgen05 instructions while the whole warp keeps their operands uniform)
+__device__ __forceinline__ bool elect_one()
+{
+   unsigned pred = 0;
+   asm volatile("{\n .reg .pred p;\n elect.sync _|p, 0xffffffff;\n selp.u32 %0, 1, 0, p;\n}" : "=r"(pred));
+   return pred != 0;
 }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -115,6 +164,11 @@ __device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned by
 {
    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                 : "memory");
+}
+// start bringing a global range into L2 (no completion to wait for)
+__device__ __forceinline__ void bulk_prefetch_l2(const void *gsrc, unsigned bytes)
+{
+   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(gsrc), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned bytes, unsigned long long *bar)
 {
@@ -140,37 +194,47 @@ __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
    lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Persistent kernel: one 256-thread CTA per SM walks tiles of 128 elements.
-// Thread t: element row r = 32 (warp % 4) + lane (its TMEM lane), half
-// h = warp / 4 (the two halves share a row and split its columns). Thread 0
-// issues the bulk copies and the MMAs. Every wait is bounded: on expiry the
-// tile's outputs are NaN and GBPA_FLAG_TIMEOUT is raised, and the control flow
-// (barriers) stays uniform.
+// Persistent kernel: one CTA per SM walks tiles of 128 elements. Warps 0-7
+// (256 threads) gather, split, apply the qdata and write the result: thread t
+// owns element row r = 32 (warp % 4) + lane (its TMEM lane) and half
+// h = warp / 4 of that row's columns. One thread of warp 8 issues the MMAs,
+// one thread of warp 9 the bulk copies (gather map, table and qdata chunks),
+// each waiting only for what it needs. The tensor pipe
+// runs forward(c + 1) while the CUDA cores apply the qdata of chunk c, and
+// backward(c) while they start chunk c + 1 (two forward accumulators in TMEM).
+// Every wait is bounded: after a first expiry no wait blocks, the tile's
+// outputs are NaN and GBPA_FLAG_TIMEOUT is raised.
 template <int D, int Q, int PC>
-__global__ void __launch_bounds__(256, 1)
-diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f, const unsigned char *__restrict__ tab_b,
-                    const float *__restrict__ qd, const float *__restrict__ qscale, const float *__restrict__ x,
-                    const int *__restrict__ gmap, const unsigned char *__restrict__ mask, float *__restrict__ y,
-                    int mode, const int *__restrict__ skip, int *flags)
+__global__ void __launch_bounds__(320, 1)
+diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
+                    const float *__restrict__ qT, const float *__restrict__ qscale, const float *__restrict__ x,
+                    const int *__restrict__ gmap, int map_bulk, const unsigned char *__restrict__ mask,
+                    float *__restrict__ y, int mode, const int *__restrict__ skip, int *flags)
 {
    using S = Shape<D, Q, PC>;
    if (skip && *skip) { return; }   // uniform per launch: the solver has finished
    extern __shared__ __align__(1024) unsigned char smem[];
-   __shared__ __align__(8) unsigned long long bar_load, bar_mma;
+   // mbarriers: map, table ring 0-2, qd (bulk copies); af, ab, dfree0/1,
+   // qfree (256 epilogue arrivals); fwd0/1, bwd (MMA commits)
+   __shared__ __align__(8) unsigned long long mb[13];
    __shared__ unsigned tmem_base;
    __shared__ float s_max[2][128];
-   __shared__ float s_sx[128], s_so[128];
    __shared__ int s_fail;
+   unsigned long long *MB_MAP = mb, *MB_T = mb + 1, *MB_QD = mb + 4, *MB_AF = mb + 5;
+   unsigned long long *MB_AB = mb + 6, *MB_DFREE = mb + 7, *MB_QFREE = mb + 9, *MB_FWD = mb + 10;
+   unsigned long long *MB_BWD = mb + 12;
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int half = warp >> 2;
+   const int half = (warp >> 2) & 1;
    const int r = 32 * (warp & 3) + lane;
    const unsigned sbase = smem_u32(smem);
-   float *stg = reinterpret_cast<float *>(smem + S::OFF_STG);
 
    if (tid == 0)
    {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar_load)) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar_mma)) : "memory");
+      const unsigned counts[13] = {1, 1, 1, 1, 1, 256, 256, 256, 256, 256, 1, 1, 1};
+      for (int i = 0; i < 13; ++i)
+      {
+         asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb + i)), "r"(counts[i]) : "memory");
+      }
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
       s_fail = 0;
    }
@@ -184,209 +248,338 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f, const unsig
    __syncthreads();
    fence_after();
    const unsigned tmem = tmem_base;
-   const unsigned lane_off = (unsigned)(32 * (warp & 3)) << 16;
-   // bounded wait; after a first expiry no later wait blocks (the kernel
-   // then runs to its end quickly, writing NaN)
    volatile int *fail = &s_fail;
    auto wait = [&](unsigned long long *bar, unsigned ph) {
       if (*fail) { return; }
       if (!mbar_wait(bar, ph, 1LL << 20)) { *fail = 1; }
    };
-   unsigned ph_load = 0, ph_mma = 0;
-   constexpr uint32_t ID_F = instr_desc(128, S::NC), ID_B = instr_desc(128, S::KF);
-   constexpr unsigned LBO_A = 16 * 128, LBO_BF = S::NC / 8 * 128, LBO_BB = S::KF / 8 * 128;
+   auto arrive = [&](unsigned long long *bar) {
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+   };
    const int ntiles = (ne + 127) / 128;
 
-   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+   if (warp == 8)
    {
-      const long long e0 = (long long)tile * 128;
-      // ---- gather the tile's x (ElementRestriction::Mult, signed map) into staging
-      for (int s = tid; s < 128 * S::D3; s += 256)
+      // ----------------------------------------------------- MMA issuer
+      // the whole warp runs the loop (waits, descriptors: warp-uniform);
+      // one elected lane issues each batch of MMAs and its commit
       {
-         const int el = s / S::D3, i = s - el * S::D3;
-         const long long e = e0 + el;
-         float v = 0.f;
-         if (e < ne)
+         constexpr uint32_t ID_F = instr_desc(128, S::NC), ID_B = instr_desc(128, S::KF, true);
+         constexpr unsigned LBO_A = 16 * 128, LBO_BF = S::NC / 8 * 128;
+         // descriptors of the first K step; a step advances the start
+         // address field (bits 0-13, 16-byte units)
+         const uint64_t af_hi = smem_desc(sbase + S::OFF_AF, LBO_A, 128);
+         const uint64_t af_lo = smem_desc(sbase + S::OFF_AF + S::A_LIMB, LBO_A, 128);
+         const uint64_t ab_hi = smem_desc(sbase + S::OFF_AB, LBO_A, 128);
+         const uint64_t ab_lo = smem_desc(sbase + S::OFF_AB + S::AB_LIMB, LBO_A, 128);
+         // table ring buffer k: + k * 2 BF_LIMB bytes
+         const uint64_t tf_hi = smem_desc(sbase + S::OFF_T, LBO_BF, 128);
+         const uint64_t tf_lo = smem_desc(sbase + S::OFF_T + S::BF_LIMB, LBO_BF, 128);
+         const uint64_t tb_hi = smem_desc(sbase + S::OFF_T, 128, LBO_BF);
+         const uint64_t tb_lo = smem_desc(sbase + S::OFF_T + S::BF_LIMB, 128, LBO_BF);
+         auto ring = [](int c) { return (uint64_t)((c % S::NT) * 2 * S::BF_LIMB >> 4); };
+         unsigned ph_t[S::NT] = {}, ph_af = 0, ph_ab = 0, ph_dfree[2] = {0, 0};
+         int it = 0;
+         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
          {
-            const int g = __ldg(gmap + e * S::D3 + i);
-            if (g != GBPA_GATHER_SKIP)
+            if (lane == 0) TC_TRACE(it, 1000);
+            wait(MB_AF, ph_af); ph_af ^= 1;
+            if (lane == 0) TC_TRACE(it, 1001);
+            for (int c = 0; c <= S::NCH; ++c)
             {
-               const int j = g >= 0 ? g : -1 - g;
-               if (!(mask && __ldg(mask + j)))
+               if (c < S::NCH)
                {
-                  v = __ldg(x + j);
-                  if (g < 0) { v = -v; }
+                  wait(MB_T + c % S::NT, ph_t[c % S::NT]); ph_t[c % S::NT] ^= 1;
+                  if (c >= 2) { wait(MB_DFREE + (c & 1), ph_dfree[c & 1]); ph_dfree[c & 1] ^= 1; }
+                  fence_after();
+                  if (lane == 0) TC_TRACE(it, 16 * c + 0);
+                  // forward: Gq = X K^T over the KF dofs, three limb products
+                  const unsigned d = tmem + ((c & 1) ? S::TF1 : S::TF0);
+                  const uint64_t bh = tf_hi + ring(c), bl = tf_lo + ring(c);
+                  __syncwarp();
+                  if (elect_one())
+                  {
+#pragma unroll
+                     for (int st = 0; st < S::KF / 16; ++st)
+                     {
+                        const uint64_t oa = (uint64_t)(st * 2 * LBO_A >> 4), ob = (uint64_t)(st * 2 * LBO_BF >> 4);
+                        mma_f16(d, af_hi + oa, bh + ob, ID_F, st > 0);
+                        mma_f16(d, af_hi + oa, bl + ob, ID_F, true);
+                        mma_f16(d, af_lo + oa, bh + ob, ID_F, true);
+                     }
+                     mma_commit(MB_FWD + (c & 1));
+                  }
+                  __syncwarp();
+               }
+               if (c >= 1)
+               {
+                  if (c == S::NCH)
+                  {
+                     // the epilogue's last two releases of the forward buffers
+                     wait(MB_DFREE + (S::NCH & 1), ph_dfree[S::NCH & 1]); ph_dfree[S::NCH & 1] ^= 1;
+                     wait(MB_DFREE + ((S::NCH - 1) & 1), ph_dfree[(S::NCH - 1) & 1]);
+                     ph_dfree[(S::NCH - 1) & 1] ^= 1;
+                  }
+                  wait(MB_AB, ph_ab); ph_ab ^= 1;
+                  fence_after();
+                  if (lane == 0) TC_TRACE(it, 16 * (c - 1) + 1);
+                  // backward: Y += O K over chunk c - 1's columns (its table
+                  // chunk, still in the ring, read MN-major)
+                  const uint64_t bh = tb_hi + ring(c - 1), bl = tb_lo + ring(c - 1);
+                  __syncwarp();
+                  if (elect_one())
+                  {
+#pragma unroll
+                     for (int st = 0; st < S::NC / 16; ++st)
+                     {
+                        const uint64_t oa = (uint64_t)(st * 2 * LBO_A >> 4), ob = (uint64_t)(st * 2 * 128 >> 4);
+                        mma_f16(tmem + S::TB, ab_hi + oa, bh + ob, ID_B, c > 1 || st > 0);
+                        mma_f16(tmem + S::TB, ab_hi + oa, bl + ob, ID_B, true);
+                        mma_f16(tmem + S::TB, ab_lo + oa, bh + ob, ID_B, true);
+                     }
+                     mma_commit(MB_BWD);
+                  }
+                  __syncwarp();
                }
             }
          }
-         stg[el * S::STG + i] = v;
       }
-      __syncthreads();
+   }
+   else if (warp == 9)
+   {
+      // ---------------------------------------------------- copy producer
+      if (lane == 0)
       {
-         constexpr int H = (S::D3 + 1) / 2;
-         float m = 0.f;
-         for (int i = half * H; i < (half + 1) * H && i < S::D3; ++i) { m = fmaxf(m, fabsf(stg[r * S::STG + i])); }
-         s_max[half][r] = m;
-      }
-      __syncthreads();
-      if (half == 0)
-      {
-         const float m = fmaxf(s_max[0][r], s_max[1][r]);
-         float sx = 1.f;
-         if (m > 0.f && m <= 3.0e38f)
+         unsigned ph_bwd = 0, ph_qfree = 0, ph_af = 0;
+         auto load_t = [&](int c) {
+            mbar_expect(MB_T + c % S::NT, 2 * S::BF_LIMB);
+            bulk_g2s(smem + S::off_t(c), tab_f + (size_t)c * 2 * S::BF_LIMB, 2 * S::BF_LIMB, MB_T + c % S::NT);
+         };
+         auto load_qd = [&](int tile, int c) {
+            mbar_expect(MB_QD, S::QD_BYTES);
+            bulk_g2s(smem + S::OFF_QD, qT + ((size_t)tile * S::NCH + c) * S::QT_CHUNK, S::QD_BYTES, MB_QD);
+         };
+         // qdata streams from HBM: the chunks QPF ahead of the one being
+         // copied to shared memory are on their way into L2, so that copy is
+         // an L2 hit (the next tile's chunks follow this tile's)
+         constexpr int QPF = 3;
+         auto prefetch_qd = [&](int tile, int c) {
+            int t = tile, cc = c;
+            if (cc >= S::NCH) { cc -= S::NCH; t += gridDim.x; }
+            if (t < ntiles) { bulk_prefetch_l2(qT + ((size_t)t * S::NCH + cc) * S::QT_CHUNK, S::QD_BYTES); }
+         };
+         for (int k = 0; k < QPF; ++k) { prefetch_qd(blockIdx.x, k); }
+         int it = 0;
+         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
          {
-            int ex;
-            frexpf(m, &ex);                 // m < 2^ex
-            sx = ldexpf(1.f, 14 - ex);      // m * sx in [2^13, 2^14)
+            const long long e0 = (long long)tile * 128;
+            // the previous tile's MMAs have all completed and its last qdata
+            // chunk was taken (waited below): every target buffer is free
+            if (map_bulk && e0 + 128 <= ne)
+            {
+               mbar_expect(MB_MAP, S::MAP_BYTES);
+               bulk_g2s(smem + S::OFF_MAP, gmap + e0 * S::D3, S::MAP_BYTES, MB_MAP);
+            }
+            load_qd(tile, 0);
+            load_t(0);
+            wait(MB_AF, ph_af); ph_af ^= 1;
+            // the map has been read: the buffers under it are free
+            for (int c = 1; c < S::NT && c < S::NCH; ++c) { load_t(c); }
+            for (int c = 0; c < S::NCH; ++c)
+            {
+               // qdata chunk c + 1 once the epilogue has taken chunk c; table
+               // chunk c + NT - 1 once bwd(c - 1) has freed its buffer
+               wait(MB_QFREE, ph_qfree); ph_qfree ^= 1;
+               if (c + 1 < S::NCH) { load_qd(tile, c + 1); }
+               prefetch_qd(tile, c + QPF);
+               if (c >= 1)
+               {
+                  wait(MB_BWD, ph_bwd); ph_bwd ^= 1;
+                  TC_TRACE(it, 16 * (c - 1) + 4);
+                  if (c + S::NT - 1 < S::NCH) { load_t(c + S::NT - 1); }
+               }
+            }
+            wait(MB_BWD, ph_bwd); ph_bwd ^= 1;   // the tile's last GEMM
+            TC_TRACE(it, 1002);
          }
-         s_sx[r] = sx;
-         s_so[r] = e0 + r < ne ? __ldg(qscale + e0 + r) : 1.f;
       }
-      __syncthreads();
+   }
+   else
+   {
+      // ------------------------------------------------------- epilogue warps
+      const unsigned lane_off = (unsigned)(32 * (warp & 3)) << 16;
+      unsigned ph_map = 0, ph_qd = 0, ph_fwd[2] = {0, 0}, ph_bwd = 0;
+      const int *smap = reinterpret_cast<const int *>(smem + S::OFF_MAP);
+      float *stg = reinterpret_cast<float *>(smem + S::OFF_AF);
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
       {
-         const float sx = s_sx[r];
-         for (int kg = half * (S::KF / 16); kg < (half + 1) * (S::KF / 16); ++kg)
+         const long long e0 = (long long)tile * 128;
+         const long long e = e0 + r;
+         if (tid == 0) { TC_TRACE(it, 1010); }
+         const bool act = e < ne;
+         const bool bulk = map_bulk && e0 + 128 <= ne;
+         // ---- gather this thread's half row of x (ElementRestriction::Mult)
+         if (bulk) { wait(MB_MAP, ph_map); ph_map ^= 1; }
+         // all map entries first, then all x loads (unconditional: a slot
+         // without a dof reads x[0] and is zeroed by the select), so the
+         // loads are in flight together
+         int jj[S::KH];
+         signed char sg[S::KH];
+#pragma unroll
+         for (int k = 0; k < S::KH; ++k)
+         {
+            const int i = half * S::KH + k;
+            int g = GBPA_GATHER_SKIP;
+            if (act && i < S::D3) { g = bulk ? smap[r * S::D3 + i] : __ldg(gmap + e * S::D3 + i); }
+            const bool use = g != GBPA_GATHER_SKIP;
+            jj[k] = use ? (g >= 0 ? g : -1 - g) : 0;
+            sg[k] = use ? (g >= 0 ? 1 : -1) : 0;
+         }
+         if (mask)
+         {
+#pragma unroll
+            for (int k = 0; k < S::KH; ++k)
+            {
+               if (__ldg(mask + jj[k])) { sg[k] = 0; }
+            }
+         }
+         float xv[S::KH];
+#pragma unroll
+         for (int k = 0; k < S::KH; ++k) { xv[k] = __ldg(x + jj[k]); }
+#pragma unroll
+         for (int k = 0; k < S::KH; ++k) { xv[k] = sg[k] == 0 ? 0.f : (sg[k] > 0 ? xv[k] : -xv[k]); }
+         float m = 0.f;
+#pragma unroll
+         for (int k = 0; k < S::KH; ++k) { m = fmaxf(m, fabsf(xv[k])); }
+         s_max[half][r] = m;
+         asm volatile("bar.sync 1, 256;" ::: "memory");
+         float sx = 1.f;
+         {
+            const float mm = fmaxf(s_max[0][r], s_max[1][r]);
+            if (mm > 0.f && mm <= 3.0e38f)
+            {
+               int ex;
+               frexpf(mm, &ex);              // mm < 2^ex
+               sx = ldexpf(1.f, 14 - ex);    // mm * sx in [2^13, 2^14)
+            }
+         }
+         const float so = act ? __ldg(qscale + e) : 1.f;
+#pragma unroll
+         for (int g8 = 0; g8 < S::KH / 8; ++g8)
          {
             float v[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-            {
-               const int k = 8 * kg + j;
-               v[j] = k < S::D3 ? stg[r * S::STG + k] * sx : 0.f;
-            }
+            for (int j = 0; j < 8; ++j) { v[j] = xv[8 * g8 + j] * sx; }
             uint4 hi, lo;
             split8(v, hi, lo);
+            const int kg = half * (S::KH / 8) + g8;
             const int off = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
             *reinterpret_cast<uint4 *>(smem + S::OFF_AF + off) = hi;
             *reinterpret_cast<uint4 *>(smem + S::OFF_AF + S::A_LIMB + off) = lo;
          }
-      }
-      fence_async_smem();
-      __syncthreads();
-
-      const long long e = e0 + r;
-      const bool act = e < ne;
-      const float sx = s_sx[r], so = s_so[r];
-      const float f = so / sx;   // exact: both are powers of two
-      for (int c = 0; c < S::NCH; ++c)
-      {
-         if (tid == 0)
-         {
-            mbar_expect(&bar_load, 2 * S::BF_LIMB + 2 * S::BB_LIMB);
-            bulk_g2s(smem + S::OFF_BF, tab_f + (size_t)c * 2 * S::BF_LIMB, 2 * S::BF_LIMB, &bar_load);
-            bulk_g2s(smem + S::OFF_BB, tab_b + (size_t)c * 2 * S::BB_LIMB, 2 * S::BB_LIMB, &bar_load);
-            wait(&bar_load, ph_load);
-            fence_after();
-            // forward: Gq = X K^T over the KF dofs, three limb products
-#pragma unroll 1
-            for (int s = 0; s < S::KF / 16; ++s)
-            {
-               const unsigned a0 = sbase + S::OFF_AF + s * 2 * LBO_A;
-               const unsigned b0 = sbase + S::OFF_BF + s * 2 * LBO_BF;
-               const uint64_t ahi = smem_desc(a0, LBO_A, 128), alo = smem_desc(a0 + S::A_LIMB, LBO_A, 128);
-               const uint64_t bhi = smem_desc(b0, LBO_BF, 128), blo = smem_desc(b0 + S::BF_LIMB, LBO_BF, 128);
-               mma_f16(tmem + S::TF, ahi, bhi, ID_F, s > 0);
-               mma_f16(tmem + S::TF, ahi, blo, ID_F, true);
-               mma_f16(tmem + S::TF, alo, bhi, ID_F, true);
-            }
-            mma_commit(&bar_mma);
-         }
-         ph_load ^= 1;
-         wait(&bar_mma, ph_mma);
-         ph_mma ^= 1;
-         fence_after();
-         // pointwise: this thread's PC/2 points of the chunk
-         constexpr int NP = PC / 2, NV = 3 * NP;
-         float gq[NV], o[NV];
-#pragma unroll
-         for (int j = 0; j < NV; j += 8)
-         {
-            tmem_ld8(tmem + lane_off + S::TF + half * NV + j, gq + j);
-         }
-         tmem_wait_ld();
-#pragma unroll
-         for (int p = 0; p < NP; ++p)
-         {
-            const int q = c * PC + half * NP + p;
-            float O11 = 0.f, O12 = 0.f, O13 = 0.f, O22 = 0.f, O23 = 0.f, O33 = 0.f;
-            if (act && q < S::Q3)
-            {
-               const float *qe = qd + e * 6 * S::Q3 + q;
-               O11 = __ldg(qe); O12 = __ldg(qe + S::Q3); O13 = __ldg(qe + 2 * S::Q3);
-               O22 = __ldg(qe + 3 * S::Q3); O23 = __ldg(qe + 4 * S::Q3); O33 = __ldg(qe + 5 * S::Q3);
-            }
-            const float gx = gq[3 * p], gy = gq[3 * p + 1], gz = gq[3 * p + 2];
-            o[3 * p] = (O11 * gx + O12 * gy + O13 * gz) * f;
-            o[3 * p + 1] = (O12 * gx + O22 * gy + O23 * gz) * f;
-            o[3 * p + 2] = (O13 * gx + O23 * gy + O33 * gz) * f;
-         }
-#pragma unroll
-         for (int jg = 0; jg < NV / 8; ++jg)
-         {
-            uint4 hi, lo;
-            split8(o + 8 * jg, hi, lo);
-            const int kg = half * (NV / 8) + jg;
-            const int off = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
-            *reinterpret_cast<uint4 *>(smem + S::OFF_AB + off) = hi;
-            *reinterpret_cast<uint4 *>(smem + S::OFF_AB + S::AB_LIMB + off) = lo;
-         }
          fence_async_smem();
-         fence_before();
-         __syncthreads();
-         if (tid == 0)
-         {
-            fence_after();
-            // backward: Y += O K over the chunk's columns
+         if (tid == 0) { TC_TRACE(it, 1011); }
+         arrive(MB_AF);
+
+         // ---- chunks: the producer bulk-copies chunk c's qdata (transposed
+         // layout: this thread's 6 NP values at stride 128) into shared memory
+         // one chunk ahead; it is taken into registers at the chunk's start
+         const float *sq = reinterpret_cast<const float *>(smem + S::OFF_QD) + half * S::NQ * 128 + r;
 #pragma unroll 1
-            for (int s = 0; s < S::NC / 16; ++s)
-            {
-               const unsigned a0 = sbase + S::OFF_AB + s * 2 * LBO_A;
-               const unsigned b0 = sbase + S::OFF_BB + s * 2 * LBO_BB;
-               const uint64_t ahi = smem_desc(a0, LBO_A, 128), alo = smem_desc(a0 + S::AB_LIMB, LBO_A, 128);
-               const uint64_t bhi = smem_desc(b0, LBO_BB, 128), blo = smem_desc(b0 + S::BB_LIMB, LBO_BB, 128);
-               mma_f16(tmem + S::TB, ahi, bhi, ID_B, c > 0 || s > 0);
-               mma_f16(tmem + S::TB, ahi, blo, ID_B, true);
-               mma_f16(tmem + S::TB, alo, bhi, ID_B, true);
-            }
-            mma_commit(&bar_mma);
-         }
-         wait(&bar_mma, ph_mma);
-         ph_mma ^= 1;
-         fence_after();
-      }
-      // ---- result: undo the output scale (the x scale was undone in the
-      // pointwise factor f), stage, store the tile contiguously
-      {
-         const float inv = 1.f / so;
-         constexpr int NH = S::KF / 2;
+         for (int c = 0; c < S::NCH; ++c)
+         {
+            wait(MB_QD, ph_qd); ph_qd ^= 1;
+            if (tid == 0) { TC_TRACE(it, 16 * c + 5); }
+            float qc[S::NQ];
 #pragma unroll
-         for (int j = 0; j < NH; j += 8)
+            for (int k = 0; k < S::NQ; ++k) { qc[k] = sq[k * 128]; }
+            fence_async_smem();
+            arrive(MB_QFREE);
+            wait(MB_FWD + (c & 1), ph_fwd[c & 1]); ph_fwd[c & 1] ^= 1;
+            if (tid == 0) { TC_TRACE(it, 16 * c + 6); }
+            fence_after();
+            float gq[S::NV];
+            const unsigned tcol = tmem + lane_off + ((c & 1) ? S::TF1 : S::TF0) + half * S::NV;
+#pragma unroll
+            for (int j = 0; j < S::NV; j += 8) { tmem_ld8(tcol + j, gq + j); }
+            tmem_wait_ld();
+            fence_before();
+            arrive(MB_DFREE + (c & 1));
+            float o[S::NV];
+#pragma unroll
+            for (int p = 0; p < S::NP; ++p)
+            {
+               // qdata entries 11, 12, 13, 22, 23, 33 of point p
+               const float O11 = qc[6 * p], O12 = qc[6 * p + 1], O13 = qc[6 * p + 2];
+               const float O22 = qc[6 * p + 3], O23 = qc[6 * p + 4], O33 = qc[6 * p + 5];
+               const float gx = gq[3 * p], gy = gq[3 * p + 1], gz = gq[3 * p + 2];
+               // the x scale stays in (undone at the output): |o so| < 2^14
+               o[3 * p] = (O11 * gx + O12 * gy + O13 * gz) * so;
+               o[3 * p + 1] = (O12 * gx + O22 * gy + O23 * gz) * so;
+               o[3 * p + 2] = (O13 * gx + O23 * gy + O33 * gz) * so;
+            }
+            if (tid == 0) { TC_TRACE(it, 16 * c + 7); }
+            if (c >= 1) { wait(MB_BWD, ph_bwd); ph_bwd ^= 1; }   // backward(c - 1) has read A_bwd
+            if (tid == 0) { TC_TRACE(it, 16 * c + 8); }
+#pragma unroll
+            for (int jg = 0; jg < S::NV / 8; ++jg)
+            {
+               uint4 hi, lo;
+               split8(o + 8 * jg, hi, lo);
+               const int kg = half * (S::NV / 8) + jg;
+               const int off = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
+               *reinterpret_cast<uint4 *>(smem + S::OFF_AB + off) = hi;
+               *reinterpret_cast<uint4 *>(smem + S::OFF_AB + S::AB_LIMB + off) = lo;
+            }
+            fence_async_smem();
+            arrive(MB_AB);
+            if (tid == 0) { TC_TRACE(it, 16 * c + 9); }
+         }
+         // ---- result: D_bwd = (A_e x) sx so; undo the scales, stage, store
+         wait(MB_BWD, ph_bwd); ph_bwd ^= 1;
+         if (tid == 0) { TC_TRACE(it, 1013); }
+         fence_after();
+         const float inv = 1.f / (sx * so);
+#pragma unroll
+         for (int j = 0; j < S::KH; j += 8)
          {
             float v[8];
-            tmem_ld8(tmem + lane_off + S::TB + half * NH + j, v);
+            tmem_ld8(tmem + lane_off + S::TB + half * S::KH + j, v);
             tmem_wait_ld();
 #pragma unroll
             for (int k = 0; k < 8; ++k)
             {
-               const int i = half * NH + j + k;
-               if (i < S::D3) { stg[r * S::STG + i] = v[k] * inv; }
+               const int i = half * S::KH + j + k;
+               if (i < S::D3) { stg[S::stg(r, i)] = v[k] * inv; }
             }
          }
+         fence_before();
+         asm volatile("bar.sync 1, 256;" ::: "memory");
+         const bool failed = *fail != 0;
+         if (S::D3 % 2 == 1 && mode == 0 && !failed && e0 + 128 <= ne && ((uintptr_t)y % 16) == 0)
+         {
+            // an unswizzled full tile is the contiguous E-vector slice
+            const float4 *src = reinterpret_cast<const float4 *>(stg);
+            float4 *dst = reinterpret_cast<float4 *>(y + e0 * S::D3);
+            for (int s = tid; s < 128 * S::D3 / 4; s += 256) { dst[s] = src[s]; }
+         }
+         else
+         for (int s = tid; s < 128 * S::D3; s += 256)
+         {
+            const int el = s / S::D3, i = s - el * S::D3;
+            const long long ee = e0 + el;
+            if (ee >= ne) { continue; }
+            const float v = failed ? NAN : stg[S::stg(el, i)];
+            const long long slot = ee * S::D3 + i;
+            store_result(y, slot, slot, v, mode, gmap, mask);
+         }
+         // staging (the x tile's buffer) is rewritten by the next tile's split
+         asm volatile("bar.sync 1, 256;" ::: "memory");
+         if (tid == 0) { TC_TRACE(it, 1012); }
       }
-      fence_before();
-      __syncthreads();
-      const bool failed = s_fail != 0;
-      for (int s = tid; s < 128 * S::D3; s += 256)
-      {
-         const int el = s / S::D3, i = s - el * S::D3;
-         const long long ee = e0 + el;
-         if (ee >= ne) { continue; }
-         const float v = failed ? NAN : stg[el * S::STG + i];
-         const long long slot = ee * S::D3 + i;
-         store_result(y, slot, slot, v, mode, gmap, mask);
-      }
-      __syncthreads();
    }
+   __syncthreads();
    if (tid == 0 && s_fail) { atomicOr(flags, GBPA_FLAG_TIMEOUT); }
    fence_before();
    __syncthreads();
@@ -398,8 +591,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f, const unsig
 
 // ------------------------------------------------------------- host side
 template <int D, int Q, int PC>
-static void build_tables_t(const double *B, const double *G, std::vector<unsigned char> &tf,
-                           std::vector<unsigned char> &tb, double &R)
+static void build_tables_t(const double *B, const double *G, std::vector<unsigned char> &tf, double &R)
 {
    using S = Shape<D, Q, PC>;
    const int NR = S::NCH * S::NC;                  // Kronecker rows, padded to whole chunks
@@ -426,7 +618,6 @@ static void build_tables_t(const double *B, const double *G, std::vector<unsigne
       R = fmax(R, s);
    }
    tf.assign((size_t)S::NCH * 2 * S::BF_LIMB, 0);
-   tb.assign((size_t)S::NCH * 2 * S::BB_LIMB, 0);
    auto put = [](unsigned char *base, size_t byte, double v, int limb) {
       const __half h = __double2half(v);
       const __half l = __double2half(v - (double)__half2float(h));
@@ -443,19 +634,17 @@ static void build_tables_t(const double *B, const double *G, std::vector<unsigne
             const double v = K[(size_t)(c * S::NC + j) * S::KF + i];
             for (int limb = 0; limb < 2; ++limb)
             {
-               // forward chunk: rows j (N), K = i
+               // chunk rows j, K = i (K-major for the forward GEMM; the
+               // backward GEMM reads the same bytes MN-major)
                unsigned char *bf = tf.data() + (size_t)c * 2 * S::BF_LIMB + limb * S::BF_LIMB;
                put(bf, (size_t)((i / 8) * (S::NC / 8) + j / 8) * 128 + (j % 8) * 16 + (i % 8) * 2, v, limb);
-               // backward chunk: rows i (N), K = j
-               unsigned char *bb = tb.data() + (size_t)c * 2 * S::BB_LIMB + limb * S::BB_LIMB;
-               put(bb, (size_t)((j / 8) * (S::KF / 8) + i / 8) * 128 + (i % 8) * 16 + (j % 8) * 2, v, limb);
             }
          }
       }
    }
 }
 
-#define GBPA_TC_LIST(X) X(3, 4, 32) X(4, 5, 32) X(5, 6, 32)
+#define GBPA_TC_LIST(X) X(3, 4, 16) X(4, 5, 16) X(5, 6, 16)
 
 bool supported(int D, int Q)
 {
@@ -467,27 +656,25 @@ bool supported(int D, int Q)
 
 int build_tables(int D, int Q, const double *B, const double *G, Tables *t)
 {
-   std::vector<unsigned char> tf, tb;
+   std::vector<unsigned char> tf;
    double R = 0.0;
    bool found = false;
 #define GBPA_CASE(d, q, pc) \
-   if (D == d && Q == q) { build_tables_t<d, q, pc>(B, G, tf, tb, R); found = true; }
+   if (D == d && Q == q) { build_tables_t<d, q, pc>(B, G, tf, R); found = true; }
    GBPA_TC_LIST(GBPA_CASE)
 #undef GBPA_CASE
    if (!found) { return GBPA_ERR_UNSUPPORTED; }
    t->D = D; t->Q = Q; t->R = R;
    int rc = check_cuda(cudaMalloc(&t->fwd, tf.size()), "cudaMalloc(tc tables)");
-   if (!rc) { rc = check_cuda(cudaMalloc(&t->bwd, tb.size()), "cudaMalloc(tc tables)"); }
    if (!rc) { rc = check_cuda(cudaMemcpy(t->fwd, tf.data(), tf.size(), cudaMemcpyHostToDevice), "copy tc tables"); }
-   if (!rc) { rc = check_cuda(cudaMemcpy(t->bwd, tb.data(), tb.size(), cudaMemcpyHostToDevice), "copy tc tables"); }
    if (rc) { free_tables(t); }
    return rc;
 }
 
 void free_tables(Tables *t)
 {
-   cudaFree(t->fwd); cudaFree(t->bwd);
-   t->fwd = t->bwd = nullptr;
+   cudaFree(t->fwd);
+   t->fwd = nullptr;
 }
 
 // qscale[e] = 2^-ceil(log2(qmax_e R)), qmax_e the largest absolute row sum of
@@ -524,19 +711,76 @@ int launch_qscale(gbpa_ctx *ctx, int ne, int Q, const float *qd, float R, float 
    return last_launch(ctx, "tc_qscale");
 }
 
+// qdata (Q^3, 6, NE) -> the kernel's tile layout: for tile t, chunk c, half h,
+// value k = 6 p + s (point q = c PC + h NP + p, symmetric entry s) the 128
+// elements of the tile are consecutive; padded points and elements are zero.
 template <int D, int Q, int PC>
-static int launch_t(gbpa_ctx *ctx, int ne, const Tables &t, const float *qd, const float *qscale, const float *x,
+__global__ void transpose_qdata_kernel(int ne, const float *__restrict__ qd, float *__restrict__ qT, int64_t n)
+{
+   using S = Shape<D, Q, PC>;
+   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+        i += (int64_t)gridDim.x * blockDim.x)
+   {
+      const int r = (int)(i % 128);
+      int64_t t = i / 128;
+      const int k = (int)(t % S::NQ); t /= S::NQ;
+      const int h = (int)(t % 2); t /= 2;
+      const int c = (int)(t % S::NCH);
+      const int64_t tile = t / S::NCH;
+      const int p = k / 6, sidx = k % 6;
+      const int q = c * PC + h * S::NP + p;
+      const int64_t e = tile * 128 + r;
+      qT[i] = (e < ne && q < S::Q3) ? qd[(e * 6 + sidx) * S::Q3 + q] : 0.f;
+   }
+}
+
+template <int D, int Q, int PC>
+static int64_t qt_size_t(int ne)
+{
+   using S = Shape<D, Q, PC>;
+   return (int64_t)((ne + 127) / 128) * S::NCH * S::QT_CHUNK;
+}
+
+int64_t transposed_qdata_size(int D, int Q, int ne)
+{
+#define GBPA_CASE(d, q, pc) if (D == d && Q == q) { return qt_size_t<d, q, pc>(ne); }
+   GBPA_TC_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return 0;
+}
+
+int launch_transpose_qdata(gbpa_ctx *ctx, int ne, int D, int Q, const float *qd, float *qT)
+{
+   if (ne <= 0) { return GBPA_SUCCESS; }
+#define GBPA_CASE(d, q, pc)                                                                         \
+   if (D == d && Q == q)                                                                            \
+   {                                                                                                \
+      const int64_t n = qt_size_t<d, q, pc>(ne);                                                    \
+      transpose_qdata_kernel<d, q, pc><<<grid_for(n, 256, 16 * ctx->num_sms), 256, 0, ctx->stream>>>( \
+         ne, qd, qT, n);                                                                            \
+      return last_launch(ctx, "tc_transpose_qdata");                                                \
+   }
+   GBPA_TC_LIST(GBPA_CASE)
+#undef GBPA_CASE
+   return GBPA_ERR_UNSUPPORTED;
+}
+
+template <int D, int Q, int PC>
+static int launch_t(gbpa_ctx *ctx, int ne, const Tables &t, const float *qT, const float *qscale, const float *x,
                     const int *gmap, const unsigned char *mask, float *y, int mode, const int *skip)
 {
    using S = Shape<D, Q, PC>;
    const void *k = (const void *)diffusion_tc_kernel<D, Q, PC>;
    const int ntiles = (ne + 127) / 128;
    const int grid = std::min(ntiles, ctx->num_sms > 0 ? ctx->num_sms : 148);
-   const unsigned char *tf = t.fwd, *tb = t.bwd;
+   const unsigned char *tf = t.fwd;
    int *flags = ctx->d_flags;
-   void *args[] = {&ne, (void *)&tf, (void *)&tb, (void *)&qd, (void *)&qscale, (void *)&x, (void *)&gmap,
-                   (void *)&mask, &y, &mode, (void *)&skip, &flags};
-   return launch_generic(ctx, k, dim3(grid), dim3(256), args, S::SMEM, "diffusion_tc");
+   // the tile's map slice is bulk-copied when the map starts on a 16-byte
+   // boundary (each full tile's slice then does too: 128 D^3 4 bytes)
+   int map_bulk = ((uintptr_t)gmap % 16) == 0 ? 1 : 0;
+   void *args[] = {&ne, (void *)&tf, (void *)&qT, (void *)&qscale, (void *)&x, (void *)&gmap,
+                   &map_bulk, (void *)&mask, &y, &mode, (void *)&skip, &flags};
+   return launch_generic(ctx, k, dim3(grid), dim3(320), args, S::SMEM, "diffusion_tc");
 }
 
 int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, const float *qd,
@@ -554,3 +798,11 @@ int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, c
 
 } // namespace tc
 } // namespace gbpa
+
+#ifdef GBPA_TC_TRACE
+extern "C" int gbpa_tc_trace_read(unsigned long long *out, int n)
+{
+   return cudaMemcpyFromSymbol(out, gbpa::tc::g_tc_trace, sizeof(unsigned long long) * (size_t)n) == cudaSuccess ? 0
+                                                                                                              : -3;
+}
+#endif

@@ -364,6 +364,12 @@ static int setup_tensor_core(gbpa_operator *op)
    {
       rc = tc::launch_qscale(op->ctx, d.ne, d.q1d, (const float *)d.qdata, (float)op->tct->R, op->tc_qscale);
    }
+   if (!rc)
+   {
+      const int64_t n = tc::transposed_qdata_size(d.d1d, d.q1d, d.ne);
+      rc = check_cuda(cudaMalloc(&op->tc_qdata, sizeof(float) * n), "cudaMalloc(tc qdata)");
+   }
+   if (!rc) { rc = tc::launch_transpose_qdata(op->ctx, d.ne, d.d1d, d.q1d, (const float *)d.qdata, op->tc_qdata); }
    return rc;
 }
 
@@ -492,6 +498,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    cudaFree(op->r64); cudaFree(op->t64); cudaFree(op->yEb); cudaFree(op->stage);
    if (op->tct) { tc::free_tables(op->tct); delete op->tct; }
    cudaFree(op->tc_qscale);
+   cudaFree(op->tc_qdata);
    delete op;
    return GBPA_SUCCESS;
 }
@@ -520,7 +527,7 @@ static int apply_to(gbpa_operator *op, const T *x, T *out, int mode, const int *
       // the tensor-core layout, while it stays selected for this order
       if (op->tct && apply_layout(GBPA_DIFFUSION, GBPA_F32, d.d1d, d.q1d, nullptr) == GBPA_LAYOUT_TC)
       {
-         return tc::launch_diffusion_f32(op->ctx, d.ne, d.d1d, d.q1d, *op->tct, (const float *)d.qdata,
+         return tc::launch_diffusion_f32(op->ctx, d.ne, d.d1d, d.q1d, *op->tct, op->tc_qdata,
                                          op->tc_qscale, x, op->gather(), op->gather_mask(), out, mode, skip);
       }
    }

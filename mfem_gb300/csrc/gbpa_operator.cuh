@@ -31,6 +31,7 @@ struct gbpa_operator
    // per-element output scale; null when the operator was created without it
    gbpa::tc::Tables *tct = nullptr;
    float *tc_qscale = nullptr;
+   float *tc_qdata = nullptr;       // qdata in the kernel's tile layout
    // PCG workspace (vectors in the operator's precision)
    void *r = nullptr, *dv = nullptr, *z = nullptr;
    double *partials = nullptr;      // per-block partial sums (PCG_GRID entries x 2)

@@ -8,12 +8,12 @@ namespace gbpa
 namespace tc
 {
 // The Kronecker matrix of one (D, Q) pair, split into fp16 limbs and laid out
-// per chunk for the tensor cores (forward and backward operands), in device
+// per chunk for the tensor cores (one copy serves both GEMMs), in device
 // memory; R is the largest absolute row sum of the matrix (the bound behind
 // the per-element output scale).
 struct Tables
 {
-   unsigned char *fwd = nullptr, *bwd = nullptr;
+   unsigned char *fwd = nullptr;
    double R = 0.0;
    int D = 0, Q = 0;
 };
@@ -24,9 +24,13 @@ int build_tables(int D, int Q, const double *B, const double *G, Tables *t);
 void free_tables(Tables *t);
 // Per-element power-of-two scale of the pointwise output (one float each).
 int launch_qscale(gbpa_ctx *ctx, int ne, int Q, const float *qd, float R, float *qscale);
+// The qdata (Q^3, 6, NE) re-laid per tile of 128 elements for the kernel's
+// coalesced loads (transposed_qdata_size floats).
+int64_t transposed_qdata_size(int D, int Q, int ne);
+int launch_transpose_qdata(gbpa_ctx *ctx, int ne, int D, int Q, const float *qd, float *qT);
 // y = A_e R x with the gather fused (mode as for the other element kernels:
-// 0 E-vector out, 1 accumulate, GBPA_OUT_ATOMIC L-vector). Symmetric qdata
-// (Q^3, 6, NE) in FP32. skip: optional device flag; nonzero skips the launch
+// 0 E-vector out, 1 accumulate, GBPA_OUT_ATOMIC L-vector). qd: the
+// transposed qdata (launch_transpose_qdata) of symmetric FP32 qdata. skip: optional device flag; nonzero skips the launch
 // (a solver that has converged inside a captured graph).
 int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, const float *qd,
                          const float *qscale, const float *x, const int *gmap, const unsigned char *mask,
