@@ -12,7 +12,7 @@
 // quadrature point q, fem/integ/bilininteg_diffusion_kernels.hpp:989-1215).
 // The quadrature points are processed in chunks of PC points: each chunk's
 // forward GEMM lands in TMEM, the CUDA cores apply the qdata and write the
-// chunk's O columns to shared memory, and the backward GEMM accumulates the
+// chunk's O columns back to TMEM, and the backward GEMM accumulates the
 // chunk into the TMEM result. The tables (K and its transpose, split and laid
 // out for the tensor cores) are the same for every tile and stream from L2 by
 // bulk copies.
@@ -26,10 +26,12 @@
 // float per element, computed at operator creation). Both scales are undone
 // exactly in the output.
 //
-// Shared-memory operands use the no-swizzle canonical layouts: 8 x 8 fp16
-// core matrices of 128 contiguous bytes. K-major (x, O, the forward table):
-// core (row group rg, k group kg) at byte (kg * rows/8 + rg) * 128, LBO =
-// rows/8 * 128 between K-adjacent cores, SBO = 128 between row groups. The
+// The A operands (the x tile, the chunk's O columns) are fp16 limbs in TMEM,
+// two values per column, lane = element. The table chunks in shared memory use
+// the no-swizzle canonical layouts: 8 x 8 fp16 core matrices of 128
+// contiguous bytes. K-major for the forward GEMM: core (row group rg, k group
+// kg) at byte (kg * rows/8 + rg) * 128, LBO = rows/8 * 128 between K-adjacent
+// cores, SBO = 128 between row groups. The
 // backward GEMM reads the forward table chunk as MN-major (N = dofs
 // contiguous in each 16-byte row): LBO = 128 between K-adjacent cores (chunk
 // columns), SBO = NC/8 * 128 between N-adjacent cores.
@@ -71,26 +73,27 @@ struct Shape
    static constexpr int NV = 3 * NP;                // chunk columns per thread
    static constexpr int NQ = 6 * NP;                // qdata values per thread and chunk
    static constexpr int M = 128;                    // elements per tile
-   static constexpr int A_LIMB = M * KF * 2;        // bytes of one fp16 limb of the x tile
-   static constexpr int BF_LIMB = NC * KF * 2;      // one limb of a forward table chunk
-   static constexpr int AB_LIMB = M * NC * 2;       // one limb of the chunk's O columns
+   static constexpr int BF_LIMB = NC * KF * 2;      // one limb of a table chunk
    static constexpr int MAP_BYTES = M * D3 * 4;     // the tile's gather map
-   // a ring of NT table-chunk buffers (chunk c in buffer c % NT; the forward
-   // GEMM reads a chunk K-major, the backward GEMM reads the same bytes as an
-   // MN-major operand), the chunk's O columns and the chunk's qdata
-   // (bulk-copied one chunk ahead). The tile's gather map is staged over the
-   // second and third table buffers and the O columns, which are free while
-   // the map is read (before the tile's first MMA).
+   // shared memory: a ring of NT table-chunk buffers (chunk c in buffer
+   // c % NT; the forward GEMM reads a chunk K-major, the backward GEMM reads
+   // the same bytes as an MN-major operand), the chunk's qdata (bulk-copied
+   // one chunk ahead) and the next tile's gather map. The result is staged
+   // over the ring and the qdata buffer after the tile's last GEMM.
    static constexpr int NT = 3;
    static constexpr int QD_BYTES = 2 * NQ * M * 4;  // one tile-chunk of transposed qdata
-   static constexpr int OFF_AF = 0;
-   static constexpr int OFF_T = OFF_AF + 2 * A_LIMB;
-   static constexpr int OFF_AB = OFF_T + NT * 2 * BF_LIMB;
-   static constexpr int OFF_QD = OFF_AB + 2 * AB_LIMB;
-   static constexpr int OFF_MAP = OFF_T + 2 * BF_LIMB;
-   static constexpr int SMEM = OFF_QD + QD_BYTES;
+   static constexpr int OFF_T = 0;
+   static constexpr int OFF_QD = OFF_T + NT * 2 * BF_LIMB;
+   static constexpr int OFF_MAP = OFF_QD + QD_BYTES;
+   static constexpr int SMEM = OFF_MAP + MAP_BYTES;
+   static constexpr int OFF_STG = 0;
+   // tensor memory (512 columns): two forward accumulators, the result, and
+   // the GEMMs' A operands -- the x tile and the chunk's O columns, fp16 hi and
+   // lo limbs, two values per column (lane = element)
+   static constexpr int TF0 = 0, TF1 = 64, TB = 128;
+   static constexpr int TXH = 256, TXL = TXH + KF / 2, TOH = 384, TOL = TOH + NC / 2;
    static __device__ __forceinline__ int off_t(int c) { return OFF_T + (c % NT) * 2 * BF_LIMB; }
-   // output staging in the x tile's buffer: row stride D3; an even stride is
+   // output staging: row stride D3; an even stride is
    // XOR-swizzled by the row (bank-conflict-free either way)
    static constexpr int STG = D3;
    static_assert(D3 % 2 == 1 || D3 % 32 == 0, "staging swizzle");
@@ -98,13 +101,12 @@ struct Shape
    {
       return row * STG + (D3 % 2 ? i : (i ^ (row & 31)));
    }
-   static constexpr int TF0 = 0, TF1 = 64, TB = 128;   // TMEM columns: two forward buffers, the result
    static constexpr int QT_CHUNK = 2 * NQ * M;      // floats of one tile-chunk of transposed qdata
    static_assert(KF <= 128 && NC <= 64 && NC % 16 == 0 && NV % 8 == 0, "TMEM and MMA shapes");
-   static_assert(M * STG * 4 <= 2 * A_LIMB, "output staging must fit in the x tile");
+   static_assert(M * STG * 4 <= OFF_MAP, "output staging must fit over the ring and the qdata buffer");
+   static_assert(KF / 2 <= 64 && NC / 2 <= 64, "A operands in TMEM");
    static_assert(SMEM <= 220 * 1024, "shared memory");
    static_assert(MAP_BYTES % 16 == 0, "bulk copy size");
-   static_assert(OFF_MAP + MAP_BYTES <= OFF_QD, "map staging must fit over the chunk buffers");
    static_assert(NCH >= NT, "the table ring is filled at the tile start");
 };
 
@@ -129,6 +131,13 @@ __device__ __forceinline__ void mma_f16(unsigned dtmem, uint64_t da, uint64_t db
    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                 ::"r"(dtmem), "l"(da), "l"(db), "r"(idesc), "r"((unsigned)acc) : "memory");
+}
+// A operand in tensor memory (lane = row, two fp16 per column along K)
+__device__ __forceinline__ void mma_f16_ta(unsigned dtmem, unsigned atmem, uint64_t db, uint32_t idesc, bool acc)
+{
+   asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}"
+                ::"r"(dtmem), "r"(atmem), "l"(db), "r"(idesc), "r"((unsigned)acc) : "memory");
 }
 __device__ __forceinline__ void mma_commit(unsigned long long *bar)
 {
@@ -158,6 +167,19 @@ __device__ __forceinline__ void tmem_ld8(unsigned taddr, float *v)
 #pragma unroll
    for (int j = 0; j < 8; ++j) { v[j] = __uint_as_float(r[j]); }
 }
+// 8 / 4 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_st8(unsigned taddr, const unsigned *v)
+{
+   asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                : "memory");
+}
+__device__ __forceinline__ void tmem_st4(unsigned taddr, const unsigned *v)
+{
+   asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};"
+                ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]) : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void mbar_expect(unsigned long long *bar, unsigned bytes)
@@ -176,8 +198,9 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned 
                 ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
-// v -> (hi, lo) fp16 limbs of 8 consecutive values, packed for one 16-byte
-// row of a core matrix
+// v -> (hi, lo) fp16 limbs of 8 consecutive values, two per 32-bit word
+// (the lower k in the low half): one 16-byte core-matrix row, or four TMEM
+// columns of an A operand
 __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
 {
    unsigned h[4], l[4];
@@ -202,8 +225,11 @@ __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
 // each waiting only for what it needs. The tensor pipe
 // runs forward(c + 1) while the CUDA cores apply the qdata of chunk c, and
 // backward(c) while they start chunk c + 1 (two forward accumulators in TMEM).
-// Every wait is bounded: after a first expiry no wait blocks, the tile's
-// outputs are NaN and GBPA_FLAG_TIMEOUT is raised.
+// Every wait is bounded: after a first expiry no wait blocks, no further MMA
+// or bulk copy is started, the outputs are NaN and GBPA_FLAG_TIMEOUT is
+// raised; before the CTA exits, the MMA warp and the copy producer wait
+// (bounded) for the work they already started, so that no copy lands in
+// released shared memory and no MMA uses released TMEM.
 template <int D, int Q, int PC>
 __global__ void __launch_bounds__(320, 1)
 diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
@@ -215,14 +241,16 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
    if (skip && *skip) { return; }   // uniform per launch: the solver has finished
    extern __shared__ __align__(1024) unsigned char smem[];
    // mbarriers: map, table ring 0-2, qd (bulk copies); af, ab, dfree0/1,
-   // qfree (256 epilogue arrivals); fwd0/1, bwd (MMA commits)
-   __shared__ __align__(8) unsigned long long mb[13];
+   // qfree, out (256 epilogue arrivals); fwd0/1, bwd, tfree0-2 (the ring
+   // buffer's backward GEMM is done), drain (MMA commits)
+   constexpr int NMB = 18;
+   __shared__ __align__(8) unsigned long long mb[NMB];
    __shared__ unsigned tmem_base;
    __shared__ float s_max[2][128];
    __shared__ int s_fail;
    unsigned long long *MB_MAP = mb, *MB_T = mb + 1, *MB_QD = mb + 4, *MB_AF = mb + 5;
    unsigned long long *MB_AB = mb + 6, *MB_DFREE = mb + 7, *MB_QFREE = mb + 9, *MB_FWD = mb + 10;
-   unsigned long long *MB_BWD = mb + 12;
+   unsigned long long *MB_BWD = mb + 12, *MB_OUT = mb + 13, *MB_TFREE = mb + 14, *MB_DRAIN = mb + 17;
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
    const int half = (warp >> 2) & 1;
    const int r = 32 * (warp & 3) + lane;
@@ -230,8 +258,8 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
 
    if (tid == 0)
    {
-      const unsigned counts[13] = {1, 1, 1, 1, 1, 256, 256, 256, 256, 256, 1, 1, 1};
-      for (int i = 0; i < 13; ++i)
+      const unsigned counts[NMB] = {1, 1, 1, 1, 1, 256, 256, 256, 256, 256, 1, 1, 1, 256, 1, 1, 1, 1};
+      for (int i = 0; i < NMB; ++i)
       {
          asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb + i)), "r"(counts[i]) : "memory");
       }
@@ -240,7 +268,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
    }
    if (warp == 0)
    {
-      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;"
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;"
                    ::"r"(smem_u32(&tmem_base)) : "memory");
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
    }
@@ -265,13 +293,9 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
       // one elected lane issues each batch of MMAs and its commit
       {
          constexpr uint32_t ID_F = instr_desc(128, S::NC), ID_B = instr_desc(128, S::KF, true);
-         constexpr unsigned LBO_A = 16 * 128, LBO_BF = S::NC / 8 * 128;
+         constexpr unsigned LBO_BF = S::NC / 8 * 128;
          // descriptors of the first K step; a step advances the start
          // address field (bits 0-13, 16-byte units)
-         const uint64_t af_hi = smem_desc(sbase + S::OFF_AF, LBO_A, 128);
-         const uint64_t af_lo = smem_desc(sbase + S::OFF_AF + S::A_LIMB, LBO_A, 128);
-         const uint64_t ab_hi = smem_desc(sbase + S::OFF_AB, LBO_A, 128);
-         const uint64_t ab_lo = smem_desc(sbase + S::OFF_AB + S::AB_LIMB, LBO_A, 128);
          // table ring buffer k: + k * 2 BF_LIMB bytes
          const uint64_t tf_hi = smem_desc(sbase + S::OFF_T, LBO_BF, 128);
          const uint64_t tf_lo = smem_desc(sbase + S::OFF_T + S::BF_LIMB, LBO_BF, 128);
@@ -299,13 +323,20 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
                   __syncwarp();
                   if (elect_one())
                   {
-#pragma unroll
-                     for (int st = 0; st < S::KF / 16; ++st)
+                     // after a timed-out wait no further MMA is issued (its
+                     // operands may not have arrived); the commits still arrive
+                     if (!*fail)
                      {
-                        const uint64_t oa = (uint64_t)(st * 2 * LBO_A >> 4), ob = (uint64_t)(st * 2 * LBO_BF >> 4);
-                        mma_f16(d, af_hi + oa, bh + ob, ID_F, st > 0);
-                        mma_f16(d, af_hi + oa, bl + ob, ID_F, true);
-                        mma_f16(d, af_lo + oa, bh + ob, ID_F, true);
+#pragma unroll
+                        for (int st = 0; st < S::KF / 16; ++st)
+                        {
+                           // A = the x tile in TMEM: 16 fp16 per K step = 8 columns
+                           const unsigned ah = tmem + S::TXH + 8 * st, al = tmem + S::TXL + 8 * st;
+                           const uint64_t ob = (uint64_t)(st * 2 * LBO_BF >> 4);
+                           mma_f16_ta(d, ah, bh + ob, ID_F, st > 0);
+                           mma_f16_ta(d, ah, bl + ob, ID_F, true);
+                           mma_f16_ta(d, al, bh + ob, ID_F, true);
+                        }
                      }
                      mma_commit(MB_FWD + (c & 1));
                   }
@@ -329,20 +360,34 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
                   __syncwarp();
                   if (elect_one())
                   {
-#pragma unroll
-                     for (int st = 0; st < S::NC / 16; ++st)
+                     if (!*fail)
                      {
-                        const uint64_t oa = (uint64_t)(st * 2 * LBO_A >> 4), ob = (uint64_t)(st * 2 * 128 >> 4);
-                        mma_f16(tmem + S::TB, ab_hi + oa, bh + ob, ID_B, c > 1 || st > 0);
-                        mma_f16(tmem + S::TB, ab_hi + oa, bl + ob, ID_B, true);
-                        mma_f16(tmem + S::TB, ab_lo + oa, bh + ob, ID_B, true);
+#pragma unroll
+                        for (int st = 0; st < S::NC / 16; ++st)
+                        {
+                           // A = the chunk's O columns in TMEM
+                           const unsigned ah = tmem + S::TOH + 8 * st, al = tmem + S::TOL + 8 * st;
+                           const uint64_t ob = (uint64_t)(st * 2 * 128 >> 4);
+                           mma_f16_ta(tmem + S::TB, ah, bh + ob, ID_B, c > 1 || st > 0);
+                           mma_f16_ta(tmem + S::TB, ah, bl + ob, ID_B, true);
+                           mma_f16_ta(tmem + S::TB, al, bh + ob, ID_B, true);
+                        }
                      }
+                     // the epilogue's O buffer, and the chunk's ring buffer
+                     // (its own barrier: the copy producer waits per buffer)
                      mma_commit(MB_BWD);
+                     mma_commit(MB_TFREE + (c - 1) % S::NT);
                   }
                   __syncwarp();
                }
             }
          }
+         // every MMA this warp issued has completed before TMEM is released
+         // (a commit tracks all earlier MMAs of the issuing thread)
+         __syncwarp();
+         if (elect_one()) { mma_commit(MB_DRAIN); }
+         __syncwarp();
+         if (!mbar_wait(MB_DRAIN, 0, 1LL << 20)) { *fail = 1; }
       }
    }
    else if (warp == 9)
@@ -350,14 +395,27 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
       // ---------------------------------------------------- copy producer
       if (lane == 0)
       {
-         unsigned ph_bwd = 0, ph_qfree = 0, ph_af = 0;
+         unsigned ph_qfree = 0, ph_af = 0, ph_tfree[S::NT] = {};
+         // copies issued per barrier (map, ring 0-2, qdata): each completes one
+         // phase of its barrier, which nothing else arrives on
+         int n_cp[2 + S::NT] = {};
+         auto copy = [&](int slot, unsigned long long *bar, void *dst, const void *src, unsigned bytes) {
+            if (*fail) { return; }   // after a timed-out wait nothing new is started
+            mbar_expect(bar, bytes);
+            bulk_g2s(dst, src, bytes, bar);
+            ++n_cp[slot];
+         };
+         // table chunk c into ring buffer c % NT, once the backward GEMM of
+         // the chunk held there before (if any) has completed
+         bool held[S::NT] = {};
          auto load_t = [&](int c) {
-            mbar_expect(MB_T + c % S::NT, 2 * S::BF_LIMB);
-            bulk_g2s(smem + S::off_t(c), tab_f + (size_t)c * 2 * S::BF_LIMB, 2 * S::BF_LIMB, MB_T + c % S::NT);
+            const int k = c % S::NT;
+            if (held[k]) { wait(MB_TFREE + k, ph_tfree[k]); ph_tfree[k] ^= 1; }
+            held[k] = true;
+            copy(1 + k, MB_T + k, smem + S::off_t(c), tab_f + (size_t)c * 2 * S::BF_LIMB, 2 * S::BF_LIMB);
          };
          auto load_qd = [&](int tile, int c) {
-            mbar_expect(MB_QD, S::QD_BYTES);
-            bulk_g2s(smem + S::OFF_QD, qT + ((size_t)tile * S::NCH + c) * S::QT_CHUNK, S::QD_BYTES, MB_QD);
+            copy(1 + S::NT, MB_QD, smem + S::OFF_QD, qT + ((size_t)tile * S::NCH + c) * S::QT_CHUNK, S::QD_BYTES);
          };
          // qdata streams from HBM: the chunks QPF ahead of the one being
          // copied to shared memory are on their way into L2, so that copy is
@@ -369,22 +427,25 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             if (t < ntiles) { bulk_prefetch_l2(qT + ((size_t)t * S::NCH + cc) * S::QT_CHUNK, S::QD_BYTES); }
          };
          for (int k = 0; k < QPF; ++k) { prefetch_qd(blockIdx.x, k); }
+         auto load_map = [&](int tile) {
+            const long long e0 = (long long)tile * 128;
+            if (tile < ntiles && map_bulk && e0 + 128 <= ne)
+            {
+               copy(0, MB_MAP, smem + S::OFF_MAP, gmap + e0 * S::D3, S::MAP_BYTES);
+            }
+         };
+         unsigned ph_out = 0;
+         load_map(blockIdx.x);
          int it = 0;
          for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
          {
-            const long long e0 = (long long)tile * 128;
-            // the previous tile's MMAs have all completed and its last qdata
-            // chunk was taken (waited below): every target buffer is free
-            if (map_bulk && e0 + 128 <= ne)
-            {
-               mbar_expect(MB_MAP, S::MAP_BYTES);
-               bulk_g2s(smem + S::OFF_MAP, gmap + e0 * S::D3, S::MAP_BYTES, MB_MAP);
-            }
+            // the previous tile's GEMMs are done and its result has left the
+            // staging over the ring and the qdata buffer (waited below)
             load_qd(tile, 0);
-            load_t(0);
+            for (int c = 0; c < S::NT && c < S::NCH; ++c) { load_t(c); }
             wait(MB_AF, ph_af); ph_af ^= 1;
-            // the map has been read: the buffers under it are free
-            for (int c = 1; c < S::NT && c < S::NCH; ++c) { load_t(c); }
+            // this tile's map has been read: fetch the next tile's
+            load_map(tile + gridDim.x);
             for (int c = 0; c < S::NCH; ++c)
             {
                // qdata chunk c + 1 once the epilogue has taken chunk c; table
@@ -392,15 +453,22 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
                wait(MB_QFREE, ph_qfree); ph_qfree ^= 1;
                if (c + 1 < S::NCH) { load_qd(tile, c + 1); }
                prefetch_qd(tile, c + QPF);
-               if (c >= 1)
+               if (c >= 1 && c + S::NT - 1 < S::NCH)
                {
-                  wait(MB_BWD, ph_bwd); ph_bwd ^= 1;
+                  load_t(c + S::NT - 1);
                   TC_TRACE(it, 16 * (c - 1) + 4);
-                  if (c + S::NT - 1 < S::NCH) { load_t(c + S::NT - 1); }
                }
             }
-            wait(MB_BWD, ph_bwd); ph_bwd ^= 1;   // the tile's last GEMM
             TC_TRACE(it, 1002);
+            wait(MB_OUT, ph_out); ph_out ^= 1;   // the tile's result has been stored
+         }
+         // no bulk copy is still writing shared memory when the CTA exits: the
+         // last phase each barrier was given has completed (earlier phases of a
+         // barrier complete in order)
+         for (int s = 0; s < 2 + S::NT; ++s)
+         {
+            unsigned long long *bar = s == 0 ? MB_MAP : (s <= S::NT ? MB_T + (s - 1) : MB_QD);
+            if (n_cp[s] > 0 && !mbar_wait(bar, (unsigned)(n_cp[s] - 1) & 1u, 1LL << 20)) { *fail = 1; }
          }
       }
    }
@@ -410,7 +478,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
       const unsigned lane_off = (unsigned)(32 * (warp & 3)) << 16;
       unsigned ph_map = 0, ph_qd = 0, ph_fwd[2] = {0, 0}, ph_bwd = 0;
       const int *smap = reinterpret_cast<const int *>(smem + S::OFF_MAP);
-      float *stg = reinterpret_cast<float *>(smem + S::OFF_AF);
+      float *stg = reinterpret_cast<float *>(smem + S::OFF_STG);
       int it = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
       {
@@ -466,6 +534,9 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          }
          const float so = act ? __ldg(qscale + e) : 1.f;
 #pragma unroll
+         // the x tile's fp16 limbs into TMEM (this thread's half row: KH
+         // values, KH/2 columns per limb); the forward GEMMs read them as A
+#pragma unroll
          for (int g8 = 0; g8 < S::KH / 8; ++g8)
          {
             float v[8];
@@ -473,12 +544,13 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             for (int j = 0; j < 8; ++j) { v[j] = xv[8 * g8 + j] * sx; }
             uint4 hi, lo;
             split8(v, hi, lo);
-            const int kg = half * (S::KH / 8) + g8;
-            const int off = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
-            *reinterpret_cast<uint4 *>(smem + S::OFF_AF + off) = hi;
-            *reinterpret_cast<uint4 *>(smem + S::OFF_AF + S::A_LIMB + off) = lo;
+            const unsigned col = lane_off + half * (S::KH / 2) + 4 * g8;
+            const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
+            tmem_st4(tmem + S::TXH + col, h4);
+            tmem_st4(tmem + S::TXL + col, l4);
          }
-         fence_async_smem();
+         tmem_wait_st();
+         fence_before();
          if (tid == 0) { TC_TRACE(it, 1011); }
          arrive(MB_AF);
 
@@ -498,6 +570,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             arrive(MB_QFREE);
             wait(MB_FWD + (c & 1), ph_fwd[c & 1]); ph_fwd[c & 1] ^= 1;
             if (tid == 0) { TC_TRACE(it, 16 * c + 6); }
+            __syncwarp();   // the warp-collective TMEM loads need the converged warp
             fence_after();
             float gq[S::NV];
             const unsigned tcol = tmem + lane_off + ((c & 1) ? S::TF1 : S::TF0) + half * S::NV;
@@ -521,23 +594,27 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             }
             if (tid == 0) { TC_TRACE(it, 16 * c + 7); }
             if (c >= 1) { wait(MB_BWD, ph_bwd); ph_bwd ^= 1; }   // backward(c - 1) has read A_bwd
+            __syncwarp();
             if (tid == 0) { TC_TRACE(it, 16 * c + 8); }
+            // the chunk's O limbs into TMEM (NV values, NV/2 columns per limb)
 #pragma unroll
             for (int jg = 0; jg < S::NV / 8; ++jg)
             {
                uint4 hi, lo;
                split8(o + 8 * jg, hi, lo);
-               const int kg = half * (S::NV / 8) + jg;
-               const int off = (kg * 16 + (r >> 3)) * 128 + (r & 7) * 16;
-               *reinterpret_cast<uint4 *>(smem + S::OFF_AB + off) = hi;
-               *reinterpret_cast<uint4 *>(smem + S::OFF_AB + S::AB_LIMB + off) = lo;
+               const unsigned col = lane_off + half * (S::NV / 2) + 4 * jg;
+               const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
+               tmem_st4(tmem + S::TOH + col, h4);
+               tmem_st4(tmem + S::TOL + col, l4);
             }
-            fence_async_smem();
+            tmem_wait_st();
+            fence_before();
             arrive(MB_AB);
             if (tid == 0) { TC_TRACE(it, 16 * c + 9); }
          }
          // ---- result: D_bwd = (A_e x) sx so; undo the scales, stage, store
          wait(MB_BWD, ph_bwd); ph_bwd ^= 1;
+         __syncwarp();
          if (tid == 0) { TC_TRACE(it, 1013); }
          fence_after();
          const float inv = 1.f / (sx * so);
@@ -574,8 +651,10 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             const long long slot = ee * S::D3 + i;
             store_result(y, slot, slot, v, mode, gmap, mask);
          }
-         // staging (the x tile's buffer) is rewritten by the next tile's split
-         asm volatile("bar.sync 1, 256;" ::: "memory");
+         // the staging overlays the ring and the qdata buffer: release it to
+         // the copy producer
+         fence_async_smem();
+         arrive(MB_OUT);
          if (tid == 0) { TC_TRACE(it, 1012); }
       }
    }
@@ -585,7 +664,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
    __syncthreads();
    if (warp == 0)
    {
-      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
    }
 }
 
