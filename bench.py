@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "x2"],
                     help="arithmetic of the timed operator (x2: FP64 data, double-float on FP32 pipes)")
+    ap.add_argument("--layout", default="default", choices=["default", "cuda_core", "tensor_core"],
+                    help="FP32 diffusion: the apply layout of the timed operator (default: the tuned one)")
     ap.add_argument("--cpu-sample-n", type=int, default=None,
                     help="mesh of the CPU baseline (default: the GPU workload's n)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
@@ -203,15 +205,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def profiled_traffic(precision, kind, p, ne):
+def profiled_traffic(precision, kind, p, ne, layout=0):
     """DRAM bytes per launch of the element kernel from the committed ncu
-    summary of the same kernel on the 24^3 case (profiles/), scaled by the
-    element count (traffic grows with elements: qdata, map and E-vector are
-    per element, the gathered x is ~1 dof per element)."""
+    summary of the same kernel on a small case (profiles/: the 24^3 case, or
+    40^3 for the tensor-core kernel), scaled by the element count (traffic
+    grows with elements: qdata, map and E-vector are per element, the
+    gathered x is ~1 dof per element)."""
     if kind != "diffusion" or p != 4:
         return None, None
     name = {"f64": "f64", "x2": "f64x2", "f32": "f32"}[precision]
     path = os.path.join(REPO, "profiles", f"diffusion_apply_{name}_p4_n24.md")
+    if layout == 2:
+        path = os.path.join(REPO, "profiles", "diffusion_tc_f32_p4_n40.md")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_element:"):
@@ -399,6 +404,14 @@ def run_gpu(args):
     ne, ndofs, D, Q = fes.ne, fes.ndofs, integ.D, integ.Q
     prec = {"f64": 0, "f32": 1, "x2": 2}[args.precision]
     wbytes = 4 if prec == 1 else 8
+    if args.layout != "default":
+        from mfem_gb300 import autotune
+        if prec != 1 or args.kind != "diffusion":
+            raise SystemExit("--layout selects between the FP32 diffusion layouts (--precision f32)")
+        lay = autotune.GBPA_LAYOUT_TC if args.layout == "tensor_core" else 0
+        _lib.check(lib.gbpa_set_apply_layout(0, 1, D, Q, lay, 0), "gbpa_set_apply_layout")
+    nbl = ctypes.c_int(0)
+    layout_used = lib.gbpa_get_apply_layout(kid, prec, D, Q, ctypes.byref(nbl))
     op = PAOperator(kid, fes, D, Q, integ.B, integ.G, integ.qdata, precision=prec)
     from mfem_gb300 import fem
     x = torch.from_numpy(2 * fem.u01_array(2, ndofs) - 1).cuda()
@@ -448,7 +461,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak_hbm()
     hbm_live = measured_hbm_live_gbs()
     achieved = kbytes / (k_ms * 1e-3) / 1e9
-    traffic, traffic_src = profiled_traffic(args.precision, args.kind, args.p, ne)
+    traffic, traffic_src = profiled_traffic(args.precision, args.kind, args.p, ne, layout_used)
     fp64_roof = None
     if prec == 0:
         fpe = element_flops(D, Q, args.kind)
@@ -500,10 +513,11 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {0: "f64", 1: "f32", 2: "f64x2"}[prec], "data": "synthetic",
-        "config": workload_config(args, world),
+        "config": dict(workload_config(args, world), layout=LAYOUT_NAMES.get(layout_used, str(layout_used))),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                     "kernel": f"{args.kind}_apply (gather fused)",
+                     "kernel": (f"{args.kind}_apply (gather fused)" if layout_used != 2 else
+                                "diffusion_tc (tensor cores, gather fused)"),
                      "kernel_ms": k_ms, "algorithmic_bytes": kbytes, "peak_source": peak_kind,
                      "peak_live": hbm_live, "frac_live": achieved / hbm_live,
                      "note": ("native FP64 is FP64-pipe bound on GB300 (ncu: FP64 pipe 91.5% active); "
@@ -558,45 +572,82 @@ def run_gpu(args):
     return 0 if parity_ok else 1
 
 
-def run_extras(args, fes, integ, op, x, y):
-    """FP32 twin of the operator and the same apply in FP32 (the inner operator
-    of the mixed-precision form)."""
+def _event_ms(fn, steps):
+    """ms per call of fn, CUDA events on the current stream, 3 warm-up calls."""
     import torch
-    from mfem_gb300.pa import PAOperator
-    out = {}
-    op32 = PAOperator(0 if args.kind == "diffusion" else 1, fes, integ.D, integ.Q, integ.B, integ.G,
-                      integ.qdata, precision=1)
-    x32, y32 = x.float(), y.float()
     for _ in range(3):
-        op32.Mult(x32, y32)
+        fn()
     torch.cuda.synchronize()
     s = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(s)
-    for _ in range(args.steps):
-        op32.Mult(x32, y32)
+    for _ in range(steps):
+        fn()
     b.record(s)
     torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / args.steps
-    out["fp32_apply"] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
-                         "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, 4, args.kind,
-                                                           False) / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0]}
-    del op32, x32, y32
+    return a.elapsed_time(b) / steps
+
+
+LAYOUT_NAMES = {0: "slab2d", 1: "3d", 2: "tensor_core"}
+
+
+def run_extras(args, fes, integ, op, x, y):
+    """The same apply in FP32 (the inner operator of the mixed-precision form)
+    on the CUDA cores and, where the order has one, on the tensor cores
+    (GBPA_LAYOUT_TC: two Kronecker GEMMs per tile of 128 elements, fp16 hi/lo
+    limbs, FP32 accumulation), each as the L->L Mult and as the element kernel
+    alone; then the double-float apply."""
+    import ctypes
+    import torch
+    from mfem_gb300 import autotune
+    from mfem_gb300.pa import Device, PAOperator
+    lib = Device.get().lib
+    kind = 0 if args.kind == "diffusion" else 1
+    D, Q = integ.D, integ.Q
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    out = {}
+    op.Mult(x, y)
+    torch.cuda.synchronize()
+    x32 = x.float()
+    yE = torch.empty(fes.ne * D ** 3, dtype=torch.float32, device=x.device)
+    nb = ctypes.c_int(0)
+    prev = lib.gbpa_get_apply_layout(kind, 1, D, Q, ctypes.byref(nb))
+    out["fp32_default_layout"] = LAYOUT_NAMES.get(prev, str(prev))
+    cuda_core = (prev, nb.value) if prev != autotune.GBPA_LAYOUT_TC else (0, 0)
+    runs = [("fp32_apply", cuda_core)]
+    if kind == 0 and (D, Q) in autotune.TC:
+        runs.append(("fp32_apply_tensor_core", (autotune.GBPA_LAYOUT_TC, 0)))
+    peak = measured_peak_hbm()[0]
+    try:
+        for name, (layout, nbz) in runs:
+            if lib.gbpa_set_apply_layout(kind, 1, D, Q, layout, nbz) != 0:
+                continue
+            op32 = PAOperator(kind, fes, D, Q, integ.B, integ.G, integ.qdata, precision=1)
+            y32 = torch.empty_like(x32)
+            ms = _event_ms(lambda: op32.Mult(x32, y32), args.steps)
+            mse = _event_ms(lambda: lib.gbpa_operator_apply_element(op32.handle, P(x32), P(yE)), args.steps)
+            op32.Mult(x32, y32)
+            torch.cuda.synchronize()
+            rel = float(torch.linalg.norm(y32.double() - y) / torch.linalg.norm(y))
+            out[name] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
+                         "layout": LAYOUT_NAMES.get(layout, str(layout)), "rel_l2_vs_f64": rel,
+                         "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, D, Q, 4, args.kind, False)
+                         / (ms * 1e-3) / 1e9 / peak,
+                         "element_kernel_ms": mse,
+                         "element_kernel_hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, D, Q, 4, args.kind,
+                                                                          True) / (mse * 1e-3) / 1e9 / peak}
+            del op32, y32
+    finally:
+        lib.gbpa_set_apply_layout(kind, 1, D, Q, prev, nb.value)
+    del x32, yE
     # FP64 data, double-float arithmetic on the FP32 pipes
     opx = PAOperator(0 if args.kind == "diffusion" else 1, fes, integ.D, integ.Q, integ.B, integ.G,
                      integ.qdata, precision=2)
     yx = torch.empty_like(y)
-    for _ in range(3):
-        opx.Mult(x, yx)
+    ms = _event_ms(lambda: opx.Mult(x, yx), args.steps)
     op.Mult(x, y)
     torch.cuda.synchronize()
     rel = float(torch.linalg.norm(yx - y) / torch.linalg.norm(y))
-    a.record(s)
-    for _ in range(args.steps):
-        opx.Mult(x, yx)
-    b.record(s)
-    torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / args.steps
     out["f64x2_apply"] = {"value": fes.ndofs / (ms * 1e-3) / 1e9, "unit": "GDOF/s", "ms_per_apply": ms,
                           "rel_l2_vs_native_f64": rel,
                           "hbm_frac_alg": algorithmic_bytes(fes.ne, fes.ndofs, integ.D, integ.Q, 8, args.kind,

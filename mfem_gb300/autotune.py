@@ -11,7 +11,14 @@ slab, "layout3d" for the orders where the 3D layout won) and applied by
 Device() on start-up through gbpa_set_elements_per_block and
 gbpa_set_apply_layout.
 
+FP32 diffusion at the orders with a tensor-core kernel (GBPA_LAYOUT_TC) is
+compared separately, on a large mesh (--tc-dofs, 3e7 by default: the kernel
+runs persistent CTAs over tiles of 128 elements, so small meshes leave SMs
+idle): "tensor_core" lists the orders where it beat the best CUDA-core
+layout, with the timings of both.
+
     python -m mfem_gb300.autotune [--orders 1-8] [--dofs 2e6] [--out path]
+    python -m mfem_gb300.autotune --tensor-core-only [--tc-dofs 3e7]   (updates "tensor_core" in place)
 """
 import argparse
 import ctypes
@@ -62,6 +69,11 @@ DQ3 = {(2, 2), (2, 3), (3, 3), (3, 4), (4, 4), (4, 5), (5, 5), (5, 6), (6, 6), (
        (8, 8), (8, 9), (9, 9), (9, 10), (4, 6), (5, 8)}
 
 
+# (D, Q) pairs with a tensor-core FP32 diffusion kernel (GBPA_TC_LIST)
+TC = {(3, 4), (4, 5), (5, 6)}
+GBPA_LAYOUT_TC = 2
+
+
 def apply_layouts(lib, layout3d):
     """Install the 3D-layout entries {key: nbz} (parsed first, malformed
     entries skipped)."""
@@ -87,6 +99,7 @@ def load_default(lib, path=TUNING):
         skipped = []
         nbz = _parse_table(t.get("nbz", {}), "nbz", skipped)
         lay = _parse_table(t.get("layout3d", {}), "layout3d", skipped)
+        tc = _parse_table(t.get("tensor_core", {}), "tensor_core", skipped)
     except (OSError, ValueError, TypeError, AttributeError) as e:
         warnings.warn(f"tuning table {path} not applied ({type(e).__name__}: {e}); using the defaults")
         return 0
@@ -94,6 +107,10 @@ def load_default(lib, path=TUNING):
         warnings.warn(f"tuning table {path}: skipped malformed entries {', '.join(skipped)}")
     n = sum(1 for kd, pr, D, Q, v in nbz if lib.gbpa_set_elements_per_block(kd, pr, D, Q, v) == 0)
     n += sum(1 for kd, pr, D, Q, v in lay if lib.gbpa_set_apply_layout(kd, pr, D, Q, 1, v) == 0)
+    # tensor-core entries (value 1) come last: they take precedence over a
+    # 3D-layout entry for the same key
+    n += sum(1 for kd, pr, D, Q, v in tc
+             if v == 1 and lib.gbpa_set_apply_layout(kd, pr, D, Q, GBPA_LAYOUT_TC, 0) == 0)
     return n
 
 
@@ -207,6 +224,71 @@ def tune(orders=range(1, 9), kinds=("diffusion", "mass"), precs=("f64", "f32", "
     return table, timings, layout3d
 
 
+def time_mult(lib, op, x, y, reps):
+    """ms per L->L apply (gbpa_operator_mult, the operator's Mult)."""
+    import torch
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    for _ in range(2):
+        lib.gbpa_operator_mult(op.handle, P(x), P(y))
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        if lib.gbpa_operator_mult(op.handle, P(x), P(y)) != 0:
+            return float("inf")
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def tune_tensor_core(orders=range(1, 9), target_dofs=3e7, reps=20, verbose=True):
+    """FP32 diffusion: the tensor-core layout against the layout installed for
+    the CUDA cores (the tuned slab or 3D entry), both timed through the
+    operator's Mult on one jittered mesh of about target_dofs dofs per order.
+    Returns ({key: 1} for the orders where the tensor cores won, timings)."""
+    import torch
+    from . import fem
+    from .pa import DiffusionIntegrator, Device, FiniteElementSpace, PAOperator
+    lib = Device.get().lib
+    won, timings = {}, {}
+    for p in orders:
+        D, Q = p + 1, p + 2
+        if (D, Q) not in TC:
+            continue
+        n = max(2, int(round((target_dofs ** (1 / 3) - 1) / p)))
+        fes = FiniteElementSpace(fem.CartesianMesh(n, jitter=0.1, seed=1), p)
+        integ = DiffusionIntegrator()
+        integ.AssemblePA(fes)
+        x = (torch.rand(fes.ndofs, device="cuda", dtype=torch.float64) - 0.5)
+        y64 = torch.empty_like(x)
+        PAOperator(0, fes, D, Q, integ.B, integ.G, integ.qdata).Mult(x, y64)
+        x32 = x.float()
+        ms, rel = {}, {}
+        nb = ctypes.c_int(0)
+        prev = lib.gbpa_get_apply_layout(0, 1, D, Q, ctypes.byref(nb))
+        # the CUDA-core side: the installed layout, or the 2D slab when the
+        # installed one is the tensor-core layout
+        cuda_core = (prev, nb.value) if prev != GBPA_LAYOUT_TC else (0, 0)
+        for name, (layout, nbz) in (("cuda_core", cuda_core), ("tensor_core", (GBPA_LAYOUT_TC, 0))):
+            if lib.gbpa_set_apply_layout(0, 1, D, Q, layout, nbz) != 0:
+                continue
+            op = PAOperator(0, fes, D, Q, integ.B, integ.G, integ.qdata, precision=1)
+            y = torch.empty_like(x32)
+            ms[name] = time_mult(lib, op, x32, y, reps)
+            rel[name] = float(torch.linalg.norm(y.double() - y64) / torch.linalg.norm(y64))
+            del op, y
+        lib.gbpa_set_apply_layout(0, 1, D, Q, prev, nb.value)
+        k = key("diffusion", "f32", D, Q)
+        timings[k] = {"ne": fes.ne, "ndofs": fes.ndofs, "mult_ms": ms, "rel_l2_vs_f64": rel}
+        if "tensor_core" in ms and ms["tensor_core"] < ms["cuda_core"]:
+            won[k] = 1
+        if verbose:
+            print(f"diffusion f32 p={p}: {ms} (rel vs f64 {rel})", flush=True)
+        del fes, integ, x, y64, x32
+        torch.cuda.empty_cache()
+    return won, timings
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--orders", default="1-8")
@@ -214,13 +296,25 @@ def main():
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--kinds", default="diffusion,mass")
     ap.add_argument("--out", default=TUNING)
+    ap.add_argument("--tc-dofs", type=float, default=3e7)
+    ap.add_argument("--tensor-core-only", action="store_true",
+                    help="re-time only the tensor-core layout; keep the rest of the table at --out")
     args = ap.parse_args()
     lo, hi = (int(v) for v in args.orders.split("-"))
-    table, timings, layout3d = tune(range(lo, hi + 1), kinds=tuple(args.kinds.split(",")),
-                                    target_dofs=args.dofs, reps=args.reps)
+    if args.tensor_core_only:
+        with open(args.out) as f:
+            t = json.load(f)
+    else:
+        table, timings, layout3d = tune(range(lo, hi + 1), kinds=tuple(args.kinds.split(",")),
+                                        target_dofs=args.dofs, reps=args.reps)
+        t = {"nbz": table, "layout3d": layout3d, "timings_ms": timings}
+    if "diffusion" in args.kinds:
+        won, tct = tune_tensor_core(range(lo, hi + 1), target_dofs=args.tc_dofs)
+        t["tensor_core"], t["tensor_core_timings"] = won, tct
     with open(args.out, "w") as f:
-        json.dump({"nbz": table, "layout3d": layout3d, "timings_ms": timings}, f, indent=1, sort_keys=True)
-    print(f"wrote {args.out} ({len(table)} entries, 3D layout for {len(layout3d)})")
+        json.dump(t, f, indent=1, sort_keys=True)
+    print(f"wrote {args.out} ({len(t['nbz'])} entries, 3D layout for {len(t['layout3d'])}, "
+          f"tensor cores for {len(t.get('tensor_core', {}))})")
 
 
 if __name__ == "__main__":

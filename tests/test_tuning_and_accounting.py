@@ -55,6 +55,16 @@ def test_3d_kernel_list_matches_library_dispatch():
     assert pairs == at.DQ3
 
 
+def test_tensor_core_list_matches_library_dispatch():
+    """The tuner's TC set is the library's GBPA_TC_LIST."""
+    import re
+    from mfem_gb300 import autotune as at
+    src = open(os.path.join(REPO, "mfem_gb300", "csrc", "gbpa_apply_tc.cu")).read()
+    line = next(ln for ln in src.splitlines() if ln.startswith("#define GBPA_TC_LIST"))
+    pairs = {(int(a), int(b)) for a, b, _ in re.findall(r"X\((\d+),\s*(\d+),\s*(\d+)\)", line)}
+    assert pairs == at.TC
+
+
 @pytest.mark.parametrize("p", range(1, 9))
 def test_element_flops_against_the_closed_form(p):
     """The bench's diffusion flop count is the kernel's contraction sequence:
@@ -91,6 +101,12 @@ class _FakeLib:
         return 0
 
     def gbpa_set_apply_layout(self, kind, prec, D, Q, layout, nbz):
+        from mfem_gb300 import autotune as at
+        if layout == at.GBPA_LAYOUT_TC:
+            if kind != 0 or prec != 1 or (D, Q) not in at.TC:
+                return -2
+            self.layout[(kind, prec, D, Q)] = (layout, 0)
+            return 0
         if nbz < 1 or nbz * Q > 64 or nbz * Q ** 3 > 1024:
             return -1
         self.layout[(kind, prec, D, Q)] = (layout, nbz)
@@ -102,8 +118,40 @@ def test_load_default_installs_the_committed_table():
     lib = _FakeLib()
     t = tuning()
     n = at.load_default(lib)
-    assert n == len(t["nbz"]) + len(t.get("layout3d", {}))
-    assert len(lib.layout) == len(t.get("layout3d", {}))
+    tc = t.get("tensor_core", {})
+    assert n == len(t["nbz"]) + len(t.get("layout3d", {})) + len(tc)
+    assert len(lib.layout) == len(set(t.get("layout3d", {})) | set(tc))
+    for k in tc:
+        kind, prec, D, Q = k.split(":")
+        assert lib.layout[(at.KINDS[kind], at.PRECS[prec], int(D), int(Q))] == (at.GBPA_LAYOUT_TC, 0)
+
+
+def test_tensor_core_entries_name_kernels_that_exist():
+    """Every committed tensor-core entry is FP32 diffusion at an order with a
+    tensor-core kernel, and its recorded timing shows the tensor cores ahead
+    of the CUDA cores on the same mesh."""
+    from mfem_gb300 import autotune as at
+    t = tuning()
+    for k, v in t.get("tensor_core", {}).items():
+        kind, prec, D, Q = k.split(":")
+        assert kind == "diffusion" and prec == "f32" and (int(D), int(Q)) in at.TC and v == 1, k
+        ms = t["tensor_core_timings"][k]["mult_ms"]
+        assert ms["tensor_core"] < ms["cuda_core"], k
+
+
+def test_tensor_core_section_overrides_and_is_checked(tmp_path):
+    """A tensor-core entry is installed after (and so replaces) a 3D-layout
+    entry for the same key; entries the library refuses (FP64, mass, an
+    order without a kernel) or whose value is not 1 install nothing."""
+    from mfem_gb300 import autotune as at
+    lib = _FakeLib()
+    f = tmp_path / "tc.json"
+    f.write_text(json.dumps({"nbz": {}, "layout3d": {"diffusion:f32:5:6": 1},
+                             "tensor_core": {"diffusion:f32:5:6": 1, "diffusion:f64:5:6": 1, "mass:f32:5:6": 1,
+                                             "diffusion:f32:7:8": 1, "diffusion:f32:3:4": 0}}))
+    n = at.load_default(lib, str(f))
+    assert n == 2
+    assert lib.layout == {(0, 1, 5, 6): (at.GBPA_LAYOUT_TC, 0)}
 
 
 def test_load_default_tolerates_bad_files(tmp_path):
