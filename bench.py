@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU baseline: applies timed for about this long")
     ap.add_argument("--no-pcg", action="store_true", help="skip the precision-form PCG comparison")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batching- and combined-form blocks of the default run")
     ap.add_argument("--pcg-n", type=int, default=77,
                     help="mesh size of the precision-form PCG comparison (77: ~29.5 M DOFs at p=4)")
     ap.add_argument("--pcg-only", action="store_true", help="run only the precision-form PCG comparison")
@@ -508,6 +510,13 @@ def run_gpu(args):
         if not args.no_pcg:
             extras["pcg"] = run_pcg_form(args.pcg_n, args.p, args.pcg_max_it)
             extras["mg"] = run_mg_form(args.pcg_n, args.p, (1, 2, 4))
+        if not args.no_forms:
+            # the batching and combined forms at their default sizes
+            del op
+            torch.cuda.empty_cache()
+            extras["batched"] = run_batched_form(args.nprob, persistent=False)
+            torch.cuda.empty_cache()
+            extras["combined"] = run_combined_form(args.combined_n, 5, 8, True)
 
     line = {
         "metric": METRIC, "value": value, "unit": "GDOF/s", "n_gpus": world, "steps": args.steps,
@@ -753,14 +762,17 @@ def run_pcg_form(n, p, max_it=2000):
     return out
 
 
-def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
+def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000, persistent=True):
     """Batching form: nprob independent Dirichlet Poisson problems, each a
     jittered Cartesian hex mesh of n^3 elements with n uniform in [4, 16] and
     order p uniform in {2,...,6} (splitmix64 stream, seed 5), lognormal kappa
     and RHS ~ U[0,1] per problem; all solved to 1e-10 together (graph
-    schedule: per-order grouped launches, K iterations per CUDA graph; and the
-    one-launch persistent schedule), against solving them one after another
-    with the single-problem device PCG (CUDA-graph captured iterations).
+    schedule: per-order grouped launches, K iterations per CUDA graph), in
+    double-float arithmetic (FP64 data, FP64-accurate products on the FP32
+    pipes: the batch's headline) and in native FP64, against solving them one
+    after another with the single-problem device PCG (CUDA-graph captured
+    iterations) in the same two arithmetics. With persistent=True the
+    one-launch persistent schedule is timed too.
     dof_iterations = sum over problems of DOFs x iterations: the PCG work."""
     import torch
     from mfem_gb300 import _lib, fem
@@ -785,61 +797,73 @@ def run_batched_form(nprob=256, seed=5, rel_tol=1e-10, max_it=5000):
         e = torch.from_numpy(ess).cuda()
         x = torch.zeros_like(b)
         R = fes.GetElementRestriction()
-        probs.append(dict(A=A, dinv=M.dinv, b=b, x=x, ess=e, integ=integ, R=R, n=n, p=p))
+        probs.append(dict(A=A, dinv=M.dinv, b=b, x=x, ess=e, ess_h=ess, integ=integ, R=R, n=n, p=p))
         descs.append(_lib.ProblemDesc(fes.ne, fes.ndofs, integ.D, integ.Q, integ.B.data_ptr(),
                                       integ.G.data_ptr(), integ.qdata.data_ptr(), R.gather_map.data_ptr(),
                                       R.offsets.data_ptr(), R.indices.data_ptr(), e.data_ptr(), e.numel(),
                                       M.dinv.data_ptr(), b.data_ptr(), x.data_ptr()))
         total += fes.ndofs
     arr = (_lib.ProblemDesc * nprob)(*descs)
-    its = (ctypes.c_int * nprob)()
-    conv = (ctypes.c_int * nprob)()
-    secs = ctypes.c_double(0)
-    # the persistent schedule and the double-float arithmetic first (their
-    # solutions are overwritten by the default FP64 graph-schedule run)
-    def other(precision, schedule):
+
+    def batched(precision, schedule):
         sec = ctypes.c_double(0)
         cv = (ctypes.c_int * nprob)()
+        it = (ctypes.c_int * nprob)()
         st_o = dev.lib.gbpa_batched_pcg_solve_ex(dev.ctx, nprob, arr, precision, schedule, rel_tol, 0.0,
-                                                 max_it, None, cv, None, ctypes.byref(sec))
-        return st_o, sec.value, int(sum(cv)), [pr["x"].clone() for pr in probs]
+                                                 max_it, it, cv, None, ctypes.byref(sec))
+        torch.cuda.synchronize()
+        return st_o, sec.value, int(sum(cv)), list(it), [pr["x"].clone() for pr in probs]
 
-    st_pe, secs_pe, conv_pe, pe_sols = other(_lib.GBPA_F64, _lib.GBPA_BATCH_PERSISTENT)
-    st_x2, secs_x2, conv_x2, x2_sols = other(_lib.GBPA_F64X2, _lib.GBPA_BATCH_GRAPH)
-    st = dev.lib.gbpa_batched_pcg_solve(dev.ctx, nprob, arr, rel_tol, 0.0, max_it, its, conv, None,
-                                        ctypes.byref(secs))
-    torch.cuda.synchronize()
+    def max_err(sols, ref):
+        return max(float(torch.linalg.norm(xs - xr) / torch.linalg.norm(xr)) for xs, xr in zip(sols, ref))
 
-    def max_err(sols):
-        return max(float(torch.linalg.norm(xs - pr["x"]) / torch.linalg.norm(pr["x"]))
-                   for xs, pr in zip(sols, probs))
-    x2_err, pe_err = max_err(x2_sols), max_err(pe_sols)
-    del x2_sols, pe_sols
-    seq = 0.0
-    worst = 0.0
+    out_pe = None
+    if persistent:
+        st_pe, secs_pe, conv_pe, _, pe_sols = batched(_lib.GBPA_F64, _lib.GBPA_BATCH_PERSISTENT)
+    st_x2, secs_x2, conv_x2, its_x2, x2_sols = batched(_lib.GBPA_F64X2, _lib.GBPA_BATCH_GRAPH)
+    st, secs, conv, its, f64_sols = batched(_lib.GBPA_F64, _lib.GBPA_BATCH_GRAPH)
+    if persistent:
+        out_pe = {"status": st_pe, "seconds_one_launch": secs_pe, "converged": conv_pe,
+                  "max_rel_l2_vs_graph": max_err(pe_sols, f64_sols)}
+        del pe_sols
+    x2_err = max_err(x2_sols, f64_sols)
+    # one after another: the single-problem PCG, native FP64 and double-float
     info = _lib.SolveInfo()
     P = lambda t: ctypes.c_void_p(t.data_ptr())
+    seq, seq_x2, worst, worst_x2 = 0.0, 0.0, 0.0, 0.0
     for k, pr in enumerate(probs):
         X = torch.zeros_like(pr["x"])
-        s2 = dev.lib.gbpa_pcg_solve(pr["A"].handle, P(pr["dinv"]), P(pr["b"]), P(X), rel_tol, 0.0, max_it, 0,
-                                    ctypes.byref(info))
+        dev.lib.gbpa_pcg_solve(pr["A"].handle, P(pr["dinv"]), P(pr["b"]), P(X), rel_tol, 0.0, max_it, 0,
+                               ctypes.byref(info))
         seq += info.seconds
-        worst = max(worst, float(torch.linalg.norm(pr["x"] - X) / torch.linalg.norm(X)))
+        worst = max(worst, float(torch.linalg.norm(f64_sols[k] - X) / torch.linalg.norm(X)))
+        integ = pr["integ"]
+        Ax2 = PAOperator(0, pr["R"], integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=pr["ess_h"],
+                         precision=_lib.GBPA_F64X2)
+        X2 = torch.zeros_like(pr["x"])
+        dev.lib.gbpa_pcg_solve(Ax2.handle, P(pr["dinv"]), P(pr["b"]), P(X2), rel_tol, 0.0, max_it, 0,
+                               ctypes.byref(info))
+        seq_x2 += info.seconds
+        worst_x2 = max(worst_x2, float(torch.linalg.norm(x2_sols[k] - X2) / torch.linalg.norm(X2)))
+        del Ax2, X, X2
     orders = [pr["p"] for pr in probs]
     dof_its = sum((probs[k]["b"].numel()) * its[k] for k in range(nprob))
     return {"workload": f"{nprob} Dirichlet Poisson problems, n~U[4,16], p~U{{2..6}}, lognormal kappa, "
-                        f"{total} DOFs total", "schedule": "graph", "status": st,
-            "seconds_batched": secs.value,
-            "seconds_sequential_pcg": seq, "speedup_vs_sequential": seq / max(secs.value, 1e-30),
-            "gdof_iterations_per_s": dof_its / max(secs.value, 1e-30) / 1e9,
-            "converged": int(sum(conv)), "iterations_max": max(its), "iterations_min": min(its),
-            "max_rel_l2_vs_sequential": worst, "dofs_total": total, "dof_iterations": dof_its,
-            "persistent": {"status": st_pe, "seconds_one_launch": secs_pe, "converged": conv_pe,
-                           "speedup_vs_sequential": seq / max(secs_pe, 1e-30),
-                           "max_rel_l2_vs_graph": pe_err},
-            "f64x2": {"status": st_x2, "seconds_batched": secs_x2, "converged": conv_x2,
-                      "speedup_vs_sequential_fp64": seq / max(secs_x2, 1e-30),
-                      "max_rel_l2_vs_fp64_batched": x2_err},
+                        f"{total} DOFs total, each to rel. residual {rel_tol:g}", "schedule": "graph",
+            "arithmetic": "double-float (FP64 data; FP64-accurate products on the FP32 pipes)",
+            "status": st_x2, "seconds_batched": secs_x2, "converged": conv_x2,
+            "speedup_vs_sequential_fp64": seq / max(secs_x2, 1e-30),
+            "speedup_vs_sequential_same_arithmetic": seq_x2 / max(secs_x2, 1e-30),
+            "max_rel_l2_vs_fp64_batched": x2_err, "max_rel_l2_vs_sequential_same_arithmetic": worst_x2,
+            "seconds_sequential_fp64": seq, "seconds_sequential_f64x2": seq_x2,
+            "gdof_iterations_per_s": sum(probs[k]["b"].numel() * its_x2[k] for k in range(nprob))
+            / max(secs_x2, 1e-30) / 1e9,
+            "iterations_max": max(its_x2), "iterations_min": min(its_x2),
+            "fp64": {"status": st, "seconds_batched": secs, "converged": conv,
+                     "speedup_vs_sequential_fp64": seq / max(secs, 1e-30),
+                     "max_rel_l2_vs_sequential": worst, "dof_iterations": dof_its,
+                     "iterations_max": max(its), "iterations_min": min(its)},
+            "persistent_fp64": out_pe, "dofs_total": total,
             "problems_per_order": {str(q): orders.count(q) for q in range(2, 7)}}
 
 
@@ -999,6 +1023,23 @@ def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
     B[torch.from_numpy(ess).long().cuda()] = 0.0
     B = B.contiguous()
     P = lambda t: ctypes.c_void_p(t.data_ptr())
+    # the FP32 block L->L apply (the inner solve's operator) against nrhs
+    # single applies of the same vectors
+    B32 = B.float().contiguous()
+    Y32 = torch.empty_like(B32)
+    cols = [B32[:, r].contiguous() for r in range(nrhs)]
+    ycol = torch.empty_like(cols[0])
+    ms_blk = _event_ms(lambda: _lib.check(dev.lib.gbpa_operator_mult_block(A32.handle, nrhs, P(B32), P(Y32)),
+                                          "mult_block"), 20)
+    ms_one = _event_ms(lambda: [A32.Mult(c, ycol) for c in cols], 20)
+    block_err = 0.0
+    for r in range(nrhs):
+        A32.Mult(cols[r], ycol)
+        block_err = max(block_err, float(torch.linalg.norm(Y32[:, r] - ycol) / torch.linalg.norm(ycol)))
+    apply_cmp = {"ms_block_apply": ms_blk, "ms_single_applies": ms_one,
+                 "speedup_per_vector": ms_one / max(ms_blk, 1e-30),
+                 "max_rel_l2_block_vs_single": block_err, "arithmetic": "f32"}
+    del B32, Y32, cols, ycol
     X = torch.zeros_like(B)
     info = (_lib.SolveInfo * nrhs)()
     st = dev.lib.gbpa_pcg_solve_block_mixed(A64.handle, A32.handle, nrhs, P(M.dinv.float()), P(B), P(X),
@@ -1007,7 +1048,8 @@ def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
                        f"{nrhs} RHS~U[-1,1]", "status": st, "seconds_block_mixed": info[0].seconds,
            "outer": [info[r].outer_iterations for r in range(nrhs)],
            "inner_iterations": [info[r].inner_iterations for r in range(nrhs)],
-           "true_rel_residual": [info[r].true_rel_residual for r in range(nrhs)]}
+           "true_rel_residual": [info[r].true_rel_residual for r in range(nrhs)],
+           "block_apply": apply_cmp}
     # the same right-hand sides one at a time (single-vector mixed solves)
     seq = 0.0
     si = _lib.SolveInfo()
@@ -1060,7 +1102,7 @@ def main():
     if args.batched:
         from mfem_gb300.pa import Device
         Device("cuda", dist_info()[2])
-        print(json.dumps({"batched": run_batched_form(args.nprob)}), flush=True)
+        print(json.dumps({"batched": run_batched_form(args.nprob, persistent=True)}), flush=True)
         return 0
     if args.sweep:
         from mfem_gb300.pa import Device
