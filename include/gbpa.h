@@ -594,6 +594,16 @@ enum gbpa_layout { GBPA_LAYOUT_SLAB2D = 0, GBPA_LAYOUT_3D = 1, GBPA_LAYOUT_TC = 
 int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, int layout,
                           int nbz);
 int gbpa_get_apply_layout(int kind, int precision, int d1d, int q1d, int *nbz);
+/* The element kernel of the FP32 block diffusion apply
+ * (gbpa_operator_mult_block and the block solvers) for (d1d, q1d, nrhs):
+ * GBPA_LAYOUT_TC, the tensor-core block kernel (a tile of 128 / nrhs elements
+ * times nrhs vectors; the default where one exists: (5,6) and (6,7) with
+ * nrhs 8), or GBPA_LAYOUT_SLAB2D, the CUDA-core block kernel. TC where no
+ * kernel exists returns GBPA_ERR_UNSUPPORTED. An operator prepares the
+ * tensor-core data (tables, scales, re-laid qdata: about the size of its
+ * qdata) at its first block apply or block solve with the layout selected. */
+int gbpa_set_block_apply_layout(int d1d, int q1d, int nrhs, int layout);
+int gbpa_get_block_apply_layout(int d1d, int q1d, int nrhs);
 
 /* ------------------------------------------------ failure-detection test */
 /* No counterpart in the reference. Makes one of the library's bounded device

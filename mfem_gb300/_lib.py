@@ -131,6 +131,8 @@ SIGNATURES = {
     "gbpa_get_elements_per_block": (I, [I, I, I, I]),
     "gbpa_set_apply_layout": (I, [I, I, I, I, I, I]),
     "gbpa_get_apply_layout": (I, [I, I, I, I, ctypes.POINTER(I)]),
+    "gbpa_set_block_apply_layout": (I, [I, I, I, I]),
+    "gbpa_get_block_apply_layout": (I, [I, I, I]),
 }
 
 _lib = None

@@ -9,6 +9,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <new>
+#include <vector>
 
 namespace gbpa
 {
@@ -273,6 +275,25 @@ __global__ void blk_scatter_kernel(int ndofs, int R, const int *__restrict__ off
    }
 }
 
+// The same with one thread per dof for all R right-hand sides: the row's
+// indices loaded once, R values per slot in one vector load (bit-identical
+// sums); y and xc aligned to R * sizeof(T).
+template <typename T, int R>
+__global__ void blk_scatter_rhs_kernel(int ndofs, const int *__restrict__ offsets,
+                                       const int *__restrict__ indices, const T *__restrict__ yE,
+                                       T *__restrict__ y, const unsigned char *__restrict__ mask,
+                                       const T *__restrict__ xc)
+{
+   using V = RhsVec<T, R>;
+   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndofs; i += gridDim.x * blockDim.x)
+   {
+      V v;
+      if (mask && mask[i]) { v = reinterpret_cast<const V *>(xc)[i]; }
+      else { csr_row_sum_rhs<T, R>(offsets, indices, yE, i, v.v); }
+      reinterpret_cast<V *>(y)[i] = v;
+   }
+}
+
 // per-right-hand-side dot products (a, b) -> out[R] (device)
 template <typename T>
 __global__ void blk_dot_kernel(int64_t n, int R, const T *__restrict__ a, const T *__restrict__ b,
@@ -363,8 +384,73 @@ __global__ void blk_residual_kernel(int64_t n, const double *b, double *r)
 // ------------------------------------------------------------ host side
 static bool rhs_ok(int R) { return R == 1 || R == 2 || R == 4 || R == 8; }
 
+// The tensor-core block apply's data for R vectors (FP32 symmetric diffusion
+// with a block kernel for (D, Q, R), while that layout is selected): built
+// once, outside any graph capture (every block path prepares its scratch
+// before it captures).
+static bool block_tc_wanted(const gbpa_operator *op, int R)
+{
+   const gbpa_operator_desc &d = op->d;
+   return d.precision == GBPA_F32 && d.kind == GBPA_DIFFUSION && d.symm && tc::block_supported(d.d1d, d.q1d, R) &&
+          block_apply_layout(d.d1d, d.q1d, R) == GBPA_LAYOUT_TC;
+}
+
+static int ensure_block_tc(gbpa_operator *op, int R)
+{
+   if (!block_tc_wanted(op, R) || (op->tcb && op->tcb_nrhs == R)) { return GBPA_SUCCESS; }
+   const gbpa_operator_desc &d = op->d;
+   if (op->tcb)
+   {
+      cudaStreamSynchronize(op->ctx->stream);
+      tc::free_tables(op->tcb);
+      delete op->tcb;
+      op->tcb = nullptr;
+      cudaFree(op->tcb_qdata);
+      op->tcb_qdata = nullptr;
+   }
+   op->tcb_nrhs = 0;
+   const int n = d.q1d * d.d1d;
+   std::vector<float> bf(n), gf(n);
+   int rc = check_cuda(cudaMemcpy(bf.data(), d.B, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy B");
+   if (!rc) { rc = check_cuda(cudaMemcpy(gf.data(), d.G, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy G"); }
+   if (rc) { return rc; }
+   std::vector<double> bd(bf.begin(), bf.end()), gd(gf.begin(), gf.end());
+   op->tcb = new (std::nothrow) tc::Tables;
+   if (!op->tcb) { return GBPA_ERR_OUT_OF_MEMORY; }
+   rc = tc::build_block_tables(d.d1d, d.q1d, bd.data(), gd.data(), op->tcb);
+   if (!rc && !op->tcb_qscale)
+   {
+      rc = check_cuda(cudaMalloc(&op->tcb_qscale, sizeof(float) * d.ne), "cudaMalloc(tc block scale)");
+   }
+   if (!rc)
+   {
+      rc = tc::launch_qscale(op->ctx, d.ne, d.q1d, (const float *)d.qdata, (float)op->tcb->R, op->tcb_qscale);
+   }
+   if (!rc)
+   {
+      const int64_t nq = tc::block_qdata_size(d.d1d, d.q1d, R, d.ne);
+      rc = check_cuda(cudaMalloc(&op->tcb_qdata, sizeof(float) * nq), "cudaMalloc(tc block qdata)");
+   }
+   if (!rc)
+   {
+      rc = tc::launch_block_transpose_qdata(op->ctx, d.ne, d.d1d, d.q1d, R, (const float *)d.qdata,
+                                            op->tcb_qdata);
+   }
+   if (rc)
+   {
+      if (op->tcb) { tc::free_tables(op->tcb); delete op->tcb; op->tcb = nullptr; }
+      cudaFree(op->tcb_qdata);
+      op->tcb_qdata = nullptr;
+      return rc;
+   }
+   op->tcb_nrhs = R;
+   return GBPA_SUCCESS;
+}
+
 static int ensure_block_scratch(gbpa_operator *op, int R)
 {
+   const int rt = ensure_block_tc(op, R);
+   if (rt) { return rt; }
    if (op->yEb && op->yEb_nrhs >= R) { return GBPA_SUCCESS; }
    cudaFree(op->yEb);
    op->yEb = nullptr;
@@ -382,6 +468,12 @@ static int block_apply_evec(gbpa_operator *op, int R, const T *x, const int *ski
    if (d.kind != GBPA_DIFFUSION) { return GBPA_ERR_UNSUPPORTED; }
    if constexpr (sizeof(T) == 4)
    {
+      if (op->tcb && op->tcb_nrhs == R && block_tc_wanted(op, R))
+      {
+         return tc::launch_diffusion_block_f32(op->ctx, d.ne, d.d1d, d.q1d, R, *op->tcb, op->tcb_qdata,
+                                               op->tcb_qscale, x, op->gather(), op->gather_mask(),
+                                               (float *)op->yEb, skip);
+      }
       return launch_diffusion_block_f32(op->ctx, d.ne, R, d.symm ? 1 : 0, d.d1d, d.q1d,
                                         (const float *)d.B, (const float *)d.G,
                                         (const float *)d.qdata, x, op->gather(), op->gather_mask(),
@@ -404,6 +496,21 @@ static int block_mult(gbpa_operator *op, int R, const T *x, T *y)
    rc = block_apply_evec<T>(op, R, x, nullptr);
    if (rc) { return rc; }
    const int64_t n = (int64_t)op->d.ndofs * R;
+   const uintptr_t vec = (uintptr_t)(sizeof(T) * R);
+   if (R > 1 && (uintptr_t)y % vec == 0 && (uintptr_t)x % vec == 0)
+   {
+      const unsigned grid = grid_for(op->d.ndofs, 256, 8 * op->ctx->num_sms);
+      const int nd = op->d.ndofs;
+      const T *yE = (const T *)op->yEb;
+      cudaStream_t s = op->ctx->stream;
+      switch (R)
+      {
+      case 2: blk_scatter_rhs_kernel<T, 2><<<grid, 256, 0, s>>>(nd, op->d.offsets, op->d.indices, yE, y, op->mask, x); break;
+      case 4: blk_scatter_rhs_kernel<T, 4><<<grid, 256, 0, s>>>(nd, op->d.offsets, op->d.indices, yE, y, op->mask, x); break;
+      default: blk_scatter_rhs_kernel<T, 8><<<grid, 256, 0, s>>>(nd, op->d.offsets, op->d.indices, yE, y, op->mask, x); break;
+      }
+      return last_launch(op->ctx, "blk_scatter_rhs");
+   }
    blk_scatter_kernel<T><<<grid_for(n, 256), 256, 0, op->ctx->stream>>>(
       op->d.ndofs, R, op->d.offsets, op->d.indices, (const T *)op->yEb, y, op->mask, x);
    return last_launch(op->ctx, "blk_scatter");

@@ -751,6 +751,39 @@ extern "C" int gbpa_set_apply_layout(int kind, int precision, int d1d, int q1d, 
    return GBPA_SUCCESS;
 }
 
+// FP32 block diffusion apply, per (D, Q, nrhs): the tensor-core kernel where
+// one exists, unless set to the CUDA-core block kernel
+static std::unordered_map<int, int> g_block_layout;
+
+static int block_key(int D, int Q, int nrhs) { return (D * 64 + Q) * 64 + nrhs; }
+
+int gbpa::block_apply_layout(int D, int Q, int nrhs)
+{
+   if (!gbpa::tc::block_supported(D, Q, nrhs)) { return GBPA_LAYOUT_SLAB2D; }
+   std::lock_guard<std::mutex> lock(g_nbz_mu);
+   auto it = g_block_layout.find(block_key(D, Q, nrhs));
+   return it == g_block_layout.end() ? GBPA_LAYOUT_TC : it->second;
+}
+
+extern "C" int gbpa_set_block_apply_layout(int d1d, int q1d, int nrhs, int layout)
+{
+   if (d1d < 1 || q1d < 1 || d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || nrhs < 1 ||
+       (layout != GBPA_LAYOUT_SLAB2D && layout != GBPA_LAYOUT_TC))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   if (layout == GBPA_LAYOUT_TC && !gbpa::tc::block_supported(d1d, q1d, nrhs)) { return GBPA_ERR_UNSUPPORTED; }
+   std::lock_guard<std::mutex> lock(g_nbz_mu);
+   g_block_layout[block_key(d1d, q1d, nrhs)] = layout;
+   return GBPA_SUCCESS;
+}
+
+extern "C" int gbpa_get_block_apply_layout(int d1d, int q1d, int nrhs)
+{
+   if (d1d < 1 || q1d < 1 || d1d > GBPA_MAX_1D || q1d > GBPA_MAX_1D || nrhs < 1) { return GBPA_ERR_INVALID_ARGUMENT; }
+   return gbpa::block_apply_layout(d1d, q1d, nrhs);
+}
+
 extern "C" int gbpa_get_apply_layout(int kind, int precision, int d1d, int q1d, int *nbz)
 {
    if (kind < 0 || kind > 1 || precision < 0 || precision > 2) { return GBPA_ERR_INVALID_ARGUMENT; }

@@ -178,6 +178,8 @@ int elements_per_block(int kind, int precision, int D, int Q);
 // GBPA_LAYOUT_SLAB2D (default) or GBPA_LAYOUT_3D, with *nbz the 3D kernel's
 // elements per block.
 int apply_layout(int kind, int precision, int D, int Q, int *nbz);
+// FP32 block diffusion apply: GBPA_LAYOUT_TC or GBPA_LAYOUT_SLAB2D for (D, Q, nrhs)
+int block_apply_layout(int D, int Q, int nrhs);
 
 // Vector mass with a matrix coefficient (vdim 3): block-major qdata
 // (Q^3, NE, 9), y_E += sum over the coupled blocks (gbpa_vector_coupled.cu).

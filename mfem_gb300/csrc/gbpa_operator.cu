@@ -499,6 +499,9 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    if (op->tct) { tc::free_tables(op->tct); delete op->tct; }
    cudaFree(op->tc_qscale);
    cudaFree(op->tc_qdata);
+   if (op->tcb) { tc::free_tables(op->tcb); delete op->tcb; }
+   cudaFree(op->tcb_qscale);
+   cudaFree(op->tcb_qdata);
    delete op;
    return GBPA_SUCCESS;
 }

@@ -44,6 +44,13 @@ struct gbpa_operator
    // block (multi right-hand side) scratch: E-vector for nrhs interleaved
    void *yEb = nullptr;
    int yEb_nrhs = 0;
+   // FP32 block diffusion on the tensor cores, prepared for tcb_nrhs vectors:
+   // split Kronecker tables, per-element output scales, qdata in the block
+   // kernel's tile layout
+   gbpa::tc::Tables *tcb = nullptr;
+   float *tcb_qscale = nullptr;
+   float *tcb_qdata = nullptr;
+   int tcb_nrhs = 0;
    // host-buffer Mult: device staging for pageable x / y (2 L-vectors)
    void *stage = nullptr;
 };

@@ -35,5 +35,17 @@ int launch_transpose_qdata(gbpa_ctx *ctx, int ne, int D, int Q, const float *qd,
 int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, const float *qd,
                          const float *qscale, const float *x, const int *gmap, const unsigned char *mask,
                          float *y, int mode, const int *skip = nullptr);
+
+// Block form (gbpa_apply_tc_block.cu): nrhs right-hand sides stored
+// interleaved (x[j nrhs + r]), block E-vector out (y[(e D^3 + i) nrhs + r]);
+// a tile is 128 / nrhs elements times nrhs vectors.
+bool block_supported(int D, int Q, int nrhs);
+int build_block_tables(int D, int Q, const double *B, const double *G, Tables *t);
+// The qdata re-laid per tile of 128 / nrhs elements (block_qdata_size floats).
+int64_t block_qdata_size(int D, int Q, int nrhs, int ne);
+int launch_block_transpose_qdata(gbpa_ctx *ctx, int ne, int D, int Q, int nrhs, const float *qd, float *qT);
+int launch_diffusion_block_f32(gbpa_ctx *ctx, int ne, int D, int Q, int nrhs, const Tables &t, const float *qT,
+                               const float *qscale, const float *x, const int *gmap, const unsigned char *mask,
+                               float *y, const int *skip = nullptr);
 } // namespace tc
 } // namespace gbpa

@@ -181,3 +181,109 @@ def test_tc_layout_api():
     assert lib.gbpa_set_apply_layout(0, 1, 7, 8, TC, 0) == -2      # order without a kernel
     with tc_layout(lib, 5, 6):
         assert lib.gbpa_get_apply_layout(0, 1, 5, 6, None) == TC
+
+
+# ----------------------------------------------------------------- block form
+class block_layout:
+    """Select the FP32 block apply's kernel for (D, Q, nrhs) while the block
+    runs; restore the previous choice afterwards."""
+
+    def __init__(self, lib, D, Q, R, layout):
+        self.lib, self.D, self.Q, self.R, self.layout = lib, D, Q, R, layout
+
+    def __enter__(self):
+        self.prev = self.lib.gbpa_get_block_apply_layout(self.D, self.Q, self.R)
+        assert self.lib.gbpa_set_block_apply_layout(self.D, self.Q, self.R, self.layout) == 0
+        return self
+
+    def __exit__(self, *a):
+        self.lib.gbpa_set_block_apply_layout(self.D, self.Q, self.R, self.prev)
+
+
+def _block_ops(n, p, curved):
+    from mfem_gb300 import fem
+    from mfem_gb300.pa import DiffusionIntegrator, FiniteElementSpace, PAOperator
+    mesh = fem.CartesianMesh(n, jitter=0.0 if curved else 0.1, seed=3, curved=curved)
+    fes = FiniteElementSpace(mesh, p)
+    integ = DiffusionIntegrator("kappa")
+    integ.AssemblePA(fes, modes=fem.kappa_modes(5))
+    ess = fes.GetBoundaryTrueDofs()
+    A64 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess)
+    A32 = PAOperator(0, fes, integ.D, integ.Q, integ.B, integ.G, integ.qdata, ess=ess, precision=1)
+    return fes, integ, A64, A32
+
+
+def _mult_block(lib, op, R, X, Y):
+    import ctypes
+    return lib.gbpa_operator_mult_block(op.handle, R, ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(Y.data_ptr()))
+
+
+@pytest.mark.parametrize("p,n,curved", [(5, 5, True), (5, 7, False), (4, 9, False)])
+def test_tc_block_apply_against_fp64_and_cuda_core(p, n, curved):
+    """The tensor-core block apply (tiles of 16 elements x 8 interleaved
+    right-hand sides; 125, 343 and 729 elements leave a partial last tile) on
+    a constrained lognormal-kappa operator: every column against the FP64
+    single apply (the FP32 bar, 1e-5 relative L2) and against the CUDA-core
+    block kernel (two FP32 results, 5e-6)."""
+    from tests.gpu_util import dev
+    d = dev()
+    fes, integ, A64, A32 = _block_ops(n, p, curved)
+    D, Q, R, nd = integ.D, integ.Q, 8, fes.ndofs
+    assert d.lib.gbpa_get_block_apply_layout(D, Q, R) == TC
+    gen = torch.Generator(device="cuda").manual_seed(21)
+    X64 = (torch.rand(nd, R, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1).contiguous()
+    X32 = X64.float().contiguous()
+    Y = torch.full_like(X32, float("nan"))
+    assert _mult_block(d.lib, A32, R, X32, Y) == 0
+    with block_layout(d.lib, D, Q, R, 0):
+        Yc = torch.full_like(X32, float("nan"))
+        assert _mult_block(d.lib, A32, R, X32, Yc) == 0
+    torch.cuda.synchronize()
+    assert d.error_flags() == 0
+    for r in range(R):
+        y64 = torch.empty(nd, dtype=torch.float64, device="cuda")
+        A64.Mult(X64[:, r].contiguous(), y64)
+        yr = Y[:, r].double()
+        assert float(torch.linalg.norm(yr - y64) / torch.linalg.norm(y64)) < 1e-5, r
+        assert float(torch.linalg.norm(yr - Yc[:, r].double()) / torch.linalg.norm(y64)) < 5e-6, r
+
+
+def test_tc_block_apply_wide_dynamic_range():
+    """Right-hand side r scaled by 2^(8 r - 28), each varying smoothly over
+    2^-10..2^10 across the mesh: per-row scaling keeps every column at the
+    FP32 bar (1e-5 relative L2 against the FP64 apply)."""
+    from tests.gpu_util import dev
+    d = dev()
+    fes, integ, A64, A32 = _block_ops(6, 5, False)
+    nd, R = fes.ndofs, 8
+    t = torch.linspace(0, 1, nd, dtype=torch.float64, device="cuda")
+    gen = torch.Generator(device="cuda").manual_seed(22)
+    X64 = torch.empty(nd, R, dtype=torch.float64, device="cuda")
+    for r in range(R):
+        u = torch.rand(nd, dtype=torch.float64, device="cuda", generator=gen) * 2 - 1
+        X64[:, r] = u * torch.pow(2.0, 20.0 * t - 10.0) * 2.0 ** (8 * r - 28)
+    X32 = X64.float().contiguous()
+    X64 = X32.double().contiguous()
+    Y = torch.empty_like(X32)
+    assert _mult_block(d.lib, A32, R, X32, Y) == 0
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(Y).all())
+    for r in range(R):
+        y64 = torch.empty(nd, dtype=torch.float64, device="cuda")
+        A64.Mult(X64[:, r].contiguous(), y64)
+        assert float(torch.linalg.norm(Y[:, r].double() - y64) / torch.linalg.norm(y64)) < 1e-5, r
+
+
+def test_tc_block_layout_api():
+    from tests.gpu_util import dev
+    lib = dev().lib
+    assert lib.gbpa_get_block_apply_layout(6, 7, 8) == TC
+    assert lib.gbpa_get_block_apply_layout(5, 6, 8) == TC
+    assert lib.gbpa_get_block_apply_layout(4, 5, 8) == 0          # no tensor-core block kernel
+    assert lib.gbpa_get_block_apply_layout(6, 7, 4) == 0
+    assert lib.gbpa_set_block_apply_layout(4, 5, 8, TC) == -2
+    assert lib.gbpa_set_block_apply_layout(6, 7, 8, 1) == -1       # the 3D layout has no block kernel
+    assert lib.gbpa_set_block_apply_layout(0, 7, 8, 0) == -1
+    with block_layout(lib, 6, 7, 8, 0):
+        assert lib.gbpa_get_block_apply_layout(6, 7, 8) == 0
+    assert lib.gbpa_get_block_apply_layout(6, 7, 8) == TC
