@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--combined", action="store_true", help="run only the combined-form comparison")
     ap.add_argument("--combined-n", type=int, default=24, help="54: ~19.9 M DOFs at p=5")
     ap.add_argument("--no-reference", action="store_true", help="combined form: skip the FP64 reference solve")
+    ap.add_argument("--combined-apply-only", action="store_true",
+                    help="combined form: only the block apply against single applies (no solves)")
     ap.add_argument("--mg", action="store_true", help="run only the p-multigrid-preconditioned solve")
     ap.add_argument("--sweep", action="store_true", help="run only the p = 1..8 apply sweep")
     ap.add_argument("--sweep-dofs", type=float, default=8e6)
@@ -999,7 +1001,7 @@ def run_mg_form(n=77, p=4, orders=(1, 2, 4), with_jacobi=False, rel_tol=1e-10):
     return out
 
 
-def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
+def run_combined_form(n=24, p=5, nrhs=8, with_reference=True, apply_only=False):
     """Combined form: unit cube mapped by x -> x + 0.05 sin(2 pi x) sin(2 pi y)
     sin(2 pi z) per component (order-3 geometry), H1 order p, lognormal kappa,
     nrhs right-hand sides ~ U[-1,1] solved together: FP32 block PCG inside FP64
@@ -1029,17 +1031,32 @@ def run_combined_form(n=24, p=5, nrhs=8, with_reference=True):
     Y32 = torch.empty_like(B32)
     cols = [B32[:, r].contiguous() for r in range(nrhs)]
     ycol = torch.empty_like(cols[0])
-    ms_blk = _event_ms(lambda: _lib.check(dev.lib.gbpa_operator_mult_block(A32.handle, nrhs, P(B32), P(Y32)),
-                                          "mult_block"), 20)
+    blk = lambda: _lib.check(dev.lib.gbpa_operator_mult_block(A32.handle, nrhs, P(B32), P(Y32)), "mult_block")
+    D, Q = integ.D, integ.Q
+    layout = dev.lib.gbpa_get_block_apply_layout(D, Q, nrhs)
+    ms_blk = _event_ms(blk, 20)
+    ms_cc = None
+    if layout == 2:
+        # the CUDA-core block kernel on the same vectors, for comparison
+        dev.lib.gbpa_set_block_apply_layout(D, Q, nrhs, 0)
+        try:
+            ms_cc = _event_ms(blk, 20)
+        finally:
+            dev.lib.gbpa_set_block_apply_layout(D, Q, nrhs, 2)
+        blk()
     ms_one = _event_ms(lambda: [A32.Mult(c, ycol) for c in cols], 20)
     block_err = 0.0
     for r in range(nrhs):
         A32.Mult(cols[r], ycol)
         block_err = max(block_err, float(torch.linalg.norm(Y32[:, r] - ycol) / torch.linalg.norm(ycol)))
-    apply_cmp = {"ms_block_apply": ms_blk, "ms_single_applies": ms_one,
+    apply_cmp = {"ms_block_apply": ms_blk, "block_kernel": LAYOUT_NAMES.get(layout, str(layout)),
+                 "ms_block_apply_cuda_core": ms_cc, "ms_single_applies": ms_one,
                  "speedup_per_vector": ms_one / max(ms_blk, 1e-30),
                  "max_rel_l2_block_vs_single": block_err, "arithmetic": "f32"}
     del B32, Y32, cols, ycol
+    if apply_only:
+        return {"workload": f"curved order-3 geometry, n={n}^3, p={p}, q={p + 2}, {nd} DOFs, lognormal kappa, "
+                            f"{nrhs} RHS~U[-1,1]", "block_apply": apply_cmp}
     X = torch.zeros_like(B)
     info = (_lib.SolveInfo * nrhs)()
     st = dev.lib.gbpa_pcg_solve_block_mixed(A64.handle, A32.handle, nrhs, P(M.dinv.float()), P(B), P(X),
@@ -1117,8 +1134,8 @@ def main():
     if args.combined:
         from mfem_gb300.pa import Device
         Device("cuda", dist_info()[2])
-        print(json.dumps({"combined": run_combined_form(args.combined_n, 5, 8, not args.no_reference)}),
-              flush=True)
+        print(json.dumps({"combined": run_combined_form(args.combined_n, 5, 8, not args.no_reference,
+                                                        args.combined_apply_only)}), flush=True)
         return 0
     return run_gpu(args)
 

@@ -5,7 +5,9 @@ reference's own apply on the golden cases (the FP32 bar, 1e-5 relative L2),
 against the CUDA-core FP32 kernel, on constrained and atomic-scatter
 operators, on element counts that leave a partial last tile, on inputs whose
 magnitudes span many binades (the per-element power-of-two scaling), and
-inside the mixed-precision solve."""
+inside the mixed-precision solve. The block form (tiles of 16 elements x 8
+interleaved right-hand sides) is checked column by column against the FP64
+apply and the CUDA-core block kernel."""
 import numpy as np
 import pytest
 import torch
