@@ -227,6 +227,14 @@ typedef struct gbpa_operator *gbpa_operator_t;
 
 int gbpa_operator_create(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
                          gbpa_operator_t *op);
+/* gbpa_operator_create with every array of the descriptor (B, G, qdata,
+ * gather_map, offsets, indices, ess) in HOST memory: the library keeps
+ * device copies, freed by gbpa_operator_destroy. For hosts whose arrays
+ * live in host memory -- an MFEM built without CUDA, whose
+ * PABilinearFormExtension then forwards Mult to gbpa_operator_mult_host
+ * (integration/gbpa_shim.cpp). */
+int gbpa_operator_create_host(gbpa_ctx_t ctx, const gbpa_operator_desc *desc,
+                              gbpa_operator_t *op);
 int gbpa_operator_destroy(gbpa_operator_t op);
 /* y = A x (L-vectors, the descriptor's precision). With ess dofs:
  * y = A (x with ess zeroed), then y[ess] = x[ess]. */

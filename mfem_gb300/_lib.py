@@ -86,6 +86,7 @@ SIGNATURES = {
     "gbpa_mass_apply3d_f32": (I, [P, I, I, I, P, P, P, P]),
     "gbpa_mass_diagonal3d": (I, [P, I, I, I, P, P, P]),
     "gbpa_operator_create": (I, [P, ctypes.POINTER(OperatorDesc), ctypes.POINTER(P)]),
+    "gbpa_operator_create_host": (I, [P, ctypes.POINTER(OperatorDesc), ctypes.POINTER(P)]),
     "gbpa_operator_destroy": (I, [P]),
     "gbpa_operator_mult": (I, [P, P, P]),
     "gbpa_operator_mult_host": (I, [P, P, P]),

@@ -487,6 +487,58 @@ extern "C" int gbpa_operator_set_element_markers(gbpa_operator_t op, const int *
    return rc ? rc : rl;
 }
 
+// The descriptor's arrays in host memory: one device block holds copies of
+// them (freed with the operator), then the operator is created on the copies.
+extern "C" int gbpa_operator_create_host(gbpa_ctx_t ctx, const gbpa_operator_desc *desc, gbpa_operator_t *out)
+{
+   if (!ctx || !desc || !out) { return GBPA_ERR_INVALID_ARGUMENT; }
+   *out = nullptr;
+   const gbpa_operator_desc &d = *desc;
+   if (d.ne < 0 || d.ndofs < 0 || d.n_ess < 0 || d.d1d < 1 || d.q1d < 1 ||
+       (d.kind != GBPA_DIFFUSION && d.kind != GBPA_MASS) ||
+       (d.precision != GBPA_F64 && d.precision != GBPA_F32 && d.precision != GBPA_F64X2))
+   {
+      return GBPA_ERR_INVALID_ARGUMENT;
+   }
+   const size_t w = elem_bytes(d);
+   const size_t nE = (size_t)evec_size(d);
+   const size_t sizes[7] = {w * d.q1d * d.d1d, w * d.q1d * d.d1d, w * (size_t)qdata_size(d), sizeof(int) * nE,
+                            sizeof(int) * ((size_t)d.ndofs + 1), sizeof(int) * nE, sizeof(int) * (size_t)d.n_ess};
+   const void *src[7] = {d.B, d.G, d.qdata, d.gather_map, d.offsets, d.indices, d.ess};
+   for (int k = 0; k < 7; ++k)
+   {
+      if (sizes[k] && !src[k] && k != 6) { return GBPA_ERR_INVALID_ARGUMENT; }
+   }
+   size_t off[7], total = 0;
+   for (int k = 0; k < 7; ++k)
+   {
+      off[k] = total;
+      total += (sizes[k] + 255) / 256 * 256;
+   }
+   unsigned char *blk = nullptr;
+   int rc = check_cuda(cudaMalloc(&blk, total ? total : 256), "cudaMalloc(host operator copies)");
+   for (int k = 0; k < 7 && !rc; ++k)
+   {
+      if (sizes[k] && src[k])
+      {
+         rc = check_cuda(cudaMemcpy(blk + off[k], src[k], sizes[k], cudaMemcpyHostToDevice), "copy operator array");
+      }
+   }
+   if (rc) { cudaFree(blk); return rc; }
+   gbpa_operator_desc dd = d;
+   dd.B = blk + off[0];
+   dd.G = blk + off[1];
+   dd.qdata = blk + off[2];
+   dd.gather_map = (const int *)(blk + off[3]);
+   dd.offsets = (const int *)(blk + off[4]);
+   dd.indices = (const int *)(blk + off[5]);
+   dd.ess = d.n_ess > 0 && d.ess ? (const int *)(blk + off[6]) : nullptr;
+   rc = gbpa_operator_create(ctx, &dd, out);
+   if (rc) { cudaFree(blk); return rc; }
+   (*out)->owned = blk;
+   return GBPA_SUCCESS;
+}
+
 extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
 {
    if (!op) { return GBPA_SUCCESS; }
@@ -502,6 +554,7 @@ extern "C" int gbpa_operator_destroy(gbpa_operator_t op)
    if (op->tcb) { tc::free_tables(op->tcb); delete op->tcb; }
    cudaFree(op->tcb_qscale);
    cudaFree(op->tcb_qdata);
+   cudaFree(op->owned);
    delete op;
    return GBPA_SUCCESS;
 }

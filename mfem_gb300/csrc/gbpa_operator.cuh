@@ -53,6 +53,8 @@ struct gbpa_operator
    int tcb_nrhs = 0;
    // host-buffer Mult: device staging for pageable x / y (2 L-vectors)
    void *stage = nullptr;
+   // gbpa_operator_create_host: the device copies of the descriptor's arrays
+   void *owned = nullptr;
 };
 
 namespace gbpa
