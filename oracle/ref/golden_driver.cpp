@@ -335,6 +335,27 @@ static void run_case(const Case &c, const std::string &root)
       Vector dE(R->Height()); dE = 0.0; dint->AssembleDiagonalPA(dE);
       if (!c.solve) { save(dir, "diagE_diff", dE); }
    }
+   if (!c.solve && std::string(c.name) == "jit3_p3_fn")
+   {
+      // domain-integrator element markers (AddDomainIntegrator(integ, marker):
+      // AddMultWithMarkers and the marked diagonal) on a copy of the mesh
+      // whose element e has attribute 1 + e % 3, marker {1, 0, 1}; same dofs
+      Mesh mm(mesh, true);
+      std::vector<int> attr(ne);
+      for (int e = 0; e < ne; e++) { attr[e] = 1 + e % 3; mm.SetAttribute(e, attr[e]); }
+      mm.SetAttributes();
+      FiniteElementSpace fm(&mm, &fec);
+      Array<int> marker(3);
+      marker[0] = 1; marker[1] = 0; marker[2] = 1;
+      BilinearForm am(&fm);
+      am.SetAssemblyLevel(AssemblyLevel::PARTIAL);
+      am.AddDomainIntegrator(new DiffusionIntegrator(kfn, &ir), marker);
+      am.Assemble();
+      Vector ymk(ndofs); am.Mult(x, ymk); save(dir, "y_diff_markers", ymk);
+      Vector dmk(ndofs); am.AssembleDiagonal(dmk); save(dir, "diag_diff_markers", dmk);
+      save_ints(dir, "elem_attr", attr);
+      save(dir, "markers", marker);
+   }
 
    BilinearForm m(&fes);
    m.SetAssemblyLevel(AssemblyLevel::PARTIAL);

@@ -1,8 +1,9 @@
 """Domain-integrator element markers (PABilinearFormExtension::
 AddMultWithMarkers, fem/bilinearform_ext.cpp:530-550,753-774,807-847) through
 gbpa_operator_set_element_markers: only elements whose attribute is marked
-contribute to Mult and to AssembleDiagonal. Checked against the oracle's
-restatement on a golden case, for the native FP64 and double-float
+contribute to Mult and to AssembleDiagonal. Checked against the reference's
+own marked Mult and diagonal (golden fixture), and against the oracle's
+restatement for more marker sets, for the native FP64 and double-float
 operators, constrained and not, CSR and atomic scatter; removing the markers
 restores the full operator; an attribute beyond the marker array is an index
 error."""
@@ -47,6 +48,27 @@ def test_markers_mult_matches_oracle(oracle, precision, scatter):
     op.SetElementMarkers(None, None)
     op.Mult(x, y)
     assert np.linalg.norm(H(y) - g["y_diff"]) / np.linalg.norm(g["y_diff"]) < 1e-12
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_markers_against_reference_fixture(precision):
+    """Mult and AssembleDiagonal of the marked operator against the
+    reference's own output for AddDomainIntegrator(integ, marker) (element
+    attributes 1 + e % 3, marker {1, 0, 1})."""
+    from mfem_gb300.pa import PAOperator
+    from tests.gpu_util import T, H
+    g, ne, ndofs, D, Q, R, B, G, qd = _setup()
+    op = PAOperator(0, R, D, Q, B, G, qd, precision=precision)
+    op.SetElementMarkers(g["elem_attr"].astype(np.int32), g["markers"].astype(np.int32))
+    x = T(g["x"])
+    y = torch.empty_like(x)
+    op.Mult(x, y)
+    ref = g["y_diff_markers"]
+    assert np.linalg.norm(H(y) - ref) / np.linalg.norm(ref) < 1e-12
+    diag = torch.empty(ndofs, dtype=torch.float64, device="cuda")
+    op.AssembleDiagonal(diag)
+    dref = g["diag_diff_markers"]
+    assert np.linalg.norm(H(diag) - dref) / np.linalg.norm(dref) < 1e-12
 
 
 def test_markers_diagonal_and_constrained(oracle):

@@ -195,6 +195,20 @@ def test_vector_mass_componentwise(oracle, case):
     assert np.linalg.norm(yE - ref) / np.linalg.norm(ref) < 1e-13
 
 
+def test_markers_oracle_matches_reference(oracle):
+    """The element-marker restatement against the reference's own
+    BilinearForm::Mult of a form added with AddDomainIntegrator(integ, marker)
+    (element attributes 1 + e % 3, marker {1, 0, 1}; fixture written by
+    oracle/ref/golden_driver.cpp)."""
+    g = load_golden("jit3_p3_fn")
+    ne, ndofs, D, Q = (int(v) for v in g["meta"][:4])
+    args = (0, ne, ndofs, True, D, Q, g["gather_map"], g["offsets"], g["indices"], g["B"], g["G"],
+            g["qdata_diff"])
+    y = oracle.pa_mult_markers(*args, g["elem_attr"], g["markers"], g["x"])
+    ref = g["y_diff_markers"]
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-12
+
+
 def test_markers_oracle_all_and_none_marked(oracle):
     """The element-marker restatement (AddMultWithMarkers) reduces to the
     plain L->L apply when every attribute is marked, gives zero when none
