@@ -57,11 +57,13 @@ struct Shape
 {
    static constexpr int D3 = D * D * D;
    static constexpr int KF = (D3 + 15) / 16 * 16;   // dofs, padded to the MMA K step
-   static constexpr int KH = KF / 2;                // dofs per half row
+   static constexpr int PARTS = 4;                  // epilogue threads per element row
+   static constexpr int EPI = 128 * PARTS;          // epilogue threads (16 warps)
+   static constexpr int KP = KF / PARTS;            // dofs per part of a row
    static constexpr int Q3 = Q * Q * Q;
    static constexpr int NC = 3 * PC;                // chunk columns (points x 3 components)
    static constexpr int NCH = (Q3 + PC - 1) / PC;   // chunks
-   static constexpr int NP = PC / 2;                // points of a chunk per thread (two halves per row)
+   static constexpr int NP = PC / PARTS;            // points of a chunk per thread
    static constexpr int NV = 3 * NP;                // chunk columns per thread
    static constexpr int NQ = 6 * NP;                // qdata values per thread and chunk
    static constexpr int M = 128;                    // elements per tile
@@ -73,7 +75,7 @@ struct Shape
    // one chunk ahead) and the next tile's gather map. The result is staged
    // over the ring and the qdata buffer after the tile's last GEMM.
    static constexpr int NT = 3;
-   static constexpr int QD_BYTES = 2 * NQ * M * 4;  // one tile-chunk of transposed qdata
+   static constexpr int QD_BYTES = PARTS * NQ * M * 4;  // one tile-chunk of transposed qdata
    static constexpr int OFF_T = 0;
    static constexpr int OFF_QD = OFF_T + NT * 2 * BF_LIMB;
    static constexpr int OFF_MAP = OFF_QD + QD_BYTES;
@@ -93,8 +95,8 @@ struct Shape
    {
       return row * STG + (D3 % 2 ? i : (i ^ (row & 31)));
    }
-   static constexpr int QT_CHUNK = 2 * NQ * M;      // floats of one tile-chunk of transposed qdata
-   static_assert(KF <= 128 && NC <= 64 && NC % 16 == 0 && NV % 8 == 0, "TMEM and MMA shapes");
+   static constexpr int QT_CHUNK = PARTS * NQ * M;  // floats of one tile-chunk of transposed qdata
+   static_assert(KF <= 128 && NC <= 64 && NC % 16 == 0 && NV == 12 && KP % 8 == 0, "TMEM and MMA shapes");
    static_assert(M * STG * 4 <= OFF_MAP, "output staging must fit over the ring and the qdata buffer");
    static_assert(KF / 2 <= 64 && NC / 2 <= 64, "A operands in TMEM");
    static_assert(SMEM <= 220 * 1024, "shared memory");
@@ -102,11 +104,12 @@ struct Shape
    static_assert(NCH >= NT, "the table ring is filled at the tile start");
 };
 
-// Persistent kernel: one CTA per SM walks tiles of 128 elements. Warps 0-7
-// (256 threads) gather, split, apply the qdata and write the result: thread t
-// owns element row r = 32 (warp % 4) + lane (its TMEM lane) and half
-// h = warp / 4 of that row's columns. One thread of warp 8 issues the MMAs,
-// one thread of warp 9 the bulk copies (gather map, table and qdata chunks),
+// Persistent kernel: one CTA per SM walks tiles of 128 elements. Warps 0-15
+// (512 threads) gather, split, apply the qdata and write the result: thread t
+// owns element row r = 32 (warp % 4) + lane (its TMEM lane) and part
+// warp / 4 (a quarter) of that row's columns. Warp 16 issues the MMAs (one
+// elected lane), one thread of warp 17 the bulk copies (gather map, table and
+// qdata chunks),
 // each waiting only for what it needs. The tensor pipe
 // runs forward(c + 1) while the CUDA cores apply the qdata of chunk c, and
 // backward(c) while they start chunk c + 1 (two forward accumulators in TMEM).
@@ -116,7 +119,7 @@ struct Shape
 // (bounded) for the work they already started, so that no copy lands in
 // released shared memory and no MMA uses released TMEM.
 template <int D, int Q, int PC>
-__global__ void __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(576, 1)
 diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
                     const float *__restrict__ qT, const float *__restrict__ qscale, const float *__restrict__ x,
                     const int *__restrict__ gmap, int map_bulk, const unsigned char *__restrict__ mask,
@@ -126,24 +129,25 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
    if (skip && *skip) { return; }   // uniform per launch: the solver has finished
    extern __shared__ __align__(1024) unsigned char smem[];
    // mbarriers: map, table ring 0-2, qd (bulk copies); af, ab, dfree0/1,
-   // qfree, out (256 epilogue arrivals); fwd0/1, bwd, tfree0-2 (the ring
+   // qfree, out (one arrival per epilogue thread); fwd0/1, bwd, tfree0-2 (the ring
    // buffer's backward GEMM is done), drain (MMA commits)
    constexpr int NMB = 18;
    __shared__ __align__(8) unsigned long long mb[NMB];
    __shared__ unsigned tmem_base;
-   __shared__ float s_max[2][128];
+   __shared__ float s_max[4][128];
    __shared__ int s_fail;
    unsigned long long *MB_MAP = mb, *MB_T = mb + 1, *MB_QD = mb + 4, *MB_AF = mb + 5;
    unsigned long long *MB_AB = mb + 6, *MB_DFREE = mb + 7, *MB_QFREE = mb + 9, *MB_FWD = mb + 10;
    unsigned long long *MB_BWD = mb + 12, *MB_OUT = mb + 13, *MB_TFREE = mb + 14, *MB_DRAIN = mb + 17;
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int half = (warp >> 2) & 1;
+   const int part = (warp >> 2) & 3;   // epilogue warps 0-15: the part of the row's columns
    const int r = 32 * (warp & 3) + lane;
    const unsigned sbase = smem_u32(smem);
 
    if (tid == 0)
    {
-      const unsigned counts[NMB] = {1, 1, 1, 1, 1, 256, 256, 256, 256, 256, 1, 1, 1, 256, 1, 1, 1, 1};
+      const unsigned E = S::EPI;
+      const unsigned counts[NMB] = {1, 1, 1, 1, 1, E, E, E, E, E, 1, 1, 1, E, 1, 1, 1, 1};
       for (int i = 0; i < NMB; ++i)
       {
          asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb + i)), "r"(counts[i]) : "memory");
@@ -171,7 +175,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
    };
    const int ntiles = (ne + 127) / 128;
 
-   if (warp == 8)
+   if (warp == 16)
    {
       // ----------------------------------------------------- MMA issuer
       // the whole warp runs the loop (waits, descriptors: warp-uniform);
@@ -275,7 +279,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          if (!mbar_wait(MB_DRAIN, 0, 1LL << 20)) { *fail = 1; }
       }
    }
-   else if (warp == 9)
+   else if (warp == 17)
    {
       // ---------------------------------------------------- copy producer
       if (lane == 0)
@@ -372,17 +376,17 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          if (tid == 0) { TC_TRACE(it, 1010); }
          const bool act = e < ne;
          const bool bulk = map_bulk && e0 + 128 <= ne;
-         // ---- gather this thread's half row of x (ElementRestriction::Mult)
+         // ---- gather this thread's part of the row of x (ElementRestriction::Mult)
          if (bulk) { wait(MB_MAP, ph_map); ph_map ^= 1; }
          // all map entries first, then all x loads (unconditional: a slot
          // without a dof reads x[0] and is zeroed by the select), so the
          // loads are in flight together
-         int jj[S::KH];
-         signed char sg[S::KH];
+         int jj[S::KP];
+         signed char sg[S::KP];
 #pragma unroll
-         for (int k = 0; k < S::KH; ++k)
+         for (int k = 0; k < S::KP; ++k)
          {
-            const int i = half * S::KH + k;
+            const int i = part * S::KP + k;
             int g = GBPA_GATHER_SKIP;
             if (act && i < S::D3) { g = bulk ? smap[r * S::D3 + i] : __ldg(gmap + e * S::D3 + i); }
             const bool use = g != GBPA_GATHER_SKIP;
@@ -392,24 +396,24 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          if (mask)
          {
 #pragma unroll
-            for (int k = 0; k < S::KH; ++k)
+            for (int k = 0; k < S::KP; ++k)
             {
                if (__ldg(mask + jj[k])) { sg[k] = 0; }
             }
          }
-         float xv[S::KH];
+         float xv[S::KP];
 #pragma unroll
-         for (int k = 0; k < S::KH; ++k) { xv[k] = __ldg(x + jj[k]); }
+         for (int k = 0; k < S::KP; ++k) { xv[k] = __ldg(x + jj[k]); }
 #pragma unroll
-         for (int k = 0; k < S::KH; ++k) { xv[k] = sg[k] == 0 ? 0.f : (sg[k] > 0 ? xv[k] : -xv[k]); }
+         for (int k = 0; k < S::KP; ++k) { xv[k] = sg[k] == 0 ? 0.f : (sg[k] > 0 ? xv[k] : -xv[k]); }
          float m = 0.f;
 #pragma unroll
-         for (int k = 0; k < S::KH; ++k) { m = fmaxf(m, fabsf(xv[k])); }
-         s_max[half][r] = m;
-         asm volatile("bar.sync 1, 256;" ::: "memory");
+         for (int k = 0; k < S::KP; ++k) { m = fmaxf(m, fabsf(xv[k])); }
+         s_max[part][r] = m;
+         asm volatile("bar.sync 1, %0;" ::"n"(S::EPI) : "memory");
          float sx = 1.f;
          {
-            const float mm = fmaxf(s_max[0][r], s_max[1][r]);
+            const float mm = fmaxf(fmaxf(s_max[0][r], s_max[1][r]), fmaxf(s_max[2][r], s_max[3][r]));
             if (mm > 0.f && mm <= 3.0e38f)
             {
                int ex;
@@ -419,17 +423,17 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          }
          const float so = act ? __ldg(qscale + e) : 1.f;
 #pragma unroll
-         // the x tile's fp16 limbs into TMEM (this thread's half row: KH
-         // values, KH/2 columns per limb); the forward GEMMs read them as A
+         // the x tile's fp16 limbs into TMEM (this thread's part of the row:
+         // KP values, KP/2 columns per limb); the forward GEMMs read them as A
 #pragma unroll
-         for (int g8 = 0; g8 < S::KH / 8; ++g8)
+         for (int g8 = 0; g8 < S::KP / 8; ++g8)
          {
             float v[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) { v[j] = xv[8 * g8 + j] * sx; }
             uint4 hi, lo;
             split8(v, hi, lo);
-            const unsigned col = lane_off + half * (S::KH / 2) + 4 * g8;
+            const unsigned col = lane_off + part * (S::KP / 2) + 4 * g8;
             const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
             tmem_st4(tmem + S::TXH + col, h4);
             tmem_st4(tmem + S::TXL + col, l4);
@@ -442,7 +446,7 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          // ---- chunks: the producer bulk-copies chunk c's qdata (transposed
          // layout: this thread's 6 NP values at stride 128) into shared memory
          // one chunk ahead; it is taken into registers at the chunk's start
-         const float *sq = reinterpret_cast<const float *>(smem + S::OFF_QD) + half * S::NQ * 128 + r;
+         const float *sq = reinterpret_cast<const float *>(smem + S::OFF_QD) + part * S::NQ * 128 + r;
 #pragma unroll 1
          for (int c = 0; c < S::NCH; ++c)
          {
@@ -458,9 +462,9 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             __syncwarp();   // the warp-collective TMEM loads need the converged warp
             fence_after();
             float gq[S::NV];
-            const unsigned tcol = tmem + lane_off + ((c & 1) ? S::TF1 : S::TF0) + half * S::NV;
-#pragma unroll
-            for (int j = 0; j < S::NV; j += 8) { tmem_ld8(tcol + j, gq + j); }
+            const unsigned tcol = tmem + lane_off + ((c & 1) ? S::TF1 : S::TF0) + part * S::NV;
+            tmem_ld8(tcol, gq);
+            tmem_ld4(tcol + 8, gq + 8);
             tmem_wait_ld();
             fence_before();
             arrive(MB_DFREE + (c & 1));
@@ -481,16 +485,18 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
             if (c >= 1) { wait(MB_BWD, ph_bwd); ph_bwd ^= 1; }   // backward(c - 1) has read A_bwd
             __syncwarp();
             if (tid == 0) { TC_TRACE(it, 16 * c + 8); }
-            // the chunk's O limbs into TMEM (NV values, NV/2 columns per limb)
-#pragma unroll
-            for (int jg = 0; jg < S::NV / 8; ++jg)
+            // the chunk's O limbs into TMEM (NV = 12 values, 6 columns per limb)
             {
                uint4 hi, lo;
-               split8(o + 8 * jg, hi, lo);
-               const unsigned col = lane_off + half * (S::NV / 2) + 4 * jg;
+               split8(o, hi, lo);
+               const unsigned col = lane_off + part * (S::NV / 2);
                const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
                tmem_st4(tmem + S::TOH + col, h4);
                tmem_st4(tmem + S::TOL + col, l4);
+               unsigned h2[2], l2[2];
+               split4(o + 8, h2, l2);
+               tmem_st2(tmem + S::TOH + col + 4, h2);
+               tmem_st2(tmem + S::TOL + col + 4, l2);
             }
             tmem_wait_st();
             fence_before();
@@ -504,30 +510,30 @@ diffusion_tc_kernel(int ne, const unsigned char *__restrict__ tab_f,
          fence_after();
          const float inv = 1.f / (sx * so);
 #pragma unroll
-         for (int j = 0; j < S::KH; j += 8)
+         for (int j = 0; j < S::KP; j += 8)
          {
             float v[8];
-            tmem_ld8(tmem + lane_off + S::TB + half * S::KH + j, v);
+            tmem_ld8(tmem + lane_off + S::TB + part * S::KP + j, v);
             tmem_wait_ld();
 #pragma unroll
             for (int k = 0; k < 8; ++k)
             {
-               const int i = half * S::KH + j + k;
+               const int i = part * S::KP + j + k;
                if (i < S::D3) { stg[S::stg(r, i)] = v[k] * inv; }
             }
          }
          fence_before();
-         asm volatile("bar.sync 1, 256;" ::: "memory");
+         asm volatile("bar.sync 1, %0;" ::"n"(S::EPI) : "memory");
          const bool failed = *fail != 0;
          if (S::D3 % 2 == 1 && mode == 0 && !failed && e0 + 128 <= ne && ((uintptr_t)y % 16) == 0)
          {
             // an unswizzled full tile is the contiguous E-vector slice
             const float4 *src = reinterpret_cast<const float4 *>(stg);
             float4 *dst = reinterpret_cast<float4 *>(y + e0 * S::D3);
-            for (int s = tid; s < 128 * S::D3 / 4; s += 256) { dst[s] = src[s]; }
+            for (int s = tid; s < 128 * S::D3 / 4; s += S::EPI) { dst[s] = src[s]; }
          }
          else
-         for (int s = tid; s < 128 * S::D3; s += 256)
+         for (int s = tid; s < 128 * S::D3; s += S::EPI)
          {
             const int el = s / S::D3, i = s - el * S::D3;
             const long long ee = e0 + el;
@@ -627,8 +633,8 @@ int launch_qscale(gbpa_ctx *ctx, int ne, int Q, const float *qd, float R, float 
    return last_launch(ctx, "tc_qscale");
 }
 
-// qdata (Q^3, 6, NE) -> the kernel's tile layout: for tile t, chunk c, half h,
-// value k = 6 p + s (point q = c PC + h NP + p, symmetric entry s) the 128
+// qdata (Q^3, 6, NE) -> the kernel's tile layout: for tile t, chunk c, part h
+// of the row, value k = 6 p + s (point q = c PC + h NP + p, symmetric entry s) the 128
 // elements of the tile are consecutive; padded points and elements are zero.
 template <int D, int Q, int PC>
 __global__ void transpose_qdata_kernel(int ne, const float *__restrict__ qd, float *__restrict__ qT, int64_t n)
@@ -640,7 +646,7 @@ __global__ void transpose_qdata_kernel(int ne, const float *__restrict__ qd, flo
       const int r = (int)(i % 128);
       int64_t t = i / 128;
       const int k = (int)(t % S::NQ); t /= S::NQ;
-      const int h = (int)(t % 2); t /= 2;
+      const int h = (int)(t % S::PARTS); t /= S::PARTS;
       const int c = (int)(t % S::NCH);
       const int64_t tile = t / S::NCH;
       const int p = k / 6, sidx = k % 6;
@@ -696,7 +702,7 @@ static int launch_t(gbpa_ctx *ctx, int ne, const Tables &t, const float *qT, con
    int map_bulk = ((uintptr_t)gmap % 16) == 0 ? 1 : 0;
    void *args[] = {&ne, (void *)&tf, (void *)&qT, (void *)&qscale, (void *)&x, (void *)&gmap,
                    &map_bulk, (void *)&mask, &y, &mode, (void *)&skip, &flags};
-   return launch_generic(ctx, k, dim3(grid), dim3(320), args, S::SMEM, "diffusion_tc");
+   return launch_generic(ctx, k, dim3(grid), dim3(576), args, S::SMEM, "diffusion_tc");
 }
 
 int launch_diffusion_f32(gbpa_ctx *ctx, int ne, int D, int Q, const Tables &t, const float *qd,

@@ -90,6 +90,21 @@ __device__ __forceinline__ void tmem_st4(unsigned taddr, const unsigned *v)
    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};"
                 ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]) : "memory");
 }
+// 4 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float *v)
+{
+   unsigned r[4];
+   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                : "r"(taddr));
+#pragma unroll
+   for (int j = 0; j < 4; ++j) { v[j] = __uint_as_float(r[j]); }
+}
+// 2 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_st2(unsigned taddr, const unsigned *v)
+{
+   asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(taddr), "r"(v[0]), "r"(v[1]) : "memory");
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -131,6 +146,20 @@ __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
    }
    hi = make_uint4(h[0], h[1], h[2], h[3]);
    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// v -> (hi, lo) fp16 limbs of 4 consecutive values, two per 32-bit word
+__device__ __forceinline__ void split4(const float *v, unsigned *hi, unsigned *lo)
+{
+#pragma unroll
+   for (int q = 0; q < 2; ++q)
+   {
+      const __half h0 = __float2half_rn(v[2 * q]), h1 = __float2half_rn(v[2 * q + 1]);
+      const __half l0 = __float2half_rn(v[2 * q] - __half2float(h0));
+      const __half l1 = __float2half_rn(v[2 * q + 1] - __half2float(h1));
+      hi[q] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
+      lo[q] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
+   }
 }
 
 // Host: the Kronecker matrix of the 1D tables, K[3q+c][i] (row 3q+c, q = qx
