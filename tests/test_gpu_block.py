@@ -44,13 +44,23 @@ def test_block_mult_equals_single(R, prec):
     X = (torch.rand(n, R, dtype=torch.float64, device="cuda", generator=gen) - 0.5).to(dt).contiguous()
     Y = torch.empty_like(X)
     assert d.lib.gbpa_operator_mult_block(op.handle, R, P(X), P(Y)) == 0
-    for r in range(R):
-        y = torch.empty(n, dtype=dt, device="cuda")
-        op.Mult(X[:, r].contiguous(), y)
-        if prec == 0:
-            assert torch.equal(Y[:, r], y)
-        else:
-            assert float(torch.linalg.norm(Y[:, r] - y) / torch.linalg.norm(y)) < 1e-6
+    # the single applies in the block kernel's family: at this order (no
+    # tensor-core block kernel) the CUDA-core one, whatever the FP32 default
+    D, Q = integ.D, integ.Q
+    nb = ctypes.c_int(0)
+    prev = d.lib.gbpa_get_apply_layout(0, prec, D, Q, ctypes.byref(nb))
+    if prec == 1 and d.lib.gbpa_get_block_apply_layout(D, Q, R) == 0:
+        assert d.lib.gbpa_set_apply_layout(0, 1, D, Q, 0, 0) == 0
+    try:
+        for r in range(R):
+            y = torch.empty(n, dtype=dt, device="cuda")
+            op.Mult(X[:, r].contiguous(), y)
+            if prec == 0:
+                assert torch.equal(Y[:, r], y)
+            else:
+                assert float(torch.linalg.norm(Y[:, r] - y) / torch.linalg.norm(y)) < 1e-6
+    finally:
+        d.lib.gbpa_set_apply_layout(0, prec, D, Q, prev, nb.value)
 
 
 @pytest.mark.parametrize("R", [1, 2, 4, 8])
