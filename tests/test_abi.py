@@ -130,3 +130,42 @@ def test_host_restriction_build_rejects_out_of_range(lib):
     off = np.zeros(5, np.int32); ind = np.zeros(4, np.int32); gm = np.zeros(4, np.int32)
     P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     assert lib.gbpa_restriction_build(1, 4, 4, P(ed), None, P(off), P(ind), P(gm)) == -9
+
+
+def test_block_layout_switch_without_gpu(lib):
+    """The FP32 block apply's kernel choice is host state: the tensor-core
+    block kernel by default where one exists ((5,6) and (6,7), 8 vectors),
+    the CUDA-core kernel elsewhere; TC is refused where no kernel exists and
+    any other layout is an invalid argument."""
+    TC = 2
+    assert lib.gbpa_get_block_apply_layout(6, 7, 8) == TC
+    assert lib.gbpa_get_block_apply_layout(5, 6, 8) == TC
+    assert lib.gbpa_get_block_apply_layout(4, 5, 8) == 0
+    assert lib.gbpa_get_block_apply_layout(6, 7, 2) == 0
+    assert lib.gbpa_set_block_apply_layout(4, 5, 8, TC) == -2
+    assert lib.gbpa_set_block_apply_layout(6, 7, 8, 1) == -1
+    assert lib.gbpa_set_block_apply_layout(6, 7, 0, 0) == -1
+    assert lib.gbpa_get_block_apply_layout(17, 18, 8) == -1
+    assert lib.gbpa_set_block_apply_layout(6, 7, 8, 0) == 0
+    try:
+        assert lib.gbpa_get_block_apply_layout(6, 7, 8) == 0
+    finally:
+        assert lib.gbpa_set_block_apply_layout(6, 7, 8, TC) == 0
+    assert lib.gbpa_get_block_apply_layout(6, 7, 8) == TC
+
+
+def test_host_operator_create_rejects_bad_arguments_without_gpu(lib):
+    """gbpa_operator_create_host validates before touching the GPU: no
+    context or descriptor, bad kind or precision, negative sizes, and a
+    missing array are all GBPA_ERR_INVALID_ARGUMENT."""
+    import ctypes
+    from mfem_gb300 import _lib
+    op = ctypes.c_void_p()
+    assert lib.gbpa_operator_create_host(None, None, ctypes.byref(op)) == -1
+    d = _lib.OperatorDesc(0, 0, 1, 8, 2, 3, 1, None, None, None, None, None, None, None, 0, 0)
+    fake_ctx = ctypes.c_void_p(1)   # never dereferenced: the descriptor is refused first
+    assert lib.gbpa_operator_create_host(fake_ctx, ctypes.byref(d), ctypes.byref(op)) == -1   # arrays missing
+    for field, value in (("kind", 7), ("precision", 9), ("ne", -1), ("d1d", 0)):
+        bad = _lib.OperatorDesc(0, 0, 1, 8, 2, 3, 1, None, None, None, None, None, None, None, 0, 0)
+        setattr(bad, field, value)
+        assert lib.gbpa_operator_create_host(fake_ctx, ctypes.byref(bad), ctypes.byref(op)) == -1, field
