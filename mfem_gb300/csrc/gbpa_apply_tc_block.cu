@@ -54,11 +54,13 @@ struct BShape
 {
    static constexpr int D3 = D * D * D;
    static constexpr int KF = (D3 + 15) / 16 * 16;   // dofs, padded to the MMA K step
-   static constexpr int KH = KF / 2;                // dofs per half row
+   static constexpr int PARTS = 4;                  // epilogue threads per GEMM row
+   static constexpr int EPI = 128 * PARTS;          // epilogue threads (16 warps)
+   static constexpr int KH = KF / PARTS;            // dofs per part of a row
    static constexpr int Q3 = Q * Q * Q;
    static constexpr int NC = 3 * PC;                // chunk columns
    static constexpr int NCH = (Q3 + PC - 1) / PC;   // chunks
-   static constexpr int NP = PC / 2;                // points of a chunk per thread
+   static constexpr int NP = PC / PARTS;            // points of a chunk per thread
    static constexpr int NV = 3 * NP;                // chunk columns per thread
    static constexpr int NQ = 6 * NP;                // qdata values per thread and chunk
    static constexpr int M = 128;                    // GEMM rows per tile
@@ -66,8 +68,8 @@ struct BShape
    static constexpr int XL_BYTES = M * KF * 2;      // the x tile's lo limb
    static constexpr int BF_LIMB = NC * KF * 2;      // one limb of a table chunk
    static constexpr int NT = 3;                     // table ring depth
-   static constexpr int QD_BYTES = 2 * NQ * EL * 4; // one tile-chunk of qdata, [half][k][element]
-   static constexpr int QT_CHUNK = 2 * NQ * EL;     // its floats
+   static constexpr int QD_BYTES = PARTS * NQ * EL * 4; // one tile-chunk of qdata, [part][k][element]
+   static constexpr int QT_CHUNK = PARTS * NQ * EL; // its floats
    static constexpr int OFF_XL = 0;
    static constexpr int OFF_T = OFF_XL + XL_BYTES;
    static constexpr int OFF_QD = OFF_T + NT * 2 * BF_LIMB;
@@ -79,7 +81,7 @@ struct BShape
    static __device__ __forceinline__ int off_t(int c) { return OFF_T + (c % NT) * 2 * BF_LIMB; }
    static_assert(M % R == 0 && R <= 32 && 32 % R == 0, "rows of one element stay in one warp");
    static_assert(KF <= TF0 && TF0 + NC <= TF1 && TF1 + NC <= TXH && TOL + NC / 2 <= 512, "TMEM columns");
-   static_assert(KF <= 256 && NC <= 64 && NC % 16 == 0 && NV % 8 == 0 && KH % 16 == 0, "MMA shapes");
+   static_assert(KF <= 256 && NC <= 64 && NC % 16 == 0 && NV == 12 && KH % 8 == 0, "MMA shapes");
    static_assert(NCH % 2 == 0 && NCH >= NT, "the chunk loop is unrolled by two");
    static_assert(SMEM <= 222 * 1024, "shared memory");
    static_assert(QD_BYTES % 16 == 0 && BF_LIMB % 16 == 0, "bulk copy sizes");
@@ -88,9 +90,10 @@ struct BShape
 };
 
 // Persistent kernel: one CTA per SM walks tiles of EL elements x R vectors.
-// Warps 0-7 gather, split, apply the qdata and store (thread: row r = 32
-// (warp % 4) + lane, half of the row's columns = warp / 4); warp 8 issues the
-// MMAs (one elected lane), lane 0 of warp 9 the bulk copies (table chunks into
+// Warps 0-15 gather, split, apply the qdata and store (thread: row r = 32
+// (warp % 4) + lane, part warp / 4 -- a quarter -- of the row's columns);
+// warp 16 issues the MMAs (one elected lane), lane 0 of warp 17 the bulk
+// copies (table chunks into
 // a ring of three, qdata chunks into two buffers, each refilled once the chunk
 // it held is released). A barrier that could complete twice before one of
 // its waiters looks is kept per buffer (tfree, dfree, fwd, qd, qfree), so
@@ -100,7 +103,7 @@ struct BShape
 // copy producer wait (bounded) for their work in flight before the CTA
 // releases TMEM and exits.
 template <int D, int Q, int PC, int R>
-__global__ void __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(576, 1)
 diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const float *__restrict__ qT,
                           const float *__restrict__ qscale, const float *__restrict__ x,
                           const int *__restrict__ gmap, const unsigned char *__restrict__ mask,
@@ -110,24 +113,25 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
    if (skip && *skip) { return; }
    extern __shared__ __align__(1024) unsigned char smem[];
    // mbarriers: table ring 0-2, qdata 0-1 (bulk copies); af, ab, dfree0/1,
-   // qfree0/1 (256 epilogue arrivals); fwd0/1, bwd, tfree0-2, drain (MMA
+   // qfree0/1 (one arrival per epilogue thread); fwd0/1, bwd, tfree0-2, drain (MMA
    // commits)
    constexpr int NMB = 18;
    __shared__ __align__(8) unsigned long long mb[NMB];
    __shared__ unsigned tmem_base;
-   __shared__ float s_max[2][128];
+   __shared__ float s_max[4][128];
    __shared__ int s_fail;
    unsigned long long *MB_T = mb, *MB_QD = mb + 3, *MB_AF = mb + 5, *MB_AB = mb + 6, *MB_DFREE = mb + 7;
    unsigned long long *MB_QFREE = mb + 9, *MB_FWD = mb + 11, *MB_BWD = mb + 13, *MB_TFREE = mb + 14;
    unsigned long long *MB_DRAIN = mb + 17;
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int half = (warp >> 2) & 1;
+   const int part = (warp >> 2) & 3;   // epilogue warps 0-15: the part of the row's columns
    const int r = 32 * (warp & 3) + lane;
    const unsigned sbase = smem_u32(smem);
 
    if (tid == 0)
    {
-      const unsigned counts[NMB] = {1, 1, 1, 1, 1, 256, 256, 256, 256, 256, 256, 1, 1, 1, 1, 1, 1, 1};
+      const unsigned E = S::EPI;
+      const unsigned counts[NMB] = {1, 1, 1, 1, 1, E, E, E, E, E, E, 1, 1, 1, 1, 1, 1, 1};
       for (int i = 0; i < NMB; ++i)
       {
          asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb + i)), "r"(counts[i]) : "memory");
@@ -155,7 +159,7 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
    };
    const int ntiles = (ne + S::EL - 1) / S::EL;
 
-   if (warp == 8)
+   if (warp == 16)
    {
       // ----------------------------------------------------- MMA issuer
       constexpr uint32_t ID_F = instr_desc(128, S::NC), ID_B = instr_desc(128, S::KF, true);
@@ -249,7 +253,7 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
       __syncwarp();
       if (!mbar_wait(MB_DRAIN, 0, 1LL << 20)) { *fail = 1; }
    }
-   else if (warp == 9)
+   else if (warp == 17)
    {
       // ---------------------------------------------------- copy producer
       if (lane == 0)
@@ -313,7 +317,7 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
       // this thread's 16-byte core-matrix row in a K-major shared operand of
       // 128 rows: k group kg of row r
       auto core_row = [&](int kg) { return (kg * (S::M / 8) + (r >> 3)) * 128 + (r & 7) * 16; };
-      const unsigned traw = tmem + lane_off + S::TB + half * S::KH;   // raw x staging (a tile's start)
+      const unsigned traw = tmem + lane_off + S::TB + part * S::KH;   // raw x staging (a tile's start)
       int it = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it)
       {
@@ -324,14 +328,14 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
          // ---- gather (ElementRestriction::Mult for R interleaved vectors):
          // batches of GW dofs, the next batch's map entries in flight while
          // this batch's values load; raw values into the result columns
-         constexpr int GW = 32;
+         constexpr int GW = 16;
          constexpr int NB = (S::KH + GW - 1) / GW;
-         const int *grow = gmap + e * S::D3 + half * S::KH;
+         const int *grow = gmap + e * S::D3 + part * S::KH;
          auto map_batch = [&](int g, int *gg) {
 #pragma unroll
             for (int j = 0; j < GW; ++j)
             {
-               const int k = GW * g + j, i = half * S::KH + k;
+               const int k = GW * g + j, i = part * S::KH + k;
                gg[j] = (act && k < S::KH && i < S::D3) ? __ldg(grow + k) : GBPA_GATHER_SKIP;
             }
          };
@@ -371,11 +375,11 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
             for (int j = 0; j < GW; ++j) { gcur[j] = gnext[j]; }
          }
          if (tid == 0) { TCB_TRACE(it, 1001); }
-         s_max[half][r] = m;
-         asm volatile("bar.sync 1, 256;" ::: "memory");
+         s_max[part][r] = m;
+         asm volatile("bar.sync 1, %0;" ::"n"(S::EPI) : "memory");
          float sx = 1.f;
          {
-            const float mm = fmaxf(s_max[0][r], s_max[1][r]);
+            const float mm = fmaxf(fmaxf(s_max[0][r], s_max[1][r]), fmaxf(s_max[2][r], s_max[3][r]));
             if (mm > 0.f && mm <= 3.0e38f)
             {
                int ex;
@@ -397,8 +401,8 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
             uint4 hi, lo;
             split8(v, hi, lo);
             const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w};
-            tmem_st4(tmem + lane_off + S::TXH + half * (S::KH / 2) + 4 * g8, h4);
-            *reinterpret_cast<uint4 *>(smem + S::OFF_XL + core_row(half * (S::KH / 8) + g8)) = lo;
+            tmem_st4(tmem + lane_off + S::TXH + part * (S::KH / 2) + 4 * g8, h4);
+            *reinterpret_cast<uint4 *>(smem + S::OFF_XL + core_row(part * (S::KH / 8) + g8)) = lo;
          }
          tmem_wait_st();
          fence_before();
@@ -412,14 +416,14 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
          // during the previous chunk.
          const long long enx = e + (long long)gridDim.x * S::EL;   // this row's element in the next tile
          const bool pf = tile + (int)gridDim.x < ntiles && enx < ne;
-         const int *gnrow = gmap + enx * S::D3 + half * S::KH;
+         const int *gnrow = gmap + enx * S::D3 + part * S::KH;
          int pm[8];
          auto chunk = [&](int c, int b) {
             // b = c & 1 (compile-time in each unrolled copy)
             wait(MB_QD + b, ph_qd[b]); ph_qd[b] ^= 1;
             if (tid == 0) { TCB_TRACE(it, 16 * c + 5); }
             const float *sq = reinterpret_cast<const float *>(smem + S::OFF_QD + b * S::QD_BYTES) +
-                              half * S::NQ * S::EL + el;
+                              part * S::NQ * S::EL + el;
             float qc[S::NQ];
 #pragma unroll
             for (int k = 0; k < S::NQ; ++k) { qc[k] = sq[k * S::EL]; }
@@ -442,7 +446,7 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
                   for (int j = 0; j < 8; ++j)
                   {
                      const int k = 8 * c + j;
-                     pm[j] = half * S::KH + k < S::D3 ? __ldg(gnrow + k) : GBPA_GATHER_SKIP;
+                     pm[j] = part * S::KH + k < S::D3 ? __ldg(gnrow + k) : GBPA_GATHER_SKIP;
                   }
                }
             }
@@ -451,9 +455,9 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
             __syncwarp();   // the warp-collective TMEM loads need the converged warp
             fence_after();
             float gq[S::NV];
-            const unsigned tcol = tmem + lane_off + (b ? S::TF1 : S::TF0) + half * S::NV;
-#pragma unroll
-            for (int j = 0; j < S::NV; j += 8) { tmem_ld8(tcol + j, gq + j); }
+            const unsigned tcol = tmem + lane_off + (b ? S::TF1 : S::TF0) + part * S::NV;
+            tmem_ld8(tcol, gq);
+            tmem_ld4(tcol + 8, gq + 8);
             tmem_wait_ld();
             fence_before();
             arrive(MB_DFREE + b);
@@ -474,15 +478,18 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
             if (c >= 1) { wait(MB_BWD, ph_bwd); ph_bwd ^= 1; }
             if (tid == 0) { TCB_TRACE(it, 16 * c + 8); }
             __syncwarp();
-#pragma unroll
-            for (int jg = 0; jg < S::NV / 8; ++jg)
             {
+               // 12 values: 6 columns per limb
                uint4 hi, lo;
-               split8(o + 8 * jg, hi, lo);
-               const unsigned col = lane_off + half * (S::NV / 2) + 4 * jg;
+               split8(o, hi, lo);
+               const unsigned col = lane_off + part * (S::NV / 2);
                const unsigned h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
                tmem_st4(tmem + S::TOH + col, h4);
                tmem_st4(tmem + S::TOL + col, l4);
+               unsigned h2[2], l2[2];
+               split4(o + 8, h2, l2);
+               tmem_st2(tmem + S::TOH + col + 4, h2);
+               tmem_st2(tmem + S::TOL + col + 4, l2);
             }
             tmem_wait_st();
             fence_before();
@@ -508,12 +515,12 @@ diffusion_tc_block_kernel(int ne, const unsigned char *__restrict__ tab_f, const
          for (int j = 0; j < S::KH; j += 8)
          {
             float v[8];
-            tmem_ld8(tmem + lane_off + S::TB + half * S::KH + j, v);
+            tmem_ld8(tmem + lane_off + S::TB + part * S::KH + j, v);
             tmem_wait_ld();
 #pragma unroll
             for (int k = 0; k < 8; ++k)
             {
-               const int i = half * S::KH + j + k;
+               const int i = part * S::KH + j + k;
                if (act && i < S::D3) { yrow[i * R] = v[k] * inv; }
             }
          }
@@ -568,7 +575,7 @@ int build_block_tables(int D, int Q, const double *B, const double *G, Tables *t
 }
 
 // qdata (Q^3, 6, NE) -> the block kernel's layout: tile t (EL elements),
-// chunk c, half h, value k = 6 p + s (point q = c PC + h NP + p, symmetric
+// chunk c, part h of the row, value k = 6 p + s (point q = c PC + h NP + p, symmetric
 // entry s), element el of the tile; padded points and elements are zero.
 template <int D, int Q, int PC, int R>
 __global__ void transpose_qdata_block_kernel(int ne, const float *__restrict__ qd, float *__restrict__ qT, int64_t n)
@@ -579,7 +586,7 @@ __global__ void transpose_qdata_block_kernel(int ne, const float *__restrict__ q
       const int el = (int)(i % S::EL);
       int64_t t = i / S::EL;
       const int k = (int)(t % S::NQ); t /= S::NQ;
-      const int h = (int)(t % 2); t /= 2;
+      const int h = (int)(t % S::PARTS); t /= S::PARTS;
       const int c = (int)(t % S::NCH);
       const int64_t tile = t / S::NCH;
       const int p = k / 6, sidx = k % 6;
@@ -630,7 +637,7 @@ static int launch_block_t(gbpa_ctx *ctx, int ne, const Tables &t, const float *q
    int *flags = ctx->d_flags;
    void *args[] = {&ne, (void *)&tf, (void *)&qT, (void *)&qscale, (void *)&x, (void *)&gmap,
                    (void *)&mask, &y, (void *)&skip, &flags};
-   return launch_generic(ctx, k, dim3(grid), dim3(320), args, S::SMEM, "diffusion_tc_block");
+   return launch_generic(ctx, k, dim3(grid), dim3(576), args, S::SMEM, "diffusion_tc_block");
 }
 
 int launch_diffusion_block_f32(gbpa_ctx *ctx, int ne, int D, int Q, int nrhs, const Tables &t, const float *qT,
