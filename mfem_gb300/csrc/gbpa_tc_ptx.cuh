@@ -129,37 +129,34 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, unsigned 
                 ::"r"(smem_u32(sdst)), "l"(gsrc), "r"(bytes), "r"(smem_u32(bar)) : "memory");
 }
 
+// (v0, v1) -> one 32-bit word of each fp16 limb, v0 in the low half:
+// hi = fp16(v), lo = fp16(v - hi), both rounded to nearest even (one paired
+// conversion per limb; the same bits as converting each value on its own)
+__device__ __forceinline__ void split2(float v0, float v1, unsigned &hi, unsigned &lo)
+{
+   const __half2 h = __floats2half2_rn(v0, v1);
+   const float2 hf = __half22float2(h);
+   const __half2 l = __floats2half2_rn(v0 - hf.x, v1 - hf.y);
+   hi = *reinterpret_cast<const unsigned *>(&h);
+   lo = *reinterpret_cast<const unsigned *>(&l);
+}
+
 // v -> (hi, lo) fp16 limbs of 8 consecutive values, two per 32-bit word
 // (the lower k in the low half): one 16-byte core-matrix row, or four TMEM
 // columns of an A operand
 __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
 {
-   unsigned h[4], l[4];
-#pragma unroll
-   for (int q = 0; q < 4; ++q)
-   {
-      const __half h0 = __float2half_rn(v[2 * q]), h1 = __float2half_rn(v[2 * q + 1]);
-      const __half l0 = __float2half_rn(v[2 * q] - __half2float(h0));
-      const __half l1 = __float2half_rn(v[2 * q + 1] - __half2float(h1));
-      h[q] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
-      l[q] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
-   }
-   hi = make_uint4(h[0], h[1], h[2], h[3]);
-   lo = make_uint4(l[0], l[1], l[2], l[3]);
+   split2(v[0], v[1], hi.x, lo.x);
+   split2(v[2], v[3], hi.y, lo.y);
+   split2(v[4], v[5], hi.z, lo.z);
+   split2(v[6], v[7], hi.w, lo.w);
 }
 
 // v -> (hi, lo) fp16 limbs of 4 consecutive values, two per 32-bit word
 __device__ __forceinline__ void split4(const float *v, unsigned *hi, unsigned *lo)
 {
-#pragma unroll
-   for (int q = 0; q < 2; ++q)
-   {
-      const __half h0 = __float2half_rn(v[2 * q]), h1 = __float2half_rn(v[2 * q + 1]);
-      const __half l0 = __float2half_rn(v[2 * q] - __half2float(h0));
-      const __half l1 = __float2half_rn(v[2 * q + 1] - __half2float(h1));
-      hi[q] = (unsigned)__half_as_ushort(h0) | ((unsigned)__half_as_ushort(h1) << 16);
-      lo[q] = (unsigned)__half_as_ushort(l0) | ((unsigned)__half_as_ushort(l1) << 16);
-   }
+   split2(v[0], v[1], hi[0], lo[0]);
+   split2(v[2], v[3], hi[1], lo[1]);
 }
 
 // Host: the Kronecker matrix of the 1D tables, K[3q+c][i] (row 3q+c, q = qx
